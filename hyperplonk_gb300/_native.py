@@ -1,0 +1,94 @@
+"""ctypes binding of libhp_cuda.so (the C ABI in include/hp_cuda.h).
+
+This is the Python counterpart of the reference's Rust FFI block
+(backend/src/ascend910b3/ffi.rs:34-173).  Loading fails loudly when the
+library has not been built: there is no CPU fallback behind this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import pathlib
+
+_LIB_PATH = pathlib.Path(__file__).resolve().parent / "_build" / "libhp_cuda.so"
+
+c_size = ctypes.c_size_t
+c_u8p = ctypes.POINTER(ctypes.c_uint8)
+c_voidp = ctypes.c_void_p
+c_voidpp = ctypes.POINTER(ctypes.c_void_p)
+c_sizep = ctypes.POINTER(ctypes.c_size_t)
+
+
+class Status(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("native_code", ctypes.c_int32)]
+
+
+# name -> argument types (all return Status)
+SIGNATURES: dict[str, list] = {
+    "hp_cuda_v1_context_create": [ctypes.c_int32, c_voidpp],
+    "hp_cuda_v1_context_destroy": [c_voidp],
+    "hp_cuda_v1_buffer_retire": [c_voidp, c_voidp],
+    "hp_cuda_v1_context_stream": [c_voidp, c_voidpp],
+    "hp_cuda_v1_mle_upload": [c_voidp, c_size, c_u8p, c_size, c_voidpp],
+    "hp_cuda_v1_mle_download": [c_voidp, c_voidp, c_size, c_u8p, c_size],
+    "hp_cuda_v1_mle_linear_combination": [c_voidp, c_size, c_voidpp, c_u8p, c_size, c_voidpp],
+    "hp_cuda_v1_mle_evaluate": [c_voidp, c_voidp, c_size, c_u8p, c_u8p],
+    "hp_cuda_v1_mle_build_eq_x_r": [c_voidp, c_u8p, c_size, c_voidpp],
+    "hp_cuda_v1_mle_compute_frac_poly": [c_voidp, c_size, c_voidpp, c_voidpp, c_size, c_voidpp],
+    "hp_cuda_v1_mle_compute_product_poly": [c_voidp, c_voidp, c_size, c_voidpp],
+    "hp_cuda_v1_mle_compute_nums_and_denoms": [c_voidp, c_size, c_u8p, c_u8p, c_voidpp, c_voidpp,
+                                               c_voidpp, c_size, c_voidpp, c_voidpp],
+    "hp_cuda_v1_mle_compute_product_factors": [c_voidp, c_voidp, c_voidp, c_size, c_voidpp, c_voidpp],
+    "hp_cuda_v1_multilinear_kzg_params_create": [c_voidp, c_size, c_voidpp],
+    "hp_cuda_v1_multilinear_kzg_params_upload_layer": [c_voidp, c_voidp, c_size, c_u8p, c_size],
+    "hp_cuda_v1_multilinear_kzg_params_destroy": [c_voidp, c_voidp],
+    "hp_cuda_v1_multilinear_kzg_commit": [c_voidp, c_voidp, c_voidp, c_size, c_u8p],
+    "hp_cuda_v1_multilinear_kzg_multi_commit": [c_voidp, c_voidp, c_voidpp, c_sizep, c_size, c_u8p],
+    "hp_cuda_v1_multilinear_kzg_open": [c_voidp, c_voidp, c_voidp, c_size, c_u8p, c_u8p, c_u8p],
+    "hp_cuda_v1_sumcheck_prover_state_create": [c_voidp, c_size, c_size, c_voidpp, c_size, c_u8p,
+                                                c_sizep, c_size, c_sizep, c_size, c_voidpp],
+    "hp_cuda_v1_sumcheck_prover_state_round": [c_voidp, c_voidp, c_u8p, c_u8p, c_size],
+    "hp_cuda_v1_sumcheck_prover_state_destroy": [c_voidp, c_voidp],
+    "hp_cuda_v1_sumcheck_prover_state_final_evaluations": [c_voidp, c_voidp, c_u8p, c_u8p, c_size],
+}
+
+_lib = None
+
+
+def library_path() -> pathlib.Path:
+    return _LIB_PATH
+
+
+def load() -> ctypes.CDLL:
+    """Load libhp_cuda.so and bind every declared entry point."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not _LIB_PATH.exists():
+        raise RuntimeError(
+            f"{_LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+            "(the CUDA backend has no CPU fallback)")
+    lib = ctypes.CDLL(str(_LIB_PATH))
+    for name, argtypes in SIGNATURES.items():
+        fn = getattr(lib, name, None)
+        if fn is None:
+            continue  # entry not compiled into this build; calling it raises AttributeError
+        fn.argtypes = argtypes
+        fn.restype = Status
+    _lib = lib
+    return lib
+
+
+def exported_symbols() -> list[str]:
+    lib = load()
+    return [n for n in SIGNATURES if getattr(lib, n, None) is not None]
+
+
+def buf(data) -> ctypes.Array:
+    """A ctypes uint8 view of a bytes-like object (no copy for bytearray/numpy)."""
+    if data is None:
+        return None
+    if isinstance(data, (bytes,)):
+        return ctypes.cast(ctypes.c_char_p(data), c_u8p)
+    import numpy as np
+    arr = np.ascontiguousarray(np.frombuffer(data, dtype=np.uint8)) if not isinstance(data, np.ndarray) else data
+    return arr.ctypes.data_as(c_u8p)

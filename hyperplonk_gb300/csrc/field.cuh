@@ -1,0 +1,302 @@
+// field.cuh -- BLS12-381 Fr (8 x 32-bit limbs) and Fq (12 x 32-bit limbs)
+// Montgomery arithmetic for sm_103a, register resident, carry chains in PTX.
+//
+// Storage on the device is Montgomery form with R = 2^256 (Fr) / 2^384 (Fq),
+// little-endian 32-bit limbs, so one Fr element is 32 contiguous bytes and one
+// Fq element 48.  This matches the reference's field semantics (arkworks
+// ark-bls12-381 0.6.0 Fr/Fq, canonical packets backend/src/ascend910b3/
+// encoding.rs:12-108); the limb layout is this library's own.
+#pragma once
+#include <cstdint>
+
+namespace hp {
+
+// ---------------------------------------------------------------------------
+// PTX carry-chain primitives.  Each is one SASS integer instruction; they are
+// asm volatile so the carry flag flows between consecutive calls unchanged.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t add_cc(uint32_t a, uint32_t b) {
+    uint32_t r; asm volatile("add.cc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b)); return r;
+}
+__device__ __forceinline__ uint32_t addc_cc(uint32_t a, uint32_t b) {
+    uint32_t r; asm volatile("addc.cc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b)); return r;
+}
+__device__ __forceinline__ uint32_t addc(uint32_t a, uint32_t b) {
+    uint32_t r; asm volatile("addc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b)); return r;
+}
+__device__ __forceinline__ uint32_t sub_cc(uint32_t a, uint32_t b) {
+    uint32_t r; asm volatile("sub.cc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b)); return r;
+}
+__device__ __forceinline__ uint32_t subc_cc(uint32_t a, uint32_t b) {
+    uint32_t r; asm volatile("subc.cc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b)); return r;
+}
+__device__ __forceinline__ uint32_t subc(uint32_t a, uint32_t b) {
+    uint32_t r; asm volatile("subc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b)); return r;
+}
+__device__ __forceinline__ uint32_t mad_lo_cc(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t r; asm volatile("mad.lo.cc.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c)); return r;
+}
+__device__ __forceinline__ uint32_t madc_lo_cc(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t r; asm volatile("madc.lo.cc.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c)); return r;
+}
+__device__ __forceinline__ uint32_t mad_hi_cc(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t r; asm volatile("mad.hi.cc.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c)); return r;
+}
+__device__ __forceinline__ uint32_t madc_hi_cc(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t r; asm volatile("madc.hi.cc.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c)); return r;
+}
+
+// ---------------------------------------------------------------------------
+// Moduli.  P: modulus limbs, INV: -P^-1 mod 2^32, ONE: R mod P, R2: R^2 mod P.
+// ---------------------------------------------------------------------------
+struct FrParams {
+    static constexpr int N = 8;
+    static constexpr uint32_t INV = 0xffffffffu;
+    __device__ __forceinline__ static uint32_t p(int i) {
+        constexpr uint32_t P[8] = {0x00000001u, 0xffffffffu, 0xfffe5bfeu, 0x53bda402u,
+                                   0x09a1d805u, 0x3339d808u, 0x299d7d48u, 0x73eda753u};
+        return P[i];
+    }
+    __device__ __forceinline__ static uint32_t one(int i) {
+        constexpr uint32_t R[8] = {0xfffffffeu, 0x00000001u, 0x00034802u, 0x5884b7fau,
+                                   0xecbc4ff5u, 0x998c4fefu, 0xacc5056fu, 0x1824b159u};
+        return R[i];
+    }
+    __device__ __forceinline__ static uint32_t r2(int i) {
+        constexpr uint32_t R2[8] = {0xf3f29c6du, 0xc999e990u, 0x87925c23u, 0x2b6cedcbu,
+                                    0x7254398fu, 0x05d31496u, 0x9f59ff11u, 0x0748d9d9u};
+        return R2[i];
+    }
+};
+
+struct FqParams {
+    static constexpr int N = 12;
+    static constexpr uint32_t INV = 0xfffcfffdu;
+    __device__ __forceinline__ static uint32_t p(int i) {
+        constexpr uint32_t P[12] = {0xffffaaabu, 0xb9feffffu, 0xb153ffffu, 0x1eabfffeu,
+                                    0xf6b0f624u, 0x6730d2a0u, 0xf38512bfu, 0x64774b84u,
+                                    0x434bacd7u, 0x4b1ba7b6u, 0x397fe69au, 0x1a0111eau};
+        return P[i];
+    }
+    __device__ __forceinline__ static uint32_t one(int i) {
+        constexpr uint32_t R[12] = {0x0002fffdu, 0x76090000u, 0xc40c0002u, 0xebf4000bu,
+                                    0x53c758bau, 0x5f489857u, 0x70525745u, 0x77ce5853u,
+                                    0xa256ec6du, 0x5c071a97u, 0xfa80e493u, 0x15f65ec3u};
+        return R[i];
+    }
+    __device__ __forceinline__ static uint32_t r2(int i) {
+        constexpr uint32_t R2[12] = {0x1c341746u, 0xf4df1f34u, 0x09d104f1u, 0x0a76e6a6u,
+                                     0x4c95b6d5u, 0x8de5476cu, 0x939d83c0u, 0x67eb88a9u,
+                                     0xb519952du, 0x9a793e85u, 0x92cae3aau, 0x11988fe5u};
+        return R2[i];
+    }
+};
+
+template <class P>
+struct Field {
+    static constexpr int N = P::N;
+    uint32_t v[N];
+
+    __host__ __device__ __forceinline__ static Field zero() {
+        Field r;
+#pragma unroll
+        for (int i = 0; i < N; i++) r.v[i] = 0;
+        return r;
+    }
+    __device__ __forceinline__ static Field one() {
+        Field r;
+#pragma unroll
+        for (int i = 0; i < N; i++) r.v[i] = P::one(i);
+        return r;
+    }
+    __host__ __device__ __forceinline__ bool is_zero() const {
+        uint32_t acc = 0;
+#pragma unroll
+        for (int i = 0; i < N; i++) acc |= v[i];
+        return acc == 0;
+    }
+    __device__ __forceinline__ bool operator==(const Field &o) const {
+        uint32_t acc = 0;
+#pragma unroll
+        for (int i = 0; i < N; i++) acc |= v[i] ^ o.v[i];
+        return acc == 0;
+    }
+    __device__ __forceinline__ bool operator!=(const Field &o) const { return !(*this == o); }
+};
+
+using Fr = Field<FrParams>;
+using Fq = Field<FqParams>;
+
+// r = a - p if a >= p (a < 2p assumed, with `hi` the carry-out limb)
+template <class P>
+__device__ __forceinline__ void reduce_once(Field<P> &r, uint32_t hi) {
+    constexpr int N = P::N;
+    uint32_t t[N];
+    t[0] = sub_cc(r.v[0], P::p(0));
+#pragma unroll
+    for (int i = 1; i < N; i++) t[i] = subc_cc(r.v[i], P::p(i));
+    uint32_t borrow = subc(hi, 0);  // 0xffffffff if r < p (and no carry), else 0
+#pragma unroll
+    for (int i = 0; i < N; i++) r.v[i] = borrow ? r.v[i] : t[i];
+}
+
+template <class P>
+__device__ __forceinline__ Field<P> operator+(const Field<P> &a, const Field<P> &b) {
+    constexpr int N = P::N;
+    Field<P> r;
+    r.v[0] = add_cc(a.v[0], b.v[0]);
+#pragma unroll
+    for (int i = 1; i < N; i++) r.v[i] = addc_cc(a.v[i], b.v[i]);
+    uint32_t hi = addc(0, 0);
+    reduce_once<P>(r, hi);
+    return r;
+}
+
+template <class P>
+__device__ __forceinline__ Field<P> operator-(const Field<P> &a, const Field<P> &b) {
+    constexpr int N = P::N;
+    Field<P> r;
+    r.v[0] = sub_cc(a.v[0], b.v[0]);
+#pragma unroll
+    for (int i = 1; i < N; i++) r.v[i] = subc_cc(a.v[i], b.v[i]);
+    uint32_t borrow = subc(0, 0);  // 0xffffffff on borrow
+    uint32_t t[N];
+    t[0] = add_cc(r.v[0], P::p(0) & borrow);
+#pragma unroll
+    for (int i = 1; i < N - 1; i++) t[i] = addc_cc(r.v[i], P::p(i) & borrow);
+    t[N - 1] = addc(r.v[N - 1], P::p(N - 1) & borrow);
+#pragma unroll
+    for (int i = 0; i < N; i++) r.v[i] = t[i];
+    return r;
+}
+
+template <class P>
+__device__ __forceinline__ Field<P> neg(const Field<P> &a) {
+    return Field<P>::zero() - a;
+}
+
+template <class P>
+__device__ __forceinline__ Field<P> dbl(const Field<P> &a) {
+    return a + a;
+}
+
+// CIOS Montgomery multiplication, 32-bit limbs: per row one carry chain for
+// the low halves and one for the high halves of a*b_i, then the same for
+// m*p.  4N^2 + N multiply-adds per product.
+template <class P>
+__device__ __forceinline__ Field<P> operator*(const Field<P> &a, const Field<P> &b) {
+    constexpr int N = P::N;
+    uint32_t t[N + 2];
+#pragma unroll
+    for (int i = 0; i < N + 2; i++) t[i] = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const uint32_t bi = b.v[i];
+        // t += lo(a * bi)
+        t[0] = mad_lo_cc(a.v[0], bi, t[0]);
+#pragma unroll
+        for (int j = 1; j < N; j++) t[j] = madc_lo_cc(a.v[j], bi, t[j]);
+        t[N] = addc_cc(t[N], 0);
+        t[N + 1] = addc(t[N + 1], 0);
+        // t += hi(a * bi) << 32
+        t[1] = mad_hi_cc(a.v[0], bi, t[1]);
+#pragma unroll
+        for (int j = 1; j < N; j++) t[j + 1] = madc_hi_cc(a.v[j], bi, t[j + 1]);
+        t[N + 1] = addc(t[N + 1], 0);
+        // reduction: t += m * p, t[0] becomes 0
+        const uint32_t m = t[0] * P::INV;
+        t[0] = mad_lo_cc(m, P::p(0), t[0]);
+#pragma unroll
+        for (int j = 1; j < N; j++) t[j] = madc_lo_cc(m, P::p(j), t[j]);
+        t[N] = addc_cc(t[N], 0);
+        t[N + 1] = addc(t[N + 1], 0);
+        t[1] = mad_hi_cc(m, P::p(0), t[1]);
+#pragma unroll
+        for (int j = 1; j < N; j++) t[j + 1] = madc_hi_cc(m, P::p(j), t[j + 1]);
+        t[N + 1] = addc(t[N + 1], 0);
+        // shift one limb down
+#pragma unroll
+        for (int j = 0; j < N + 1; j++) t[j] = t[j + 1];
+        t[N + 1] = 0;
+    }
+    Field<P> r;
+#pragma unroll
+    for (int i = 0; i < N; i++) r.v[i] = t[i];
+    reduce_once<P>(r, t[N]);
+    return r;
+}
+
+template <class P>
+__device__ __forceinline__ Field<P> sqr(const Field<P> &a) {
+    return a * a;
+}
+
+// Montgomery form <-> canonical integer.
+template <class P>
+__device__ __forceinline__ Field<P> to_mont(const Field<P> &canonical) {
+    Field<P> r2;
+#pragma unroll
+    for (int i = 0; i < P::N; i++) r2.v[i] = P::r2(i);
+    return canonical * r2;
+}
+template <class P>
+__device__ __forceinline__ Field<P> from_mont(const Field<P> &a) {
+    Field<P> one = Field<P>::zero();
+    one.v[0] = 1;
+    return a * one;
+}
+
+// True if the integer held in a is < p (canonical).
+template <class P>
+__device__ __forceinline__ bool is_canonical(const Field<P> &a) {
+    constexpr int N = P::N;
+    uint32_t t = sub_cc(a.v[0], P::p(0));
+#pragma unroll
+    for (int i = 1; i < N; i++) t = subc_cc(a.v[i], P::p(i));
+    (void)t;
+    uint32_t borrow = subc(0, 0);
+    return borrow != 0;
+}
+
+// a^(p-2) by square-and-multiply over the modulus bits (p is odd, > 2).
+template <class P>
+__device__ __noinline__ Field<P> inverse(const Field<P> &a) {
+    constexpr int N = P::N;
+    Field<P> acc = Field<P>::one();
+    for (int i = N - 1; i >= 0; i--) {
+        uint32_t e = P::p(i);
+        if (i == 0) e -= 2;
+        for (int bit = 31; bit >= 0; bit--) {
+            acc = acc * acc;
+            if ((e >> bit) & 1) acc = acc * a;
+        }
+    }
+    return acc;
+}
+
+// Small integer in Montgomery form.
+template <class P>
+__device__ __forceinline__ Field<P> from_u32(uint32_t x) {
+    Field<P> t = Field<P>::zero();
+    t.v[0] = x;
+    return to_mont(t);
+}
+
+// ---------------------------------------------------------------------------
+// Global-memory helpers (AoS, 16-byte vector accesses)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ Fr load_fr(const Fr *p) {
+    const uint4 *q = reinterpret_cast<const uint4 *>(p);
+    uint4 a = q[0], b = q[1];
+    Fr r;
+    r.v[0] = a.x; r.v[1] = a.y; r.v[2] = a.z; r.v[3] = a.w;
+    r.v[4] = b.x; r.v[5] = b.y; r.v[6] = b.z; r.v[7] = b.w;
+    return r;
+}
+__device__ __forceinline__ void store_fr(Fr *p, const Fr &x) {
+    uint4 *q = reinterpret_cast<uint4 *>(p);
+    q[0] = make_uint4(x.v[0], x.v[1], x.v[2], x.v[3]);
+    q[1] = make_uint4(x.v[4], x.v[5], x.v[6], x.v[7]);
+}
+
+}  // namespace hp

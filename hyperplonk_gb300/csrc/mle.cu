@@ -1,0 +1,606 @@
+// mle.cu -- resident MLE table kernels and their ABI entries.
+//
+// Reference semantics: backend/src/cpu/multilinear_polynomial.rs:32-253 (CPU
+// backend) and backend/src/common/eq.rs:38-95; device counterparts in the
+// reference are the AscendC kernels of backend/src/ascend910b3/native/
+// mle_kernels.asc:272-522.  Tables are low-bit-first: entry x holds f at the
+// Boolean point whose variable i is bit i of x.
+//
+// Every kernel here is HBM bound except eq/frac (one Fr multiply per 32-byte
+// element moved, near the IMAD/HBM balance point).  Grids are multiples of
+// the SM count with grid-stride loops; AoS 32-byte elements are moved as two
+// 16-byte vector accesses.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "host_field.h"
+#include "mle.cuh"
+#include "runtime.cuh"
+
+using hp::check_cuda;
+using hp::check_launch;
+using hp::fail;
+using hp::Fr;
+using hp::guard;
+using hp::require;
+
+namespace hp {
+
+// ---------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------
+
+// In place: canonical -> Montgomery, flagging non-canonical inputs.
+__global__ void k_to_mont_check(Fr *data, size_t n, uint32_t *flags) {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x) {
+        Fr x = load_fr(&data[i]);
+        if (!is_canonical(x)) atomicOr(flags, kFlagNonCanonical);
+        store_fr(&data[i], to_mont(x));
+    }
+}
+
+__global__ void k_from_mont(const Fr *src, Fr *dst, size_t n) {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x)
+        store_fr(&dst[i], from_mont(load_fr(&src[i])));
+}
+
+__global__ void k_linear_combination(Fr *out, FrPtrList polys, FrScalarList coefs, int count,
+                                     size_t n, bool accumulate) {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x) {
+        Fr acc = accumulate ? load_fr(&out[i]) : Fr::zero();
+        for (int j = 0; j < count; j++) acc = acc + load_fr(&polys.p[j][i]) * coefs.s[j];
+        store_fr(&out[i], acc);
+    }
+}
+
+// One fix_variables step: dst[b] = src[2b] + r * (src[2b+1] - src[2b]).
+__global__ void k_fold(const Fr *src, Fr *dst, size_t half, Fr r) {
+    for (size_t b = blockIdx.x * size_t(blockDim.x) + threadIdx.x; b < half;
+         b += size_t(gridDim.x) * blockDim.x) {
+        Fr lo = load_fr(&src[2 * b]);
+        Fr hi = load_fr(&src[2 * b + 1]);
+        store_fr(&dst[b], lo + r * (hi - lo));
+    }
+}
+
+// Fold the last `levels` variables of a table of 2^levels entries in one block
+// (levels <= 10, 32 KiB), shared-memory resident; writes the single result.
+__global__ void k_fold_tail(const Fr *src, Fr *dst, int levels, FrScalarList r) {
+    extern __shared__ Fr sm[];
+    size_t n = size_t(1) << levels;
+    for (size_t i = threadIdx.x; i < n; i += blockDim.x) sm[i] = load_fr(&src[i]);
+    __syncthreads();
+    for (int l = 0; l < levels; l++) {
+        size_t half = n >> (l + 1);
+        Fr rl = r.s[l];
+        Fr v[4];
+        int cnt = 0;
+        for (size_t b = threadIdx.x; b < half; b += blockDim.x) {
+            Fr lo = sm[2 * b], hi = sm[2 * b + 1];
+            v[cnt & 3] = lo + rl * (hi - lo);
+            cnt++;
+        }
+        __syncthreads();
+        cnt = 0;
+        for (size_t b = threadIdx.x; b < half; b += blockDim.x) sm[b] = v[cnt++ & 3];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) store_fr(dst, sm[0]);
+}
+
+// eq table by direct products: out[x] = prod_j (bit_j(x) ? r_j : 1 - r_j).
+__global__ void k_eq_direct(Fr *out, const Fr *r, int m) {
+    size_t n = size_t(1) << m;
+    Fr one = Fr::one();
+    for (size_t x = blockIdx.x * size_t(blockDim.x) + threadIdx.x; x < n;
+         x += size_t(gridDim.x) * blockDim.x) {
+        Fr acc = one;
+        for (int j = 0; j < m; j++) {
+            Fr rj = r[j];
+            acc = acc * (((x >> j) & 1) ? rj : one - rj);
+        }
+        store_fr(&out[x], acc);
+    }
+}
+
+// out[x] = lo[x & mask] * hi[x >> low_bits]
+__global__ void k_eq_outer(Fr *out, const Fr *lo, const Fr *hi, int low_bits, size_t n) {
+    size_t mask = (size_t(1) << low_bits) - 1;
+    for (size_t x = blockIdx.x * size_t(blockDim.x) + threadIdx.x; x < n;
+         x += size_t(gridDim.x) * blockDim.x)
+        store_fr(&out[x], load_fr(&lo[x & mask]) * load_fr(&hi[x >> low_bits]));
+}
+
+// num[i] = prod f_j[i], den[i] = prod g_j[i]; flags zero denominators.
+__global__ void k_frac_products(Fr *num, Fr *den, FrPtrList fs, FrPtrList gs, int count, size_t n,
+                                bool accumulate, uint32_t *flags, bool check_zero) {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x) {
+        Fr a = accumulate ? load_fr(&num[i]) : load_fr(&fs.p[0][i]);
+        Fr b = accumulate ? load_fr(&den[i]) : load_fr(&gs.p[0][i]);
+        for (int j = accumulate ? 0 : 1; j < count; j++) {
+            a = a * load_fr(&fs.p[j][i]);
+            b = b * load_fr(&gs.p[j][i]);
+        }
+        if (check_zero && b.is_zero()) atomicOr(flags, kFlagZeroDenominator);
+        store_fr(&num[i], a);
+        store_fr(&den[i], b);
+    }
+}
+
+// Block-level Montgomery-trick inversion: out[i] = num[i] / den[i].
+// Each thread owns kInvChunk consecutive entries; thread chunk products are
+// combined by shared-memory prefix/suffix scans so one field inversion serves
+// kInvBlock * kInvChunk entries.  Zero denominators were rejected before.
+constexpr int kInvBlock = 256;
+constexpr int kInvChunk = 8;
+
+__global__ void __launch_bounds__(kInvBlock) k_batch_div(const Fr *num, const Fr *den, Fr *out,
+                                                         size_t n) {
+    __shared__ Fr pre[kInvBlock];
+    __shared__ Fr suf[kInvBlock];
+    __shared__ Fr total_inv;
+    const int t = threadIdx.x;
+    const size_t base = (size_t(blockIdx.x) * kInvBlock + t) * kInvChunk;
+    Fr one = Fr::one();
+    // 1) local prefix products, stored in out[] as scratch
+    Fr p = one;
+    for (int k = 0; k < kInvChunk; k++) {
+        size_t i = base + k;
+        if (i < n) {
+            store_fr(&out[i], p);
+            p = p * load_fr(&den[i]);
+        }
+    }
+    // 2) inclusive prefix and suffix products of the thread totals
+    pre[t] = p;
+    suf[t] = p;
+    __syncthreads();
+    for (int off = 1; off < kInvBlock; off <<= 1) {
+        Fr a = (t >= off) ? pre[t - off] * pre[t] : pre[t];
+        Fr b = (t + off < kInvBlock) ? suf[t + off] * suf[t] : suf[t];
+        __syncthreads();
+        pre[t] = a;
+        suf[t] = b;
+        __syncthreads();
+    }
+    if (t == 0) total_inv = inverse(pre[kInvBlock - 1]);
+    __syncthreads();
+    // 3) inverse of this thread's own product = total^-1 * prefix_excl * suffix_excl
+    Fr inv = total_inv;
+    if (t > 0) inv = inv * pre[t - 1];
+    if (t + 1 < kInvBlock) inv = inv * suf[t + 1];
+    // 4) backward pass over the chunk
+    for (int k = kInvChunk - 1; k >= 0; k--) {
+        size_t i = base + k;
+        if (i < n) {
+            Fr d = load_fr(&den[i]);
+            Fr inv_i = inv * load_fr(&out[i]);
+            inv = inv * d;
+            store_fr(&out[i], load_fr(&num[i]) * inv_i);
+        }
+    }
+}
+
+// Product tree, first levels inside one block of 256 threads.  Block b reads
+// frac[b*1024, (b+1)*1024) and writes levels k = 0..9: level k holds
+// N/2^(k+1) entries starting at base_k = N - N/2^k, and this block's share of
+// it is [base_k + b*(512>>k), base_k + (b+1)*(512>>k)).
+constexpr int kSubtreeLeaves = 512;  // level-0 entries per block
+constexpr int kSubtreeLevels = 10;   // levels 0..9 done in shared memory
+
+__global__ void __launch_bounds__(256) k_prod_subtree(const Fr *frac, Fr *prod, size_t N) {
+    __shared__ Fr sm[kSubtreeLeaves];
+    const size_t b = blockIdx.x;
+    const int t = threadIdx.x;
+    for (int i = t; i < kSubtreeLeaves; i += 256) {
+        size_t src = (b * kSubtreeLeaves + i) * 2;
+        Fr v = load_fr(&frac[src]) * load_fr(&frac[src + 1]);
+        sm[i] = v;
+        store_fr(&prod[b * kSubtreeLeaves + i], v);
+    }
+    __syncthreads();
+    for (int k = 1; k < kSubtreeLevels; k++) {
+        int len = kSubtreeLeaves >> k;
+        size_t base = N - (N >> k);
+        Fr v;
+        if (t < len) v = sm[2 * t] * sm[2 * t + 1];
+        __syncthreads();
+        if (t < len) {
+            sm[t] = v;
+            store_fr(&prod[base + b * size_t(len) + t], v);
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_prod_from_frac(const Fr *frac, Fr *prod, size_t half) {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < half;
+         i += size_t(gridDim.x) * blockDim.x)
+        store_fr(&prod[i], load_fr(&frac[2 * i]) * load_fr(&frac[2 * i + 1]));
+}
+
+// One product-tree level above the subtree: prod[idx] = prod[2idx-N] * prod[2idx-N+1]
+// for idx in [begin, end).
+__global__ void k_prod_level(Fr *prod, size_t begin, size_t end, size_t N) {
+    for (size_t idx = begin + blockIdx.x * size_t(blockDim.x) + threadIdx.x; idx < end;
+         idx += size_t(gridDim.x) * blockDim.x)
+        store_fr(&prod[idx], load_fr(&prod[2 * idx - N]) * load_fr(&prod[2 * idx - N + 1]));
+}
+
+__global__ void k_set_zero_last(Fr *prod, size_t N) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) store_fr(&prod[N - 1], Fr::zero());
+}
+
+// nums/denoms for one column: num = f + beta*(column*N + i) + gamma,
+// den = g + beta*perm + gamma.  The identity term advances by beta*stride.
+__global__ void k_nums_denoms(const Fr *f, const Fr *g, const Fr *perm, Fr *num, Fr *den, Fr beta,
+                              Fr gamma, uint64_t column_offset, size_t n) {
+    size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    size_t stride = size_t(gridDim.x) * blockDim.x;
+    if (i >= n) return;
+    // identity value (column_offset + i) in Montgomery form via two 32-bit halves
+    uint64_t v = column_offset + i;
+    Fr lo = from_u32<FrParams>(uint32_t(v));
+    Fr hi = from_u32<FrParams>(uint32_t(v >> 32));
+    Fr two32 = from_u32<FrParams>(65536u) * from_u32<FrParams>(65536u);
+    Fr id = beta * (lo + hi * two32);
+    Fr step = beta * (from_u32<FrParams>(uint32_t(stride)) +
+                      from_u32<FrParams>(uint32_t(uint64_t(stride) >> 32)) * two32);
+    for (; i < n; i += stride) {
+        store_fr(&num[i], load_fr(&f[i]) + id + gamma);
+        store_fr(&den[i], load_fr(&g[i]) + beta * load_fr(&perm[i]) + gamma);
+        id = id + step;
+    }
+}
+
+// p1 = even entries of (frac || prod), p2 = odd entries.
+__global__ void k_product_factors(const Fr *frac, const Fr *prod, Fr *p1, Fr *p2, size_t N) {
+    size_t half = N / 2;
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < N;
+         i += size_t(gridDim.x) * blockDim.x) {
+        const Fr *src = i < half ? frac : prod;
+        size_t j = i < half ? i : i - half;
+        store_fr(&p1[i], load_fr(&src[2 * j]));
+        store_fr(&p2[i], load_fr(&src[2 * j + 1]));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host helpers shared with other translation units
+// ---------------------------------------------------------------------------
+
+Fr host_scalar(const uint8_t *canonical) {
+    host::Fr64 m;
+    require(canonical != nullptr && host::from_canonical(canonical, m));
+    Fr r;
+    std::memcpy(r.v, m.v, 32);
+    return r;
+}
+
+void host_scalars_to_device(HpCudaContext *ctx, const uint8_t *canonical, size_t count, Fr *dst) {
+    std::vector<Fr> tmp(count);
+    for (size_t i = 0; i < count; i++) tmp[i] = host_scalar(canonical + 32 * i);
+    if (count)
+        check_cuda(cudaMemcpyAsync(dst, tmp.data(), count * sizeof(Fr), cudaMemcpyHostToDevice,
+                                   ctx->stream));
+    // tmp is pageable: the copy has been staged before cudaMemcpyAsync returns
+    // only for pageable sources, so synchronize to end the host borrow.
+    ctx->sync();
+}
+
+void download_canonical(HpCudaContext *ctx, const Fr *src, size_t n, uint8_t *out) {
+    Scratch tmp(ctx, n * sizeof(Fr));
+    k_from_mont<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(src, tmp.as<Fr>(), n);
+    check_launch();
+    check_cuda(cudaMemcpyAsync(out, tmp.ptr, n * sizeof(Fr), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+}
+
+void fold_to_scalar(HpCudaContext *ctx, const Fr *table, size_t nv, const Fr *point, Fr *dst) {
+    // Levels above the tail fold through global ping-pong buffers.
+    constexpr int kTail = 10;
+    if (nv == 0) {
+        check_cuda(cudaMemcpyAsync(dst, table, sizeof(Fr), cudaMemcpyDeviceToDevice, ctx->stream));
+        return;
+    }
+    Scratch a, b;
+    const Fr *cur = table;
+    size_t level = 0;
+    if (nv > kTail) {
+        a = Scratch(ctx, table_len(nv - 1) * sizeof(Fr));
+        b = Scratch(ctx, table_len(nv - 2) * sizeof(Fr));
+        Fr *bufs[2] = {a.as<Fr>(), b.as<Fr>()};
+        int which = 0;
+        while (nv - level > size_t(kTail)) {
+            size_t half = table_len(nv - level - 1);
+            Fr *dstb = bufs[which];
+            k_fold<<<grid_for(ctx, half, 256), 256, 0, ctx->stream>>>(cur, dstb, half, point[level]);
+            check_launch();
+            cur = dstb;
+            which ^= 1;
+            level++;
+        }
+    }
+    int rest = int(nv - level);
+    FrScalarList r;
+    for (int l = 0; l < rest; l++) r.s[l] = point[level + l];
+    size_t smem = table_len(rest) * sizeof(Fr);  // <= 32 KiB
+    k_fold_tail<<<1, 512, smem, ctx->stream>>>(cur, dst, rest, r);
+    check_launch();
+}
+
+void build_eq(HpCudaContext *ctx, const Fr *r_dev, size_t nv, Fr *out) {
+    constexpr size_t kDirect = 12;
+    size_t n = table_len(nv);
+    if (nv <= kDirect) {
+        k_eq_direct<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(out, r_dev, int(nv));
+        check_launch();
+        return;
+    }
+    size_t low = nv / 2, high = nv - low;
+    Scratch lo(ctx, table_len(low) * sizeof(Fr)), hi(ctx, table_len(high) * sizeof(Fr));
+    k_eq_direct<<<grid_for(ctx, table_len(low), 256), 256, 0, ctx->stream>>>(lo.as<Fr>(), r_dev,
+                                                                            int(low));
+    check_launch();
+    k_eq_direct<<<grid_for(ctx, table_len(high), 256), 256, 0, ctx->stream>>>(
+        hi.as<Fr>(), r_dev + low, int(high));
+    check_launch();
+    k_eq_outer<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(out, lo.as<Fr>(), hi.as<Fr>(),
+                                                              int(low), n);
+    check_launch();
+}
+
+void product_tree(HpCudaContext *ctx, const Fr *frac, Fr *prod, size_t nv) {
+    size_t N = table_len(nv);
+    size_t k0;
+    if (N >= 2 * size_t(kSubtreeLeaves)) {
+        k_prod_subtree<<<unsigned(N / (2 * kSubtreeLeaves)), 256, 0, ctx->stream>>>(frac, prod, N);
+        check_launch();
+        k0 = kSubtreeLevels;
+    } else {
+        k_prod_from_frac<<<grid_for(ctx, N / 2, 256), 256, 0, ctx->stream>>>(frac, prod, N / 2);
+        check_launch();
+        k0 = 1;
+    }
+    for (size_t k = k0; k < nv; k++) {
+        size_t begin = N - (N >> k), len = N >> (k + 1);
+        k_prod_level<<<grid_for(ctx, len, 256), 256, 0, ctx->stream>>>(prod, begin, begin + len, N);
+        check_launch();
+    }
+    k_set_zero_last<<<1, 32, 0, ctx->stream>>>(prod, N);
+    check_launch();
+}
+
+}  // namespace hp
+
+// ---------------------------------------------------------------------------
+// ABI entries (reference bridge_mle.cpp; trait backend/src/multilinear_polynomial.rs)
+// ---------------------------------------------------------------------------
+
+using hp::kFrBytes;
+using hp::kMaxList;
+using hp::OwnedBuffer;
+using hp::Scratch;
+using hp::table_len;
+
+extern "C" HpCudaStatus hp_cuda_v1_mle_upload(HpCudaContext *ctx, size_t num_vars,
+                                              const uint8_t *evaluations, size_t evaluation_count,
+                                              HpCudaDeviceAddress *out) {
+    if (out) *out = nullptr;
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(out != nullptr && evaluations != nullptr && num_vars <= hp::kMaxNumVars);
+        size_t n = table_len(num_vars);
+        require(evaluation_count == n);
+        OwnedBuffer buf(ctx, n * kFrBytes);
+        ctx->clear_flags();
+        check_cuda(cudaMemcpyAsync(buf.ptr, evaluations, n * kFrBytes, cudaMemcpyHostToDevice,
+                                   ctx->stream));
+        hp::k_to_mont_check<<<hp::grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(buf.as<Fr>(), n,
+                                                                               ctx->d_flags);
+        check_launch();
+        uint32_t flags = ctx->sync_flags();
+        if (flags & hp::kFlagNonCanonical) fail(HP_CUDA_STATUS_INVALID_PARAMETERS);
+        *out = buf.release();
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_mle_download(HpCudaContext *ctx, HpCudaDeviceAddress polynomial,
+                                                size_t num_vars, uint8_t *out_evaluations,
+                                                size_t evaluation_count) {
+    return guard([&] {
+        hp::require_ctx(ctx);
+        Fr *src = hp::mle_ptr(ctx, polynomial, num_vars);
+        require(out_evaluations != nullptr && evaluation_count == table_len(num_vars));
+        hp::download_canonical(ctx, src, evaluation_count, out_evaluations);
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_mle_linear_combination(HpCudaContext *ctx, size_t num_vars,
+                                                          const HpCudaDeviceAddress *polynomials,
+                                                          const uint8_t *coefficients,
+                                                          size_t count, HpCudaDeviceAddress *out) {
+    if (out) *out = nullptr;
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(out != nullptr && polynomials != nullptr && coefficients != nullptr && count > 0);
+        require(num_vars <= hp::kMaxNumVars);
+        std::vector<const Fr *> ptrs;
+        std::vector<Fr> coefs;
+        for (size_t j = 0; j < count; j++) {
+            const Fr *p = hp::mle_ptr(ctx, polynomials[j], num_vars);
+            Fr c = hp::host_scalar(coefficients + 32 * j);
+            if (c.v[0] | c.v[1] | c.v[2] | c.v[3] | c.v[4] | c.v[5] | c.v[6] | c.v[7]) {
+                ptrs.push_back(p);
+                coefs.push_back(c);
+            }
+        }
+        size_t n = table_len(num_vars);
+        OwnedBuffer buf(ctx, n * kFrBytes);
+        if (ptrs.empty()) {
+            check_cuda(cudaMemsetAsync(buf.ptr, 0, n * kFrBytes, ctx->stream));
+        }
+        for (size_t start = 0; start < ptrs.size(); start += kMaxList) {
+            hp::FrPtrList pl{};
+            hp::FrScalarList cl{};
+            int m = int(std::min(ptrs.size() - start, size_t(kMaxList)));
+            for (int j = 0; j < m; j++) {
+                pl.p[j] = ptrs[start + j];
+                cl.s[j] = coefs[start + j];
+            }
+            hp::k_linear_combination<<<hp::grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(
+                buf.as<Fr>(), pl, cl, m, n, start > 0);
+            check_launch();
+        }
+        *out = buf.release();
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_mle_evaluate(HpCudaContext *ctx, HpCudaDeviceAddress polynomial,
+                                                size_t num_vars, const uint8_t *point,
+                                                uint8_t *out_evaluation) {
+    return guard([&] {
+        hp::require_ctx(ctx);
+        const Fr *table = hp::mle_ptr(ctx, polynomial, num_vars);
+        require(out_evaluation != nullptr && (num_vars == 0 || point != nullptr));
+        std::vector<Fr> pt(num_vars);
+        for (size_t i = 0; i < num_vars; i++) pt[i] = hp::host_scalar(point + 32 * i);
+        Scratch res(ctx, sizeof(Fr));
+        hp::fold_to_scalar(ctx, table, num_vars, pt.data(), res.as<Fr>());
+        hp::download_canonical(ctx, res.as<Fr>(), 1, out_evaluation);
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_mle_build_eq_x_r(HpCudaContext *ctx, const uint8_t *r,
+                                                    size_t num_vars, HpCudaDeviceAddress *out) {
+    if (out) *out = nullptr;
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(out != nullptr && r != nullptr && num_vars > 0 && num_vars <= hp::kMaxNumVars);
+        Scratch rd(ctx, num_vars * sizeof(Fr));
+        hp::host_scalars_to_device(ctx, r, num_vars, rd.as<Fr>());
+        OwnedBuffer buf(ctx, table_len(num_vars) * kFrBytes);
+        hp::build_eq(ctx, rd.as<Fr>(), num_vars, buf.as<Fr>());
+        *out = buf.release();
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_mle_compute_frac_poly(HpCudaContext *ctx, size_t num_vars,
+                                                         const HpCudaDeviceAddress *numerators,
+                                                         const HpCudaDeviceAddress *denominators,
+                                                         size_t count, HpCudaDeviceAddress *out) {
+    if (out) *out = nullptr;
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(out != nullptr && numerators != nullptr && denominators != nullptr && count > 0);
+        require(num_vars <= hp::kMaxNumVars);
+        std::vector<const Fr *> fs(count), gs(count);
+        for (size_t j = 0; j < count; j++) {
+            fs[j] = hp::mle_ptr(ctx, numerators[j], num_vars);
+            gs[j] = hp::mle_ptr(ctx, denominators[j], num_vars);
+        }
+        size_t n = table_len(num_vars);
+        Scratch num(ctx, n * kFrBytes), den(ctx, n * kFrBytes);
+        ctx->clear_flags();
+        for (size_t start = 0; start < count; start += kMaxList) {
+            hp::FrPtrList fl{}, gl{};
+            int m = int(std::min(count - start, size_t(kMaxList)));
+            for (int j = 0; j < m; j++) {
+                fl.p[j] = fs[start + j];
+                gl.p[j] = gs[start + j];
+            }
+            bool last = start + kMaxList >= count;
+            hp::k_frac_products<<<hp::grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(
+                num.as<Fr>(), den.as<Fr>(), fl, gl, m, n, start > 0, ctx->d_flags, last);
+            check_launch();
+        }
+        uint32_t flags = ctx->sync_flags();
+        if (flags & hp::kFlagZeroDenominator) fail(HP_CUDA_STATUS_INVALID_PARAMETERS);
+        OwnedBuffer buf(ctx, n * kFrBytes);
+        size_t per_block = size_t(hp::kInvBlock) * hp::kInvChunk;
+        hp::k_batch_div<<<unsigned((n + per_block - 1) / per_block), hp::kInvBlock, 0,
+                          ctx->stream>>>(num.as<Fr>(), den.as<Fr>(), buf.as<Fr>(), n);
+        check_launch();
+        *out = buf.release();
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_mle_compute_product_poly(HpCudaContext *ctx,
+                                                            HpCudaDeviceAddress frac,
+                                                            size_t num_vars,
+                                                            HpCudaDeviceAddress *out) {
+    if (out) *out = nullptr;
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(out != nullptr && num_vars > 0);
+        const Fr *f = hp::mle_ptr(ctx, frac, num_vars);
+        OwnedBuffer buf(ctx, table_len(num_vars) * kFrBytes);
+        hp::product_tree(ctx, f, buf.as<Fr>(), num_vars);
+        *out = buf.release();
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_mle_compute_nums_and_denoms(
+    HpCudaContext *ctx, size_t num_vars, const uint8_t *beta, const uint8_t *gamma,
+    const HpCudaDeviceAddress *fxs, const HpCudaDeviceAddress *gxs,
+    const HpCudaDeviceAddress *permutations, size_t count, HpCudaDeviceAddress *out_numerators,
+    HpCudaDeviceAddress *out_denominators) {
+    if (out_numerators)
+        for (size_t j = 0; j < count; j++) out_numerators[j] = nullptr;
+    if (out_denominators)
+        for (size_t j = 0; j < count; j++) out_denominators[j] = nullptr;
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(out_numerators != nullptr && out_denominators != nullptr && fxs != nullptr &&
+                gxs != nullptr && permutations != nullptr && count > 0 && beta != nullptr &&
+                gamma != nullptr);
+        require(num_vars <= hp::kMaxNumVars);
+        Fr b = hp::host_scalar(beta), g = hp::host_scalar(gamma);
+        size_t n = table_len(num_vars);
+        std::vector<OwnedBuffer> nums, dens;
+        nums.reserve(count);
+        dens.reserve(count);
+        for (size_t j = 0; j < count; j++) {
+            const Fr *f = hp::mle_ptr(ctx, fxs[j], num_vars);
+            const Fr *gx = hp::mle_ptr(ctx, gxs[j], num_vars);
+            const Fr *p = hp::mle_ptr(ctx, permutations[j], num_vars);
+            nums.emplace_back(ctx, n * kFrBytes);
+            dens.emplace_back(ctx, n * kFrBytes);
+            hp::k_nums_denoms<<<hp::grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(
+                f, gx, p, nums.back().as<Fr>(), dens.back().as<Fr>(), b, g, uint64_t(j) * n, n);
+            check_launch();
+        }
+        for (size_t j = 0; j < count; j++) {
+            out_numerators[j] = nums[j].release();
+            out_denominators[j] = dens[j].release();
+        }
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_mle_compute_product_factors(HpCudaContext *ctx,
+                                                               HpCudaDeviceAddress frac,
+                                                               HpCudaDeviceAddress product,
+                                                               size_t num_vars,
+                                                               HpCudaDeviceAddress *out_p1,
+                                                               HpCudaDeviceAddress *out_p2) {
+    if (out_p1) *out_p1 = nullptr;
+    if (out_p2) *out_p2 = nullptr;
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(out_p1 != nullptr && out_p2 != nullptr && num_vars > 0);
+        const Fr *f = hp::mle_ptr(ctx, frac, num_vars);
+        const Fr *p = hp::mle_ptr(ctx, product, num_vars);
+        size_t n = table_len(num_vars);
+        OwnedBuffer a(ctx, n * kFrBytes), b(ctx, n * kFrBytes);
+        hp::k_product_factors<<<hp::grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(
+            f, p, a.as<Fr>(), b.as<Fr>(), n);
+        check_launch();
+        *out_p1 = a.release();
+        *out_p2 = b.release();
+    });
+}

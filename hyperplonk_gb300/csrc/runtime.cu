@@ -1,0 +1,151 @@
+// runtime.cu -- context lifetime, buffer registry, retirement.
+// ABI: hp_cuda_v1_context_create / _destroy / _buffer_retire / _context_stream
+// (reference bridge.h:43-45, bridge_runtime.cpp).
+#include <cstring>
+
+#include "runtime.cuh"
+
+using hp::check_cuda;
+using hp::fail;
+using hp::guard;
+using hp::require;
+
+void *HpCudaContext::alloc(size_t bytes) {
+    void *p = nullptr;
+    check_cuda(cudaMallocFromPoolAsync(&p, bytes ? bytes : 16, pool, stream));
+    try {
+        buffers.emplace(p, Buffer{bytes, 1, true});
+    } catch (...) {
+        cudaFreeAsync(p, stream);
+        throw;
+    }
+    return p;
+}
+
+void *HpCudaContext::scratch(size_t bytes) {
+    void *p = nullptr;
+    check_cuda(cudaMallocFromPoolAsync(&p, bytes ? bytes : 16, pool, stream));
+    return p;
+}
+
+void HpCudaContext::scratch_free(void *p) {
+    if (p) cudaFreeAsync(p, stream);
+}
+
+void HpCudaContext::ref(void *p) {
+    auto it = buffers.find(p);
+    if (it == buffers.end()) fail(HP_CUDA_STATUS_INVALID_PARAMETERS);
+    it->second.refs++;
+}
+
+void HpCudaContext::unref(void *p) {
+    auto it = buffers.find(p);
+    if (it == buffers.end()) fail(HP_CUDA_STATUS_INVALID_PARAMETERS);
+    if (--it->second.refs == 0) {
+        buffers.erase(it);
+        check_cuda(cudaFreeAsync(p, stream));
+    }
+}
+
+void HpCudaContext::retire(void *p) {
+    auto it = buffers.find(p);
+    if (it == buffers.end() || !it->second.public_handle) fail(HP_CUDA_STATUS_INVALID_PARAMETERS);
+    it->second.public_handle = false;
+    unref(p);
+}
+
+size_t HpCudaContext::bytes_of(void *p) const {
+    auto it = buffers.find(p);
+    return it == buffers.end() ? 0 : it->second.bytes;
+}
+
+void HpCudaContext::clear_flags() { check_cuda(cudaMemsetAsync(d_flags, 0, sizeof(uint32_t), stream)); }
+
+uint32_t HpCudaContext::sync_flags() {
+    check_cuda(cudaMemcpyAsync(h_flags, d_flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+    check_cuda(cudaStreamSynchronize(stream));
+    return *h_flags;
+}
+
+void HpCudaContext::sync() { check_cuda(cudaStreamSynchronize(stream)); }
+
+bool hp::host_fr_is_canonical(const uint8_t *bytes) {
+    static const uint8_t P[32] = {0x01, 0x00, 0x00, 0x00, 0xff, 0xff, 0xff, 0xff, 0xfe, 0x5b, 0xfe,
+                                  0xff, 0x02, 0xa4, 0xbd, 0x53, 0x05, 0xd8, 0xa1, 0x09, 0x08, 0xd8,
+                                  0x39, 0x33, 0x48, 0x7d, 0x9d, 0x29, 0x53, 0xa7, 0xed, 0x73};
+    for (int i = 31; i >= 0; i--) {
+        if (bytes[i] != P[i]) return bytes[i] < P[i];
+    }
+    return false;
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_context_create(int32_t device_id, HpCudaContext **out) {
+    if (out) *out = nullptr;
+    return guard([&] {
+        require(out != nullptr && device_id >= 0);
+        int count = 0;
+        check_cuda(cudaGetDeviceCount(&count));
+        require(device_id < count);
+        check_cuda(cudaSetDevice(device_id));
+        HpCudaContext *ctx = new HpCudaContext();
+        ctx->device = device_id;
+        try {
+            check_cuda(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device_id));
+            check_cuda(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+            cudaMemPoolProps props;
+            std::memset(&props, 0, sizeof props);
+            props.allocType = cudaMemAllocationTypePinned;
+            props.handleTypes = cudaMemHandleTypeNone;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = device_id;
+            check_cuda(cudaMemPoolCreate(&ctx->pool, &props));
+            uint64_t threshold = UINT64_MAX;
+            check_cuda(cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &threshold));
+            check_cuda(cudaMalloc(&ctx->d_flags, sizeof(uint32_t)));
+            check_cuda(cudaMallocHost(&ctx->h_flags, sizeof(uint32_t)));
+            check_cuda(cudaMemset(ctx->d_flags, 0, sizeof(uint32_t)));
+        } catch (...) {
+            if (ctx->d_flags) cudaFree(ctx->d_flags);
+            if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
+            if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
+            if (ctx->stream) cudaStreamDestroy(ctx->stream);
+            delete ctx;
+            throw;
+        }
+        *out = ctx;
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_context_destroy(HpCudaContext *ctx) {
+    return guard([&] {
+        require(ctx != nullptr);
+        cudaSetDevice(ctx->device);
+        cudaError_t first = cudaStreamSynchronize(ctx->stream);
+        for (auto &kv : ctx->buffers) cudaFreeAsync(kv.first, ctx->stream);
+        ctx->buffers.clear();
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        if (first == cudaSuccess) first = e;
+        cudaFree(ctx->d_flags);
+        cudaFreeHost(ctx->h_flags);
+        cudaStreamDestroy(ctx->stream);
+        cudaMemPoolDestroy(ctx->pool);
+        delete ctx;
+        check_cuda(first);
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_buffer_retire(HpCudaContext *ctx, HpCudaDeviceAddress address) {
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(address != nullptr && ctx->owns(address));
+        ctx->retire(address);
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_context_stream(HpCudaContext *ctx, void **out_stream) {
+    if (out_stream) *out_stream = nullptr;
+    return guard([&] {
+        require(ctx != nullptr && out_stream != nullptr);
+        *out_stream = static_cast<void *>(ctx->stream);
+    });
+}

@@ -1,0 +1,188 @@
+// runtime.cuh -- context, buffer registry and ABI guard shared by every
+// translation unit of libhp_cuda.so.
+//
+// GB300 design: one context = one device + one non-blocking CUDA stream + one
+// private stream-ordered memory pool.  Every device allocation is a
+// cudaMallocFromPoolAsync on the context stream and every release a
+// cudaFreeAsync on the same stream, so a buffer returns to the pool only after
+// all work queued before its release (the reference's "free only after the
+// block's recorded stream event completes", bridge.h:17-19, by construction).
+// Public MLE addresses are reference counted: prover states and parameter
+// objects take a reference, so a retired handle's storage lives as long as any
+// of them needs it (bridge_runtime.h in the reference keeps BufferRef copies
+// for the same reason).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <new>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/hp_cuda.h"
+#include "field.cuh"
+
+namespace hp {
+
+struct Failure {
+    int32_t kind;
+    int32_t code;
+};
+
+[[noreturn]] inline void fail(int32_t kind, int32_t code = 0) { throw Failure{kind, code}; }
+inline void require(bool cond) {
+    if (!cond) fail(HP_CUDA_STATUS_INVALID_PARAMETERS);
+}
+inline void check_cuda(cudaError_t e) {
+    if (e != cudaSuccess) fail(HP_CUDA_STATUS_INVALID_STATE, static_cast<int32_t>(e));
+}
+
+template <class Fn>
+inline HpCudaStatus guard(Fn &&fn) {
+    try {
+        fn();
+        return HpCudaStatus{HP_CUDA_STATUS_SUCCESS, 0};
+    } catch (const Failure &f) {
+        return HpCudaStatus{f.kind, f.code};
+    } catch (const std::bad_alloc &) {
+        return HpCudaStatus{HP_CUDA_STATUS_INVALID_STATE, static_cast<int32_t>(cudaErrorMemoryAllocation)};
+    } catch (...) {
+        return HpCudaStatus{HP_CUDA_STATUS_INVALID_STATE, -1};
+    }
+}
+
+// Status word bits written by kernels (device flag, read after a sync).
+enum : uint32_t {
+    kFlagNonCanonical = 1u,
+    kFlagZeroDenominator = 2u,
+    kFlagPointOffCurve = 4u,
+    kFlagTimeout = 8u,
+};
+
+constexpr size_t kFrBytes = 32;
+constexpr size_t kG1PacketBytes = 97;
+constexpr size_t kAffineBytes = 96;
+constexpr size_t kMaxNumVars = 30;  // 2^30 Fr = 32 GiB per table
+
+inline size_t table_len(size_t num_vars) { return size_t(1) << num_vars; }
+
+}  // namespace hp
+
+struct HpCudaContext {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaMemPool_t pool = nullptr;
+    uint32_t *d_flags = nullptr;  // device status word
+    uint32_t *h_flags = nullptr;  // pinned host mirror
+    int sm_count = 0;
+    struct Buffer {
+        size_t bytes;
+        int refs;
+        bool public_handle;  // still owned by the caller (not yet retired)
+    };
+    std::unordered_map<void *, Buffer> buffers;
+
+    // Stream-ordered allocation registered with one reference.
+    void *alloc(size_t bytes);
+    // Unregistered scratch (freed with scratch_free, stream ordered).
+    void *scratch(size_t bytes);
+    void scratch_free(void *p);
+    void ref(void *p);
+    void unref(void *p);
+    // True while `p` is a caller-owned handle (allocated, not yet retired).
+    bool owns(void *p) const {
+        auto it = buffers.find(p);
+        return it != buffers.end() && it->second.public_handle;
+    }
+    // Caller gives up its handle; storage lives while internal refs remain.
+    void retire(void *p);
+    size_t bytes_of(void *p) const;
+    // Clear the device status word (stream ordered).
+    void clear_flags();
+    // Synchronize and return the status word.
+    uint32_t sync_flags();
+    void sync();
+};
+
+namespace hp {
+
+// RAII scratch: stream-ordered free at scope exit.
+struct Scratch {
+    HpCudaContext *ctx = nullptr;
+    void *ptr = nullptr;
+    Scratch() = default;
+    Scratch(HpCudaContext *c, size_t bytes) : ctx(c), ptr(c->scratch(bytes)) {}
+    Scratch(const Scratch &) = delete;
+    Scratch &operator=(const Scratch &) = delete;
+    Scratch(Scratch &&o) noexcept : ctx(o.ctx), ptr(o.ptr) { o.ptr = nullptr; }
+    Scratch &operator=(Scratch &&o) noexcept {
+        if (this != &o) {
+            if (ptr) ctx->scratch_free(ptr);
+            ctx = o.ctx;
+            ptr = o.ptr;
+            o.ptr = nullptr;
+        }
+        return *this;
+    }
+    ~Scratch() {
+        if (ptr) ctx->scratch_free(ptr);
+    }
+    template <class T>
+    T *as() const { return static_cast<T *>(ptr); }
+};
+
+// RAII owned output buffer: released unless handed out with release().
+struct OwnedBuffer {
+    HpCudaContext *ctx = nullptr;
+    void *ptr = nullptr;
+    OwnedBuffer() = default;
+    OwnedBuffer(HpCudaContext *c, size_t bytes) : ctx(c), ptr(c->alloc(bytes)) {}
+    OwnedBuffer(const OwnedBuffer &) = delete;
+    OwnedBuffer &operator=(const OwnedBuffer &) = delete;
+    OwnedBuffer(OwnedBuffer &&o) noexcept : ctx(o.ctx), ptr(o.ptr) { o.ptr = nullptr; }
+    ~OwnedBuffer() {
+        if (ptr) {
+            try { ctx->unref(ptr); } catch (...) {}
+        }
+    }
+    void *release() {
+        void *p = ptr;
+        ptr = nullptr;
+        return p;
+    }
+    template <class T>
+    T *as() const { return static_cast<T *>(ptr); }
+};
+
+inline void require_ctx(HpCudaContext *ctx) {
+    if (!ctx) fail(HP_CUDA_STATUS_INVALID_PARAMETERS);
+    check_cuda(cudaSetDevice(ctx->device));
+}
+
+// A registered MLE buffer of exactly 2^num_vars Fr.
+inline Fr *mle_ptr(HpCudaContext *ctx, HpCudaDeviceAddress a, size_t num_vars) {
+    require(a != nullptr && num_vars <= kMaxNumVars);
+    require(ctx->owns(a));
+    require(ctx->bytes_of(a) == table_len(num_vars) * kFrBytes);
+    return static_cast<Fr *>(a);
+}
+
+// Grid sizing: a multiple of the SM count, capped by the work.
+inline unsigned grid_for(const HpCudaContext *ctx, size_t work_items, unsigned block,
+                         unsigned blocks_per_sm = 8) {
+    size_t need = (work_items + block - 1) / block;
+    size_t cap = size_t(ctx->sm_count > 0 ? ctx->sm_count : 152) * blocks_per_sm;
+    if (need > cap) need = cap;
+    if (need == 0) need = 1;
+    return static_cast<unsigned>(need);
+}
+
+// Launch-error check after a kernel launch.
+inline void check_launch() { check_cuda(cudaGetLastError()); }
+
+// Canonical host Fr bytes -> device Montgomery values, in a small scratch.
+// Host side only validates canonical range; conversion happens on device.
+bool host_fr_is_canonical(const uint8_t *bytes);
+
+}  // namespace hp

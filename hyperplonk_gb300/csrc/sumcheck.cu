@@ -1,0 +1,358 @@
+// sumcheck.cu -- SumCheck prover state and the fused fold + round-message
+// kernel.
+//
+// Reference semantics: backend/src/cpu/sum_check.rs:35-217.  Round k (1-based)
+// first fixes the lowest variable of every distinct factor with the previous
+// challenge (ark-poly fix_variables: f'[b] = f[2b] + r*(f[2b+1] - f[2b])),
+// then for every product of arity m evaluates
+//     s(t) = sum_b prod_j (f_j[2b] + t*(f_j[2b+1] - f_j[2b]))   for t = 0..m,
+// scales by the product coefficient and extends the degree-m polynomial to
+// t = 0..max_degree.  The reference extends with barycentric weights; this
+// backend extends with forward differences over the integer nodes, which
+// yields the same field elements (the degree-m interpolant is unique).
+//
+// GB300 shape: one launch per round fuses the fold of round k-1's challenge
+// with the message of round k, so each factor table is read once and its
+// folded half written once per round.  Per-thread partial sums stay in shared
+// memory, are tree-reduced per block, and a one-block finalize kernel sums
+// the block partials, extrapolates, scales and converts to canonical bytes.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "host_field.h"
+#include "mle.cuh"
+#include "runtime.cuh"
+#include "sumcheck.cuh"
+
+using hp::check_cuda;
+using hp::check_launch;
+using hp::fail;
+using hp::Fr;
+using hp::guard;
+using hp::require;
+
+namespace hp {
+
+// Shared-memory layout per thread (T threads per block, column-major by slot
+// so thread t's entries are sm[slot * T + t]):
+//   [0, 2F)           lo_f, d_f  (folded pair value and its step)
+//   [2F, 2F + M)      running evaluations of the current product
+//   [2F + M, ...+S)   accumulators, one per (product, t) slot
+__global__ void k_sumcheck_round(SumcheckDesc desc, FrPtrList src, FrMutPtrList dst, bool fold,
+                                 Fr r, size_t pairs, Fr *partials) {
+    extern __shared__ Fr sm[];
+    const int T = blockDim.x;
+    const int t = threadIdx.x;
+    const int F = desc.factor_count;
+    const int M = desc.max_arity;
+    const int S = desc.slot_count;
+    Fr *fv = sm;
+    Fr *ev = sm + 2 * F * T;
+    Fr *acc = ev + M * T;
+    for (int s = 0; s < S; s++) acc[s * T + t] = Fr::zero();
+
+    for (size_t b = blockIdx.x * size_t(T) + t; b < pairs; b += size_t(gridDim.x) * T) {
+        for (int f = 0; f < F; f++) {
+            Fr lo, hi;
+            if (fold) {
+                const Fr *s = src.p[f] + 4 * b;
+                Fr a0 = load_fr(s), a1 = load_fr(s + 1), a2 = load_fr(s + 2), a3 = load_fr(s + 3);
+                lo = a0 + r * (a1 - a0);
+                hi = a2 + r * (a3 - a2);
+                Fr *d = dst.p[f] + 2 * b;
+                store_fr(d, lo);
+                store_fr(d + 1, hi);
+            } else {
+                const Fr *s = src.p[f] + 2 * b;
+                lo = load_fr(s);
+                hi = load_fr(s + 1);
+            }
+            fv[(2 * f) * T + t] = lo;
+            fv[(2 * f + 1) * T + t] = hi - lo;
+        }
+        for (int p = 0; p < desc.product_count; p++) {
+            const int begin = desc.offsets[p], m = desc.offsets[p + 1] - begin;
+            const int slot = desc.slot_base[p];
+            Fr prod = fv[(2 * desc.indices[begin]) * T + t];
+            ev[t] = prod;
+            for (int j = 1; j < m; j++) {
+                Fr v = fv[(2 * desc.indices[begin + j]) * T + t];
+                ev[j * T + t] = v;
+                prod = prod * v;
+            }
+            acc[slot * T + t] = acc[slot * T + t] + prod;
+            for (int k = 1; k <= m; k++) {
+                Fr e = ev[t] + fv[(2 * desc.indices[begin] + 1) * T + t];
+                ev[t] = e;
+                prod = e;
+                for (int j = 1; j < m; j++) {
+                    Fr ej = ev[j * T + t] + fv[(2 * desc.indices[begin + j] + 1) * T + t];
+                    ev[j * T + t] = ej;
+                    prod = prod * ej;
+                }
+                acc[(slot + k) * T + t] = acc[(slot + k) * T + t] + prod;
+            }
+        }
+    }
+    // block tree reduction of every slot
+    for (int s = 0; s < S; s++) {
+        __syncthreads();
+        for (int half = T / 2; half > 0; half >>= 1) {
+            if (t < half) acc[s * T + t] = acc[s * T + t] + acc[s * T + t + half];
+            __syncthreads();
+        }
+        if (t == 0) partials[size_t(blockIdx.x) * S + s] = acc[s * T];
+    }
+}
+
+// One block: sum block partials per slot, extend each product to degree D by
+// forward differences, scale by its coefficient, accumulate, write canonical.
+__global__ void k_sumcheck_finalize(SumcheckDesc desc, const Fr *partials, int blocks,
+                                    const Fr *coefs, int degree, Fr *slot_sums, Fr *out) {
+    extern __shared__ Fr red[];
+    const int T = blockDim.x, t = threadIdx.x, S = desc.slot_count;
+    for (int s = 0; s < S; s++) {
+        Fr a = Fr::zero();
+        for (int b = t; b < blocks; b += T) a = a + partials[size_t(b) * S + s];
+        red[t] = a;
+        __syncthreads();
+        for (int half = T / 2; half > 0; half >>= 1) {
+            if (t < half) red[t] = red[t] + red[t + half];
+            __syncthreads();
+        }
+        if (t == 0) slot_sums[s] = red[0];
+        __syncthreads();
+    }
+    if (t != 0) return;
+    for (int k = 0; k <= degree; k++) out[k] = Fr::zero();
+    for (int p = 0; p < desc.product_count; p++) {
+        const int m = desc.offsets[p + 1] - desc.offsets[p];
+        const Fr *v = slot_sums + desc.slot_base[p];
+        Fr c = coefs[p];
+        // diagonal of the forward-difference table: last[k] = Delta^k v at m-k
+        Fr last[kMaxDegree + 1];
+        Fr row[kMaxDegree + 1];
+        for (int i = 0; i <= m; i++) row[i] = v[i];
+        last[0] = row[m];
+        for (int k = 1; k <= m; k++) {
+            for (int i = 0; i + k <= m; i++) row[i] = row[i + 1] - row[i];
+            last[k] = row[m - k];
+        }
+        for (int k = 0; k <= m; k++) out[k] = out[k] + c * v[k];
+        for (int x = m + 1; x <= degree; x++) {
+            for (int k = m - 1; k >= 0; k--) last[k] = last[k] + last[k + 1];
+            out[x] = out[x] + c * last[0];
+        }
+    }
+    for (int k = 0; k <= degree; k++) out[k] = from_mont(out[k]);
+}
+
+__global__ void k_sumcheck_final_fold(FrPtrList tables, int count, Fr r, Fr *out) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= count) return;
+    Fr lo = load_fr(tables.p[f]), hi = load_fr(tables.p[f] + 1);
+    out[f] = from_mont(lo + r * (hi - lo));
+}
+
+}  // namespace hp
+
+// ---------------------------------------------------------------------------
+// Prover state
+// ---------------------------------------------------------------------------
+
+struct HpCudaSumCheckProverState {
+    size_t num_vars = 0, max_degree = 0, round = 0;
+    bool poisoned = false;
+    hp::SumcheckDesc desc{};
+    std::vector<void *> inputs;  // referenced input factor buffers
+    void *fold_a = nullptr;      // F x 2^(nv-1) Fr
+    void *fold_b = nullptr;      // F x 2^(nv-2) Fr
+    void *coefs = nullptr;       // P Montgomery coefficients (device)
+    int current = 0;             // 0: inputs, 1: fold_a, 2: fold_b
+};
+
+namespace hp {
+
+static const Fr *state_table(HpCudaSumCheckProverState *s, int which, int f) {
+    size_t a_stride = s->num_vars >= 1 ? table_len(s->num_vars - 1) : 1;
+    size_t b_stride = s->num_vars >= 2 ? table_len(s->num_vars - 2) : 1;
+    if (which == 0) return static_cast<const Fr *>(s->inputs[f]);
+    if (which == 1) return static_cast<const Fr *>(s->fold_a) + f * a_stride;
+    return static_cast<const Fr *>(s->fold_b) + f * b_stride;
+}
+
+static void release_state(HpCudaContext *ctx, HpCudaSumCheckProverState *s) {
+    for (void *p : s->inputs) {
+        try { ctx->unref(p); } catch (...) {}
+    }
+    s->inputs.clear();
+    if (s->fold_a) ctx->scratch_free(s->fold_a);
+    if (s->fold_b) ctx->scratch_free(s->fold_b);
+    if (s->coefs) ctx->scratch_free(s->coefs);
+    s->fold_a = s->fold_b = s->coefs = nullptr;
+}
+
+static int round_block_size(const SumcheckDesc &d, size_t *smem_out) {
+    size_t per_thread = size_t(2 * d.factor_count + d.max_arity + d.slot_count) * sizeof(Fr);
+    int T = 256;
+    while (T > 32 && per_thread * T > 200 * 1024) T /= 2;
+    if (per_thread * T > 200 * 1024) fail(HP_CUDA_STATUS_NOT_IMPLEMENTED);
+    *smem_out = per_thread * T;
+    return T;
+}
+
+}  // namespace hp
+
+extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_create(
+    HpCudaContext *ctx, size_t num_vars, size_t max_degree, const HpCudaDeviceAddress *factors,
+    size_t factor_count, const uint8_t *coefficients, const size_t *product_offsets,
+    size_t product_count, const size_t *factor_indices, size_t index_count,
+    HpCudaSumCheckProverState **out) {
+    if (out) *out = nullptr;
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(out != nullptr && product_offsets != nullptr);
+        require(num_vars > 0 && num_vars <= hp::kMaxNumVars && max_degree > 0);
+        require(factor_count == 0 || factors != nullptr);
+        require(product_count == 0 || coefficients != nullptr);
+        require(index_count == 0 || factor_indices != nullptr);
+        require(product_offsets[0] == 0 && product_offsets[product_count] == index_count);
+        for (size_t p = 0; p < product_count; p++) {
+            size_t m = product_offsets[p + 1] - product_offsets[p];
+            require(product_offsets[p + 1] >= product_offsets[p] && m >= 1 && m <= max_degree);
+        }
+        for (size_t i = 0; i < index_count; i++) require(factor_indices[i] < factor_count);
+        if (factor_count > size_t(hp::kMaxList) || product_count > size_t(hp::kMaxProducts) ||
+            index_count > size_t(hp::kMaxIndices) || max_degree > size_t(hp::kMaxDegree))
+            fail(HP_CUDA_STATUS_NOT_IMPLEMENTED);
+
+        auto *s = new HpCudaSumCheckProverState();
+        try {
+            s->num_vars = num_vars;
+            s->max_degree = max_degree;
+            hp::SumcheckDesc &d = s->desc;
+            d.factor_count = int(factor_count);
+            d.product_count = int(product_count);
+            int slots = 0, max_arity = 1;
+            for (size_t p = 0; p < product_count; p++) {
+                int m = int(product_offsets[p + 1] - product_offsets[p]);
+                d.offsets[p] = uint16_t(product_offsets[p]);
+                d.slot_base[p] = uint16_t(slots);
+                slots += m + 1;
+                max_arity = std::max(max_arity, m);
+            }
+            d.offsets[product_count] = uint16_t(index_count);
+            for (size_t i = 0; i < index_count; i++) d.indices[i] = uint8_t(factor_indices[i]);
+            d.slot_count = std::max(slots, 1);
+            d.max_arity = max_arity;
+            for (size_t f = 0; f < factor_count; f++) {
+                hp::mle_ptr(ctx, factors[f], num_vars);
+                ctx->ref(factors[f]);
+                s->inputs.push_back(factors[f]);
+            }
+            s->coefs = ctx->scratch(std::max(product_count, size_t(1)) * sizeof(Fr));
+            hp::host_scalars_to_device(ctx, coefficients, product_count, static_cast<Fr *>(s->coefs));
+            size_t a_len = hp::table_len(num_vars - 1);
+            size_t b_len = num_vars >= 2 ? hp::table_len(num_vars - 2) : 1;
+            size_t fcount = std::max(factor_count, size_t(1));
+            s->fold_a = ctx->scratch(fcount * a_len * sizeof(Fr));
+            s->fold_b = ctx->scratch(fcount * b_len * sizeof(Fr));
+            size_t smem;
+            hp::round_block_size(d, &smem);
+        } catch (...) {
+            hp::release_state(ctx, s);
+            delete s;
+            throw;
+        }
+        *out = s;
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_round(HpCudaContext *ctx,
+                                                               HpCudaSumCheckProverState *s,
+                                                               const uint8_t *challenge_or_null,
+                                                               uint8_t *out_evaluations,
+                                                               size_t evaluation_count) {
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(s != nullptr && out_evaluations != nullptr);
+        if (s->poisoned) fail(HP_CUDA_STATUS_INVALID_STATE);
+        require(evaluation_count == s->max_degree + 1);
+        if (s->round >= s->num_vars) fail(HP_CUDA_STATUS_INVALID_STATE);
+        if (s->round == 0 && challenge_or_null != nullptr) fail(HP_CUDA_STATUS_INVALID_STATE);
+        if (s->round > 0 && challenge_or_null == nullptr) fail(HP_CUDA_STATUS_INVALID_STATE);
+        Fr r = Fr::zero();
+        if (challenge_or_null) r = hp::host_scalar(challenge_or_null);
+        try {
+            const hp::SumcheckDesc &d = s->desc;
+            const bool fold = s->round > 0;
+            const int src_which = s->current;
+            const int dst_which = fold ? (src_which == 1 ? 2 : 1) : src_which;
+            size_t pairs = hp::table_len(s->num_vars - s->round - 1);
+            hp::FrPtrList src{};
+            hp::FrMutPtrList dst{};
+            for (int f = 0; f < d.factor_count; f++) {
+                src.p[f] = hp::state_table(s, src_which, f);
+                dst.p[f] = const_cast<Fr *>(hp::state_table(s, dst_which, f));
+            }
+            size_t smem;
+            int T = hp::round_block_size(d, &smem);
+            if (smem > 48 * 1024)
+                check_cuda(cudaFuncSetAttribute(hp::k_sumcheck_round,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                int(smem)));
+            unsigned grid = hp::grid_for(ctx, pairs, unsigned(T), 2);
+            hp::Scratch partials(ctx, size_t(grid) * d.slot_count * sizeof(Fr));
+            hp::Scratch sums(ctx, d.slot_count * sizeof(Fr));
+            hp::Scratch outd(ctx, evaluation_count * sizeof(Fr));
+            hp::k_sumcheck_round<<<grid, T, smem, ctx->stream>>>(d, src, dst, fold, r, pairs,
+                                                                 partials.as<Fr>());
+            check_launch();
+            hp::k_sumcheck_finalize<<<1, 256, 256 * sizeof(Fr), ctx->stream>>>(
+                d, partials.as<Fr>(), int(grid), static_cast<const Fr *>(s->coefs),
+                int(s->max_degree), sums.as<Fr>(), outd.as<Fr>());
+            check_launch();
+            check_cuda(cudaMemcpyAsync(out_evaluations, outd.ptr, evaluation_count * sizeof(Fr),
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+            ctx->sync();
+            s->current = dst_which;
+            s->round++;
+        } catch (const hp::Failure &f) {
+            if (f.kind == HP_CUDA_STATUS_INVALID_STATE) s->poisoned = true;
+            throw;
+        }
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_final_evaluations(
+    HpCudaContext *ctx, HpCudaSumCheckProverState *s, const uint8_t *challenge,
+    uint8_t *out_evaluations, size_t factor_count) {
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(s != nullptr && challenge != nullptr && out_evaluations != nullptr);
+        if (s->poisoned || s->round != s->num_vars) fail(HP_CUDA_STATUS_INVALID_STATE);
+        require(factor_count == size_t(s->desc.factor_count));
+        if (factor_count == 0) return;
+        Fr r = hp::host_scalar(challenge);
+        hp::FrPtrList tl{};
+        for (int f = 0; f < s->desc.factor_count; f++) tl.p[f] = hp::state_table(s, s->current, f);
+        hp::Scratch outd(ctx, factor_count * sizeof(Fr));
+        hp::k_sumcheck_final_fold<<<1, 32, 0, ctx->stream>>>(tl, int(factor_count), r,
+                                                             outd.as<Fr>());
+        check_launch();
+        check_cuda(cudaMemcpyAsync(out_evaluations, outd.ptr, factor_count * sizeof(Fr),
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+        ctx->sync();
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_destroy(HpCudaContext *ctx,
+                                                                 HpCudaSumCheckProverState *s) {
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(s != nullptr);
+        hp::release_state(ctx, s);
+        delete s;
+    });
+}

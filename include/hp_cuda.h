@@ -1,0 +1,187 @@
+/*
+ * hp_cuda.h -- C ABI of the GB300 (sm_103a) HyperPlonk prover backend.
+ *
+ * Drop-in counterpart of the reference's Ascend bridge
+ * (backend/src/ascend910b3/native/bridge.h:43-62, bound from Rust in
+ * backend/src/ascend910b3/ffi.rs:34-173).  Every `hp_cuda_v1_*` entry below
+ * replaces the `hp_ascend910b3_v1_*` entry of the same suffix with the same
+ * argument order, meaning and error behaviour:
+ *
+ *  - Host packets, not device layouts: Fr is canonical little-endian 32 bytes;
+ *    G1 is 97 bytes = tag (0 finite, 1 infinity with zero coordinates) then x
+ *    and y as canonical little-endian 48-byte Fq.
+ *  - Host buffers are borrowed only until return.  Zero-count arrays may be
+ *    null, except product_offsets which always holds product_count + 1 entries
+ *    starting at 0.
+ *  - On success host outputs are completely written; device outputs (MLE
+ *    addresses) are unique, immutable and owned by the caller until retired.
+ *  - On failure partial resources are released and every resource output slot
+ *    is nulled.  No C++ exception crosses this ABI.
+ *  - A context is driven by one host thread and owns one CUDA stream; all
+ *    device work of the context is ordered on that stream.
+ *  - buffer_retire releases the caller's ownership; storage is returned to the
+ *    stream-ordered pool only after all work already queued on the context's
+ *    stream that uses it, and only when no prover state or parameter object
+ *    still references it.
+ *  - Zero denominators (including 0/0) are InvalidParameters.
+ *  - Sumcheck: the first round requires a null challenge, later rounds a
+ *    non-null one; misuse or exhaustion returns InvalidState without
+ *    advancing the state.  An execution failure poisons the state; later
+ *    rounds return InvalidState.
+ *
+ * Status: kind 0 success, 1 InvalidParameters, 2 InvalidState, 3
+ * NotImplemented (bridge.h:29-34); native_code carries the CUDA error code of
+ * a failed runtime call, or 0.
+ *
+ * Device layout (not part of the ABI contract): MLE tables are Montgomery Fr
+ * (R = 2^256), eight little-endian 32-bit limbs, 32 bytes per entry,
+ * low-bit-first evaluation order; SRS layers are affine Montgomery Fq points,
+ * 96 bytes each.
+ */
+#ifndef HP_CUDA_H
+#define HP_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#define HP_CUDA_STATUS_SUCCESS 0
+#define HP_CUDA_STATUS_INVALID_PARAMETERS 1
+#define HP_CUDA_STATUS_INVALID_STATE 2
+#define HP_CUDA_STATUS_NOT_IMPLEMENTED 3
+
+typedef struct HpCudaStatus {
+    int32_t kind;
+    int32_t native_code;
+} HpCudaStatus;
+
+typedef struct HpCudaContext HpCudaContext;
+typedef struct HpCudaMultilinearKzgPreparedProverParam HpCudaMultilinearKzgPreparedProverParam;
+typedef struct HpCudaSumCheckProverState HpCudaSumCheckProverState;
+typedef void *HpCudaDeviceAddress;
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- context and buffers (bridge.h:43-45) ------------------------------ */
+
+/* Replaces hp_ascend910b3_v1_context_create (bridge.h:43). */
+HpCudaStatus hp_cuda_v1_context_create(int32_t device_id, HpCudaContext **out);
+/* Replaces hp_ascend910b3_v1_context_destroy (bridge.h:44): drains the stream,
+ * frees every buffer the context still holds. */
+HpCudaStatus hp_cuda_v1_context_destroy(HpCudaContext *ctx);
+/* Replaces hp_ascend910b3_v1_buffer_retire (bridge.h:45). */
+HpCudaStatus hp_cuda_v1_buffer_retire(HpCudaContext *ctx, HpCudaDeviceAddress address);
+
+/* ---- MLE tables (bridge.h:46-53; traits backend/src/multilinear_polynomial.rs:33-121) */
+
+/* Replaces hp_ascend910b3_v1_mle_upload (bridge.h:46): evaluation_count must be
+ * 2^num_vars canonical Fr. */
+HpCudaStatus hp_cuda_v1_mle_upload(HpCudaContext *ctx, size_t num_vars, const uint8_t *evaluations,
+                                   size_t evaluation_count, HpCudaDeviceAddress *out);
+/* Replaces hp_ascend910b3_v1_mle_linear_combination (bridge.h:47). */
+HpCudaStatus hp_cuda_v1_mle_linear_combination(HpCudaContext *ctx, size_t num_vars,
+                                               const HpCudaDeviceAddress *polynomials,
+                                               const uint8_t *coefficients, size_t count,
+                                               HpCudaDeviceAddress *out);
+/* Replaces hp_ascend910b3_v1_mle_evaluate (bridge.h:48). */
+HpCudaStatus hp_cuda_v1_mle_evaluate(HpCudaContext *ctx, HpCudaDeviceAddress polynomial,
+                                     size_t num_vars, const uint8_t *point,
+                                     uint8_t *out_evaluation);
+/* Replaces hp_ascend910b3_v1_mle_build_eq_x_r (bridge.h:49). */
+HpCudaStatus hp_cuda_v1_mle_build_eq_x_r(HpCudaContext *ctx, const uint8_t *r, size_t num_vars,
+                                         HpCudaDeviceAddress *out);
+/* Replaces hp_ascend910b3_v1_mle_compute_frac_poly (bridge.h:50). */
+HpCudaStatus hp_cuda_v1_mle_compute_frac_poly(HpCudaContext *ctx, size_t num_vars,
+                                              const HpCudaDeviceAddress *numerators,
+                                              const HpCudaDeviceAddress *denominators,
+                                              size_t count, HpCudaDeviceAddress *out);
+/* Replaces hp_ascend910b3_v1_mle_compute_product_poly (bridge.h:51). */
+HpCudaStatus hp_cuda_v1_mle_compute_product_poly(HpCudaContext *ctx, HpCudaDeviceAddress frac,
+                                                 size_t num_vars, HpCudaDeviceAddress *out);
+/* Replaces hp_ascend910b3_v1_mle_compute_nums_and_denoms (bridge.h:52). */
+HpCudaStatus hp_cuda_v1_mle_compute_nums_and_denoms(
+    HpCudaContext *ctx, size_t num_vars, const uint8_t *beta, const uint8_t *gamma,
+    const HpCudaDeviceAddress *fxs, const HpCudaDeviceAddress *gxs,
+    const HpCudaDeviceAddress *permutations, size_t count, HpCudaDeviceAddress *out_numerators,
+    HpCudaDeviceAddress *out_denominators);
+/* Replaces hp_ascend910b3_v1_mle_compute_product_factors (bridge.h:53). */
+HpCudaStatus hp_cuda_v1_mle_compute_product_factors(HpCudaContext *ctx, HpCudaDeviceAddress frac,
+                                                    HpCudaDeviceAddress product, size_t num_vars,
+                                                    HpCudaDeviceAddress *out_p1,
+                                                    HpCudaDeviceAddress *out_p2);
+
+/* ---- multilinear KZG (bridge.h:54-59; trait backend/src/multilinear_kzg.rs:20-55) */
+
+/* Replaces hp_ascend910b3_v1_multilinear_kzg_params_create (bridge.h:54). */
+HpCudaStatus hp_cuda_v1_multilinear_kzg_params_create(
+    HpCudaContext *ctx, size_t num_vars, HpCudaMultilinearKzgPreparedProverParam **out);
+/* Replaces hp_ascend910b3_v1_multilinear_kzg_params_upload_layer (bridge.h:55):
+ * layer_index in 0..=num_vars carries 2^(num_vars - layer_index) 97-byte points. */
+HpCudaStatus hp_cuda_v1_multilinear_kzg_params_upload_layer(
+    HpCudaContext *ctx, HpCudaMultilinearKzgPreparedProverParam *params, size_t layer_index,
+    const uint8_t *points, size_t point_count);
+/* Replaces hp_ascend910b3_v1_multilinear_kzg_params_destroy (bridge.h:56). */
+HpCudaStatus hp_cuda_v1_multilinear_kzg_params_destroy(
+    HpCudaContext *ctx, HpCudaMultilinearKzgPreparedProverParam *params);
+/* Replaces hp_ascend910b3_v1_multilinear_kzg_commit (bridge.h:57). */
+HpCudaStatus hp_cuda_v1_multilinear_kzg_commit(
+    HpCudaContext *ctx, const HpCudaMultilinearKzgPreparedProverParam *params,
+    HpCudaDeviceAddress polynomial, size_t num_vars, uint8_t *out_commitment);
+/* Replaces hp_ascend910b3_v1_multilinear_kzg_multi_commit (bridge.h:58). */
+HpCudaStatus hp_cuda_v1_multilinear_kzg_multi_commit(
+    HpCudaContext *ctx, const HpCudaMultilinearKzgPreparedProverParam *params,
+    const HpCudaDeviceAddress *polynomials, const size_t *num_vars, size_t count,
+    uint8_t *out_commitments);
+/* Replaces hp_ascend910b3_v1_multilinear_kzg_open (bridge.h:59). */
+HpCudaStatus hp_cuda_v1_multilinear_kzg_open(
+    HpCudaContext *ctx, const HpCudaMultilinearKzgPreparedProverParam *params,
+    HpCudaDeviceAddress polynomial, size_t num_vars, const uint8_t *point,
+    uint8_t *out_quotients, uint8_t *out_evaluation);
+
+/* ---- sumcheck prover (bridge.h:60-62; trait backend/src/sum_check.rs:17-38) */
+
+/* Replaces hp_ascend910b3_v1_sumcheck_prover_state_create (bridge.h:60). */
+HpCudaStatus hp_cuda_v1_sumcheck_prover_state_create(
+    HpCudaContext *ctx, size_t num_vars, size_t max_degree, const HpCudaDeviceAddress *factors,
+    size_t factor_count, const uint8_t *coefficients, const size_t *product_offsets,
+    size_t product_count, const size_t *factor_indices, size_t index_count,
+    HpCudaSumCheckProverState **out);
+/* Replaces hp_ascend910b3_v1_sumcheck_prover_state_round (bridge.h:61). */
+HpCudaStatus hp_cuda_v1_sumcheck_prover_state_round(HpCudaContext *ctx,
+                                                    HpCudaSumCheckProverState *state,
+                                                    const uint8_t *challenge_or_null,
+                                                    uint8_t *out_evaluations,
+                                                    size_t evaluation_count);
+/* Replaces hp_ascend910b3_v1_sumcheck_prover_state_destroy (bridge.h:62). */
+HpCudaStatus hp_cuda_v1_sumcheck_prover_state_destroy(HpCudaContext *ctx,
+                                                      HpCudaSumCheckProverState *state);
+
+/* ---- additions of this backend ----------------------------------------- */
+
+/* Final folded evaluations of every distinct factor after the last round:
+ * fixes the last variable with `challenge` (r_nv) and writes factor_count
+ * canonical Fr in the factor order given at create.  Equal to evaluate_mle of
+ * each factor at the full challenge point (the reference obtains them through
+ * evaluate_mle, backend/src/cpu/multilinear_polynomial.rs:84-100).  Requires
+ * all num_vars rounds to have run; does not advance the state. */
+HpCudaStatus hp_cuda_v1_sumcheck_prover_state_final_evaluations(
+    HpCudaContext *ctx, HpCudaSumCheckProverState *state, const uint8_t *challenge,
+    uint8_t *out_evaluations, size_t factor_count);
+
+/* Copy a resident MLE back as canonical Fr (2^num_vars * 32 bytes).  The
+ * reference exposes no such call (its tests re-evaluate instead); this one
+ * lets callers and tests check tables byte for byte. */
+HpCudaStatus hp_cuda_v1_mle_download(HpCudaContext *ctx, HpCudaDeviceAddress polynomial,
+                                     size_t num_vars, uint8_t *out_evaluations,
+                                     size_t evaluation_count);
+
+/* The context's CUDA stream (a cudaStream_t), so a caller can order its own
+ * work or timing events with the backend's. */
+HpCudaStatus hp_cuda_v1_context_stream(HpCudaContext *ctx, void **out_stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HP_CUDA_H */
