@@ -49,6 +49,7 @@ SIGNATURES: dict[str, list] = {
     "hp_cuda_v1_sumcheck_prover_state_round": [c_voidp, c_voidp, c_u8p, c_u8p, c_size],
     "hp_cuda_v1_sumcheck_prover_state_destroy": [c_voidp, c_voidp],
     "hp_cuda_v1_sumcheck_prover_state_final_evaluations": [c_voidp, c_voidp, c_u8p, c_u8p, c_size],
+    "hp_cuda_v1_msm": [c_voidp, c_u8p, c_u8p, c_size, c_u8p],
 }
 
 _lib = None

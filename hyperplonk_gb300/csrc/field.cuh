@@ -262,10 +262,14 @@ __device__ __forceinline__ bool is_canonical(const Field<P> &a) {
 template <class P>
 __device__ __noinline__ Field<P> inverse(const Field<P> &a) {
     constexpr int N = P::N;
+    // exponent p - 2 with the borrow carried across limbs (Fr's low limb is 1)
+    uint32_t exp[N];
+    exp[0] = sub_cc(P::p(0), 2u);
+#pragma unroll
+    for (int i = 1; i < N; i++) exp[i] = subc_cc(P::p(i), 0u);
     Field<P> acc = Field<P>::one();
     for (int i = N - 1; i >= 0; i--) {
-        uint32_t e = P::p(i);
-        if (i == 0) e -= 2;
+        uint32_t e = exp[i];
         for (int bit = 31; bit >= 0; bit--) {
             acc = acc * acc;
             if ((e >> bit) & 1) acc = acc * a;

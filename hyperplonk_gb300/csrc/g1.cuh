@@ -1,0 +1,184 @@
+// g1.cuh -- BLS12-381 G1 (y^2 = x^3 + 4 over Fq) on the device.
+//
+// Buckets use XYZZ coordinates (x = X/ZZ, y = Y/ZZZ, ZZ^3 = ZZZ^2; ZZ = 0 is
+// the point at infinity): a mixed addition of an affine base costs 8M + 2S
+// and needs no inversion.  Formulas: the public Explicit-Formulas Database,
+// "xyzz" shape for short Weierstrass curves with a = 0 (madd-2008-s,
+// add-2008-s, dbl-2008-s-1, mdbl-2008-s-1), with the exceptional cases
+// (doubling through an addition, P + (-P), infinity) handled explicitly so
+// every addition is complete.  The reference's own device curve code is
+// backend/src/ascend910b3/native/g1.h (Jacobian, cuZK-derived formulas); the
+// values produced are the same group elements.
+#pragma once
+#include "field.cuh"
+
+namespace hp {
+
+struct Affine {  // (0, 0) encodes infinity (not on the curve since 0 != 4)
+    Fq x, y;
+};
+
+struct Xyzz {
+    Fq x, y, zz, zzz;
+};
+
+__device__ __forceinline__ bool affine_is_inf(const Affine &p) { return p.x.is_zero() && p.y.is_zero(); }
+__device__ __forceinline__ bool xyzz_is_inf(const Xyzz &p) { return p.zz.is_zero(); }
+
+__device__ __forceinline__ Xyzz xyzz_inf() {
+    Xyzz r;
+    r.x = Fq::one();
+    r.y = Fq::one();
+    r.zz = Fq::zero();
+    r.zzz = Fq::zero();
+    return r;
+}
+
+__device__ __forceinline__ Xyzz xyzz_from_affine(const Affine &a) {
+    if (affine_is_inf(a)) return xyzz_inf();
+    Xyzz r;
+    r.x = a.x;
+    r.y = a.y;
+    r.zz = Fq::one();
+    r.zzz = Fq::one();
+    return r;
+}
+
+// mdbl-2008-s-1: 2 * (x, y) for an affine input.
+__device__ __forceinline__ Xyzz xyzz_double_affine(const Fq &x, const Fq &y) {
+    Fq u = y + y;
+    Fq v = u * u;
+    Fq w = u * v;
+    Fq s = x * v;
+    Fq xx = x * x;
+    Fq m = xx + xx + xx;
+    Xyzz r;
+    r.x = m * m - (s + s);
+    r.y = m * (s - r.x) - w * y;
+    r.zz = v;
+    r.zzz = w;
+    return r;
+}
+
+// dbl-2008-s-1
+__device__ __forceinline__ Xyzz xyzz_double(const Xyzz &p) {
+    if (xyzz_is_inf(p)) return p;
+    Fq u = p.y + p.y;
+    Fq v = u * u;
+    Fq w = u * v;
+    Fq s = p.x * v;
+    Fq xx = p.x * p.x;
+    Fq m = xx + xx + xx;
+    Xyzz r;
+    r.x = m * m - (s + s);
+    r.y = m * (s - r.x) - w * p.y;
+    r.zz = v * p.zz;
+    r.zzz = w * p.zzz;
+    return r;
+}
+
+// madd-2008-s: p + (x2, y2) with (x2, y2) finite affine.
+__device__ __forceinline__ Xyzz xyzz_add_affine(const Xyzz &p, const Fq &x2, const Fq &y2) {
+    if (xyzz_is_inf(p)) {
+        Xyzz r;
+        r.x = x2;
+        r.y = y2;
+        r.zz = Fq::one();
+        r.zzz = Fq::one();
+        return r;
+    }
+    Fq u2 = x2 * p.zz;
+    Fq s2 = y2 * p.zzz;
+    Fq pp_ = u2 - p.x;
+    Fq rr = s2 - p.y;
+    if (pp_.is_zero()) {
+        if (rr.is_zero()) return xyzz_double_affine(x2, y2);
+        return xyzz_inf();
+    }
+    Fq pp = pp_ * pp_;
+    Fq ppp = pp_ * pp;
+    Fq q = p.x * pp;
+    Xyzz r;
+    r.x = rr * rr - ppp - (q + q);
+    r.y = rr * (q - r.x) - p.y * ppp;
+    r.zz = p.zz * pp;
+    r.zzz = p.zzz * ppp;
+    return r;
+}
+
+// add-2008-s: general XYZZ addition.
+__device__ __forceinline__ Xyzz xyzz_add(const Xyzz &p, const Xyzz &q) {
+    if (xyzz_is_inf(p)) return q;
+    if (xyzz_is_inf(q)) return p;
+    Fq u1 = p.x * q.zz;
+    Fq u2 = q.x * p.zz;
+    Fq s1 = p.y * q.zzz;
+    Fq s2 = q.y * p.zzz;
+    Fq pp_ = u2 - u1;
+    Fq rr = s2 - s1;
+    if (pp_.is_zero()) {
+        if (rr.is_zero()) return xyzz_double(p);
+        return xyzz_inf();
+    }
+    Fq pp = pp_ * pp_;
+    Fq ppp = pp_ * pp;
+    Fq qq = u1 * pp;
+    Xyzz r;
+    r.x = rr * rr - ppp - (qq + qq);
+    r.y = rr * (qq - r.x) - s1 * ppp;
+    r.zz = p.zz * q.zz * pp;
+    r.zzz = p.zzz * q.zzz * ppp;
+    return r;
+}
+
+// ---- global memory access (16-byte vectors) ----
+template <class F>
+__device__ __forceinline__ void load_words(F &dst, const uint32_t *src) {
+    const uint4 *q = reinterpret_cast<const uint4 *>(src);
+#pragma unroll
+    for (int i = 0; i < F::N / 4; i++) {
+        uint4 v = q[i];
+        dst.v[4 * i] = v.x;
+        dst.v[4 * i + 1] = v.y;
+        dst.v[4 * i + 2] = v.z;
+        dst.v[4 * i + 3] = v.w;
+    }
+}
+template <class F>
+__device__ __forceinline__ void store_words(uint32_t *dst, const F &src) {
+    uint4 *q = reinterpret_cast<uint4 *>(dst);
+#pragma unroll
+    for (int i = 0; i < F::N / 4; i++)
+        q[i] = make_uint4(src.v[4 * i], src.v[4 * i + 1], src.v[4 * i + 2], src.v[4 * i + 3]);
+}
+
+__device__ __forceinline__ Affine load_affine(const Affine *p) {
+    Affine a;
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(p);
+    load_words(a.x, w);
+    load_words(a.y, w + 12);
+    return a;
+}
+__device__ __forceinline__ void store_affine(Affine *p, const Affine &a) {
+    uint32_t *w = reinterpret_cast<uint32_t *>(p);
+    store_words(w, a.x);
+    store_words(w + 12, a.y);
+}
+__device__ __forceinline__ Xyzz load_xyzz(const Xyzz *p) {
+    Xyzz a;
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(p);
+    load_words(a.x, w);
+    load_words(a.y, w + 12);
+    load_words(a.zz, w + 24);
+    load_words(a.zzz, w + 36);
+    return a;
+}
+__device__ __forceinline__ void store_xyzz(Xyzz *p, const Xyzz &a) {
+    uint32_t *w = reinterpret_cast<uint32_t *>(p);
+    store_words(w, a.x);
+    store_words(w + 12, a.y);
+    store_words(w + 24, a.zz);
+    store_words(w + 36, a.zzz);
+}
+
+}  // namespace hp

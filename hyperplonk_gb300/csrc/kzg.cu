@@ -1,0 +1,238 @@
+// kzg.cu -- multilinear-KZG prepared parameters, commit, multi_commit, open.
+//
+// Reference: backend/src/cpu/multilinear_kzg.rs:40-137 (semantics) and
+// backend/src/ascend910b3/native/bridge_kzg.cpp:253-676 (ABI behaviour).
+//  - params hold num_vars + 1 SRS layers; layer k has 2^(num_vars - k) bases
+//    and is prepared once (Montgomery affine + precomputed MSM windows) and
+//    stays resident in HBM;
+//  - commit(poly with nv vars) = MSM against layer (num_vars - nv);
+//  - open runs nv rounds of q[b] = f[2b+1] - f[2b], f[b] = f[2b] + q[b]*z_i
+//    (one fused kernel) and an MSM of q against layer (num_vars - nv + 1 + i);
+//    quotients stay on the device as MSM scalars, only the partial sums and
+//    the final scalar come back.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "host_ec.h"
+#include "mle.cuh"
+#include "msm.cuh"
+#include "runtime.cuh"
+
+using hp::check_cuda;
+using hp::check_launch;
+using hp::fail;
+using hp::Fr;
+using hp::guard;
+using hp::require;
+
+struct HpCudaMultilinearKzgPreparedProverParam {
+    size_t num_vars = 0;
+    std::vector<hp::MsmLayer> layers;
+    std::vector<bool> uploaded;
+};
+
+namespace hp {
+
+__global__ void k_open_fold(const Fr *f, Fr *fnext, Fr *q, size_t half, Fr z) {
+    for (size_t b = blockIdx.x * size_t(blockDim.x) + threadIdx.x; b < half;
+         b += size_t(gridDim.x) * blockDim.x) {
+        Fr lo = load_fr(&f[2 * b]);
+        Fr d = load_fr(&f[2 * b + 1]) - lo;
+        store_fr(&q[b], d);
+        store_fr(&fnext[b], lo + d * z);
+    }
+}
+
+static const MsmLayer &ready_layer(const HpCudaMultilinearKzgPreparedProverParam *p, size_t k) {
+    if (k >= p->layers.size() || !p->uploaded[k]) fail(HP_CUDA_STATUS_INVALID_STATE);
+    return p->layers[k];
+}
+
+// Download `total` XYZZ partials and finish each MSM into a packet.
+static void finish_msms(HpCudaContext *ctx, const Xyzz *dev, const std::vector<MsmShape> &shapes,
+                        uint8_t *out97) {
+    size_t total = 0;
+    for (auto &s : shapes) total += size_t(s.partials);
+    std::vector<host::Xyzz64> hostp(std::max<size_t>(total, 1));
+    if (total)
+        check_cuda(cudaMemcpyAsync(hostp.data(), dev, total * sizeof(Xyzz), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    size_t off = 0;
+    for (size_t i = 0; i < shapes.size(); i++) {
+        msm_finalize_host(shapes[i], hostp.data() + off, out97 + 97 * i);
+        off += size_t(shapes[i].partials);
+    }
+}
+
+}  // namespace hp
+
+extern "C" HpCudaStatus hp_cuda_v1_multilinear_kzg_params_create(
+    HpCudaContext *ctx, size_t num_vars, HpCudaMultilinearKzgPreparedProverParam **out) {
+    if (out) *out = nullptr;
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(out != nullptr && num_vars <= hp::kMaxNumVars);
+        auto *p = new HpCudaMultilinearKzgPreparedProverParam();
+        p->num_vars = num_vars;
+        p->layers.resize(num_vars + 1);
+        p->uploaded.assign(num_vars + 1, false);
+        *out = p;
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_multilinear_kzg_params_upload_layer(
+    HpCudaContext *ctx, HpCudaMultilinearKzgPreparedProverParam *params, size_t layer_index,
+    const uint8_t *points, size_t point_count) {
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(params != nullptr && points != nullptr && layer_index <= params->num_vars);
+        require(point_count == hp::table_len(params->num_vars - layer_index));
+        require(!params->uploaded[layer_index]);
+        hp::MsmLayer layer;
+        bool ok;
+        try {
+            ok = hp::msm_prepare_layer(ctx, layer, points, point_count);
+        } catch (...) {
+            hp::msm_release_layer(ctx, layer);
+            throw;
+        }
+        if (!ok) {
+            hp::msm_release_layer(ctx, layer);
+            fail(HP_CUDA_STATUS_INVALID_PARAMETERS);
+        }
+        params->layers[layer_index] = layer;
+        params->uploaded[layer_index] = true;
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_multilinear_kzg_params_destroy(
+    HpCudaContext *ctx, HpCudaMultilinearKzgPreparedProverParam *params) {
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(params != nullptr);
+        for (auto &l : params->layers) hp::msm_release_layer(ctx, l);
+        delete params;
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_multilinear_kzg_commit(
+    HpCudaContext *ctx, const HpCudaMultilinearKzgPreparedProverParam *params,
+    HpCudaDeviceAddress polynomial, size_t num_vars, uint8_t *out_commitment) {
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(params != nullptr && out_commitment != nullptr && num_vars <= params->num_vars);
+        const Fr *scalars = hp::mle_ptr(ctx, polynomial, num_vars);
+        const hp::MsmLayer &layer = hp::ready_layer(params, params->num_vars - num_vars);
+        hp::MsmShape sh = hp::msm_shape(layer);
+        hp::Scratch parts(ctx, size_t(sh.partials) * sizeof(hp::Xyzz));
+        hp::msm_run(ctx, layer, scalars, parts.as<hp::Xyzz>());
+        hp::finish_msms(ctx, parts.as<hp::Xyzz>(), {sh}, out_commitment);
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_multilinear_kzg_multi_commit(
+    HpCudaContext *ctx, const HpCudaMultilinearKzgPreparedProverParam *params,
+    const HpCudaDeviceAddress *polynomials, const size_t *num_vars, size_t count,
+    uint8_t *out_commitments) {
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(params != nullptr);
+        if (count == 0) return;
+        require(polynomials != nullptr && num_vars != nullptr && out_commitments != nullptr);
+        std::vector<const Fr *> scalars(count);
+        std::vector<const hp::MsmLayer *> layers(count);
+        std::vector<hp::MsmShape> shapes(count);
+        size_t total = 0;
+        for (size_t i = 0; i < count; i++) {
+            require(num_vars[i] <= params->num_vars);
+            scalars[i] = hp::mle_ptr(ctx, polynomials[i], num_vars[i]);
+            layers[i] = &hp::ready_layer(params, params->num_vars - num_vars[i]);
+            shapes[i] = hp::msm_shape(*layers[i]);
+            total += size_t(shapes[i].partials);
+        }
+        hp::Scratch parts(ctx, total * sizeof(hp::Xyzz));
+        size_t off = 0;
+        for (size_t i = 0; i < count; i++) {
+            hp::msm_run(ctx, *layers[i], scalars[i], parts.as<hp::Xyzz>() + off);
+            off += size_t(shapes[i].partials);
+        }
+        hp::finish_msms(ctx, parts.as<hp::Xyzz>(), shapes, out_commitments);
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_multilinear_kzg_open(
+    HpCudaContext *ctx, const HpCudaMultilinearKzgPreparedProverParam *params,
+    HpCudaDeviceAddress polynomial, size_t num_vars, const uint8_t *point, uint8_t *out_quotients,
+    uint8_t *out_evaluation) {
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(params != nullptr && out_evaluation != nullptr && num_vars <= params->num_vars);
+        require(num_vars == 0 || (point != nullptr && out_quotients != nullptr));
+        const Fr *f = hp::mle_ptr(ctx, polynomial, num_vars);
+        std::vector<Fr> z(num_vars);
+        for (size_t i = 0; i < num_vars; i++) z[i] = hp::host_scalar(point + 32 * i);
+        if (num_vars == 0) {
+            hp::download_canonical(ctx, f, 1, out_evaluation);
+            return;
+        }
+        const size_t nv = num_vars, ignored = params->num_vars - nv + 1;
+        std::vector<const hp::MsmLayer *> layers(nv);
+        std::vector<hp::MsmShape> shapes(nv);
+        size_t total = 0;
+        for (size_t i = 0; i < nv; i++) {
+            layers[i] = &hp::ready_layer(params, ignored + i);
+            shapes[i] = hp::msm_shape(*layers[i]);
+            total += size_t(shapes[i].partials);
+        }
+        hp::Scratch parts(ctx, total * sizeof(hp::Xyzz));
+        hp::Scratch fa(ctx, hp::table_len(nv - 1) * sizeof(Fr));
+        hp::Scratch fb(ctx, hp::table_len(nv >= 2 ? nv - 2 : 0) * sizeof(Fr));
+        hp::Scratch q(ctx, hp::table_len(nv - 1) * sizeof(Fr));
+        const Fr *cur = f;
+        Fr *bufs[2] = {fa.as<Fr>(), fb.as<Fr>()};
+        size_t off = 0;
+        for (size_t i = 0; i < nv; i++) {
+            size_t half = hp::table_len(nv - 1 - i);
+            Fr *next = bufs[i & 1];
+            hp::k_open_fold<<<hp::grid_for(ctx, half, 256), 256, 0, ctx->stream>>>(cur, next, q.as<Fr>(), half,
+                                                                                   z[i]);
+            check_launch();
+            hp::msm_run(ctx, *layers[i], q.as<Fr>(), parts.as<hp::Xyzz>() + off);
+            off += size_t(shapes[i].partials);
+            cur = next;
+        }
+        hp::download_canonical(ctx, cur, 1, out_evaluation);
+        hp::finish_msms(ctx, parts.as<hp::Xyzz>(), shapes, out_quotients);
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_msm(HpCudaContext *ctx, const uint8_t *bases, const uint8_t *scalars,
+                                       size_t count, uint8_t *out_point) {
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(out_point != nullptr);
+        if (count == 0) {
+            std::memset(out_point, 0, 97);
+            out_point[0] = 1;
+            return;
+        }
+        require(bases != nullptr && scalars != nullptr && count < (size_t(1) << 27));
+        hp::MsmLayer layer;
+        struct Release {
+            HpCudaContext *c;
+            hp::MsmLayer *l;
+            ~Release() { hp::msm_release_layer(c, *l); }
+        } release{ctx, &layer};
+        if (!hp::msm_prepare_layer(ctx, layer, bases, count)) fail(HP_CUDA_STATUS_INVALID_PARAMETERS);
+        hp::Scratch s(ctx, count * sizeof(Fr));
+        ctx->clear_flags();
+        check_cuda(cudaMemcpyAsync(s.ptr, scalars, count * sizeof(Fr), cudaMemcpyHostToDevice, ctx->stream));
+        hp::mle_to_mont_checked(ctx, s.as<Fr>(), count);
+        if (ctx->sync_flags() & hp::kFlagNonCanonical) fail(HP_CUDA_STATUS_INVALID_PARAMETERS);
+        hp::MsmShape sh = hp::msm_shape(layer);
+        hp::Scratch parts(ctx, size_t(sh.partials) * sizeof(hp::Xyzz));
+        hp::msm_run(ctx, layer, s.as<Fr>(), parts.as<hp::Xyzz>());
+        hp::finish_msms(ctx, parts.as<hp::Xyzz>(), {sh}, out_point);
+    });
+}

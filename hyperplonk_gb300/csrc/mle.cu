@@ -293,6 +293,11 @@ void host_scalars_to_device(HpCudaContext *ctx, const uint8_t *canonical, size_t
     ctx->sync();
 }
 
+void mle_to_mont_checked(HpCudaContext *ctx, Fr *data, size_t n) {
+    k_to_mont_check<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(data, n, ctx->d_flags);
+    check_launch();
+}
+
 void download_canonical(HpCudaContext *ctx, const Fr *src, size_t n, uint8_t *out) {
     Scratch tmp(ctx, n * sizeof(Fr));
     k_from_mont<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(src, tmp.as<Fr>(), n);

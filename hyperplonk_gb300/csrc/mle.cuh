@@ -26,6 +26,9 @@ struct FrScalarList {
 Fr host_scalar(const uint8_t *canonical);
 // Canonical scalars -> Montgomery, copied to a device array (synchronous).
 void host_scalars_to_device(HpCudaContext *ctx, const uint8_t *canonical, size_t count, Fr *dst);
+// In place canonical -> Montgomery on the context stream; non-canonical
+// entries raise kFlagNonCanonical in the context status word.
+void mle_to_mont_checked(HpCudaContext *ctx, Fr *data, size_t n);
 // Device Montgomery table -> canonical host bytes (synchronous).
 void download_canonical(HpCudaContext *ctx, const Fr *src, size_t n, uint8_t *out);
 // Fix all nv variables (point[0] <-> bit 0) and leave the scalar at dst (device).

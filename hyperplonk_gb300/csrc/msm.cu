@@ -1,0 +1,423 @@
+// msm.cu -- variable-base MSM sum_i s_i * P_i over BLS12-381 G1.
+//
+// Reference value semantics: ark-ec 0.6.0 VariableBaseMSM::msm_unchecked as
+// called by backend/src/cpu/multilinear_kzg.rs:55,131.  The reference's
+// device MSM (backend/src/ascend910b3/native/msm*.{cpp,asc}) uses unsigned
+// windows, LSD radix grouping and an affine bucket tree; this is a different,
+// GB300-first design:
+//
+//  1. prepare (once per SRS layer): window w of base i is 2^(c*w) * P_i,
+//     stored affine in HBM, so all ceil(256/c) windows of the signed-digit
+//     expansion share ONE set of 2^(c-1) buckets and there is no window
+//     combination;
+//  2. digits: signed c-bit digits in [-2^(c-1), 2^(c-1)]; a counting sort
+//     (histogram -> exclusive scan -> atomic scatter) groups the
+//     (window, point, sign) records by bucket -- bucket order inside a group
+//     is irrelevant because field arithmetic is exact;
+//  3. accumulate: one thread per bucket, XYZZ mixed additions (8M + 2S);
+//  4. reduce: sum_b (b+1) S_b via segments of `seg` buckets (running sums,
+//     two XYZZ additions per bucket), then the segment weights j are split
+//     into bits: sum_j j R_j = sum_k 2^k sum_{j : bit k} R_j, whose subset sums
+//     are parallel tree reductions;
+//  5. the host finishes the short Horner chain over those subset sums and
+//     converts to affine (one inversion), see host_ec.h.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "msm.cuh"
+#include "runtime.cuh"
+
+namespace hp {
+
+int msm_window_bits(size_t n) {
+    int best = 4;
+    double best_cost = 1e300;
+    for (int c = 4; c <= 20; c++) {
+        double cost = double(msm_windows(c)) * 10.0 * double(n) + 28.0 * double(size_t(1) << (c - 1));
+        if (cost < best_cost) {
+            best_cost = cost;
+            best = c;
+        }
+    }
+    return best;
+}
+
+MsmShape msm_shape(const MsmLayer &layer) {
+    MsmShape s;
+    s.buckets = size_t(1) << (layer.c - 1);
+    s.seg = s.buckets >= 16 ? 16 : s.buckets;
+    s.segments = s.buckets / s.seg;
+    s.seg_bits = 0;
+    while ((size_t(1) << s.seg_bits) < s.segments) s.seg_bits++;
+    s.partials = s.seg_bits + 1;
+    return s;
+}
+
+// ---------------------------------------------------------------------------
+// Prepare: packets -> window 0 -> windows 1..W-1
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ bool fq_canonical_le(const uint8_t *b, Fq &out) {
+    Fq v;
+#pragma unroll
+    for (int i = 0; i < 12; i++)
+        v.v[i] = uint32_t(b[4 * i]) | (uint32_t(b[4 * i + 1]) << 8) | (uint32_t(b[4 * i + 2]) << 16) |
+                 (uint32_t(b[4 * i + 3]) << 24);
+    out = v;
+    return is_canonical(v);
+}
+
+__global__ void k_unpack_packets(const uint8_t *packets, size_t n, Affine *out, uint32_t *flags) {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x) {
+        const uint8_t *p = packets + 97 * i;
+        Affine a;
+        a.x = Fq::zero();
+        a.y = Fq::zero();
+        uint8_t tag = p[0];
+        if (tag == 1) {
+            uint32_t any = 0;
+            for (int k = 1; k < 97; k++) any |= p[k];
+            if (any) atomicOr(flags, kFlagNonCanonical);
+        } else if (tag == 0) {
+            Fq x, y;
+            bool ok = fq_canonical_le(p + 1, x) & fq_canonical_le(p + 49, y);
+            if (!ok) atomicOr(flags, kFlagNonCanonical);
+            a.x = to_mont(x);
+            a.y = to_mont(y);
+            if (affine_is_inf(a)) atomicOr(flags, kFlagNonCanonical);  // (0,0) is not a finite point
+        } else {
+            atomicOr(flags, kFlagNonCanonical);
+        }
+        store_affine(&out[i], a);
+    }
+}
+
+// tmp[i] = 2^c * prev[i] (XYZZ)
+__global__ void k_window_double(const Affine *prev, Xyzz *tmp, size_t n, int c) {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x) {
+        Affine a = load_affine(&prev[i]);
+        Xyzz p;
+        if (affine_is_inf(a)) {
+            p = xyzz_inf();
+        } else {
+            p = xyzz_double_affine(a.x, a.y);
+            for (int k = 1; k < c; k++) p = xyzz_double(p);
+        }
+        store_xyzz(&tmp[i], p);
+    }
+}
+
+// XYZZ -> affine with one inversion per block (Montgomery trick over
+// kNormBlock * kNormChunk points).  `pre` is scratch of n Fq.
+constexpr int kNormBlock = 128;
+constexpr int kNormChunk = 4;
+
+__global__ void __launch_bounds__(kNormBlock) k_normalize(const Xyzz *in, Affine *out, Fq *pre, size_t n) {
+    __shared__ Fq spre[kNormBlock];
+    __shared__ Fq ssuf[kNormBlock];
+    __shared__ Fq total_inv;
+    const int t = threadIdx.x;
+    const size_t base = (size_t(blockIdx.x) * kNormBlock + t) * kNormChunk;
+    Fq one = Fq::one();
+    Fq p = one;
+    for (int k = 0; k < kNormChunk; k++) {
+        size_t i = base + k;
+        if (i < n) {
+            Xyzz q = load_xyzz(&in[i]);
+            Fq v = xyzz_is_inf(q) ? one : q.zz * q.zzz;
+            store_words(reinterpret_cast<uint32_t *>(&pre[i]), p);
+            p = p * v;
+        }
+    }
+    spre[t] = p;
+    ssuf[t] = p;
+    __syncthreads();
+    for (int off = 1; off < kNormBlock; off <<= 1) {
+        Fq a = (t >= off) ? spre[t - off] * spre[t] : spre[t];
+        Fq b = (t + off < kNormBlock) ? ssuf[t + off] * ssuf[t] : ssuf[t];
+        __syncthreads();
+        spre[t] = a;
+        ssuf[t] = b;
+        __syncthreads();
+    }
+    if (t == 0) total_inv = inverse(spre[kNormBlock - 1]);
+    __syncthreads();
+    Fq inv = total_inv;
+    if (t > 0) inv = inv * spre[t - 1];
+    if (t + 1 < kNormBlock) inv = inv * ssuf[t + 1];
+    for (int k = kNormChunk - 1; k >= 0; k--) {
+        size_t i = base + k;
+        if (i < n) {
+            Xyzz q = load_xyzz(&in[i]);
+            Affine a;
+            if (xyzz_is_inf(q)) {
+                a.x = Fq::zero();
+                a.y = Fq::zero();
+            } else {
+                Fq prefix;
+                load_words(prefix, reinterpret_cast<const uint32_t *>(&pre[i]));
+                Fq vinv = inv * prefix;            // (zz * zzz)^-1
+                inv = inv * (q.zz * q.zzz);
+                a.x = q.x * (vinv * q.zzz);        // X / ZZ
+                a.y = q.y * (vinv * q.zz);         // Y / ZZZ
+            }
+            store_affine(&out[i], a);
+        }
+    }
+}
+
+bool msm_prepare_layer(HpCudaContext *ctx, MsmLayer &layer, const uint8_t *packets, size_t n) {
+    layer.n = n;
+    layer.c = msm_window_bits(n);
+    layer.windows = msm_windows(layer.c);
+    layer.bases = static_cast<Affine *>(ctx->scratch(size_t(layer.windows) * n * sizeof(Affine)));
+    Scratch raw(ctx, n * 97);
+    check_cuda(cudaMemcpyAsync(raw.ptr, packets, n * 97, cudaMemcpyHostToDevice, ctx->stream));
+    ctx->clear_flags();
+    k_unpack_packets<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(raw.as<uint8_t>(), n, layer.bases,
+                                                                     ctx->d_flags);
+    check_launch();
+    if (layer.windows > 1) {
+        Scratch tmp(ctx, n * sizeof(Xyzz)), pre(ctx, n * sizeof(Fq));
+        size_t per_block = size_t(kNormBlock) * kNormChunk;
+        for (int w = 1; w < layer.windows; w++) {
+            k_window_double<<<grid_for(ctx, n, 128), 128, 0, ctx->stream>>>(
+                layer.bases + size_t(w - 1) * n, tmp.as<Xyzz>(), n, layer.c);
+            check_launch();
+            k_normalize<<<unsigned((n + per_block - 1) / per_block), kNormBlock, 0, ctx->stream>>>(
+                tmp.as<Xyzz>(), layer.bases + size_t(w) * n, pre.as<Fq>(), n);
+            check_launch();
+        }
+    }
+    uint32_t flags = ctx->sync_flags();
+    return (flags & kFlagNonCanonical) == 0;
+}
+
+void msm_release_layer(HpCudaContext *ctx, MsmLayer &layer) {
+    if (layer.bases) ctx->scratch_free(layer.bases);
+    layer.bases = nullptr;
+}
+
+// ---------------------------------------------------------------------------
+// Digits and counting sort
+// ---------------------------------------------------------------------------
+
+// bits [bit, bit + c) of a canonical 256-bit value (c <= 20)
+__device__ __forceinline__ uint32_t window_bits(const Fr &s, int bit, int c) {
+    if (bit >= 256) return 0;
+    int limb = bit >> 5, off = bit & 31;
+    uint32_t v = s.v[limb] >> off;
+    if (off + c > 32 && limb + 1 < 8) v |= s.v[limb + 1] << (32 - off);
+    return v & ((1u << c) - 1);
+}
+
+// Signed-digit recoding: calls f(window, magnitude, negative) for nonzero digits.
+template <class F>
+__device__ __forceinline__ void for_each_digit(const Fr &canon, int c, int windows, F &&f) {
+    const uint32_t half = 1u << (c - 1);
+    uint32_t carry = 0;
+    for (int w = 0; w < windows; w++) {
+        uint32_t raw = window_bits(canon, w * c, c) + carry;
+        if (raw > half) {
+            carry = 1;
+            uint32_t mag = (1u << c) - raw;
+            if (mag) f(w, mag, true);
+        } else {
+            carry = 0;
+            if (raw) f(w, raw, false);
+        }
+    }
+}
+
+__global__ void k_msm_histogram(const Fr *scalars, size_t n, int c, int windows, uint32_t *counts) {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x) {
+        Fr s = from_mont(load_fr(&scalars[i]));
+        for_each_digit(s, c, windows, [&](int, uint32_t mag, bool) { atomicAdd(&counts[mag - 1], 1u); });
+    }
+}
+
+// Exclusive scan of `m` counts by one block of 1024 threads; writes offsets
+// [0..m] (offsets[m] = total) and a copy of offsets[0..m) into cursor.
+__global__ void __launch_bounds__(1024) k_msm_scan(const uint32_t *counts, size_t m, uint32_t *offsets,
+                                                   uint32_t *cursor) {
+    __shared__ uint32_t part[1024];
+    const int t = threadIdx.x;
+    size_t chunk = (m + 1023) / 1024;
+    size_t b = t * chunk, e = min(m, b + chunk);
+    uint32_t s = 0;
+    for (size_t i = b; i < e; i++) s += counts[i];
+    part[t] = s;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        uint32_t v = t >= off ? part[t - off] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[t] - s;  // exclusive prefix of this chunk
+    for (size_t i = b; i < e; i++) {
+        offsets[i] = run;
+        cursor[i] = run;
+        run += counts[i];
+    }
+    if (t == 1023) offsets[m] = part[1023];
+}
+
+__global__ void k_msm_scatter(const Fr *scalars, size_t n, int c, int windows, uint32_t *cursor,
+                              uint32_t *records) {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * blockDim.x) {
+        Fr s = from_mont(load_fr(&scalars[i]));
+        for_each_digit(s, c, windows, [&](int w, uint32_t mag, bool neg) {
+            uint32_t pos = atomicAdd(&cursor[mag - 1], 1u);
+            records[pos] = uint32_t(size_t(w) * n + i) | (neg ? 0x80000000u : 0u);
+        });
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Bucket accumulation: one thread per bucket, XYZZ mixed additions
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(128) k_msm_accumulate(const Affine *bases, const uint32_t *offsets,
+                                                        const uint32_t *records, size_t buckets, Xyzz *out) {
+    for (size_t b = blockIdx.x * size_t(blockDim.x) + threadIdx.x; b < buckets;
+         b += size_t(gridDim.x) * blockDim.x) {
+        uint32_t begin = offsets[b], end = offsets[b + 1];
+        Xyzz acc = xyzz_inf();
+        for (uint32_t k = begin; k < end; k++) {
+            uint32_t rec = records[k];
+            Affine a = load_affine(&bases[rec & 0x7fffffffu]);
+            if (affine_is_inf(a)) continue;
+            if (rec & 0x80000000u) a.y = neg(a.y);
+            acc = xyzz_add_affine(acc, a.x, a.y);
+        }
+        store_xyzz(&out[b], acc);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Bucket reduction
+// ---------------------------------------------------------------------------
+
+// Segment j of `seg` buckets: run_j = sum S, acc_j = sum_l (l+1) S_{j*seg+l}.
+__global__ void __launch_bounds__(128) k_msm_segments(const Xyzz *buckets, size_t segments, size_t seg,
+                                                      Xyzz *acc_out, Xyzz *run_out) {
+    for (size_t j = blockIdx.x * size_t(blockDim.x) + threadIdx.x; j < segments;
+         j += size_t(gridDim.x) * blockDim.x) {
+        Xyzz run = xyzz_inf(), acc = xyzz_inf();
+        for (size_t l = seg; l-- > 0;) {
+            run = xyzz_add(run, load_xyzz(&buckets[j * seg + l]));
+            acc = xyzz_add(acc, run);
+        }
+        store_xyzz(&acc_out[j], acc);
+        store_xyzz(&run_out[j], run);
+    }
+}
+
+// Subset sums.  Subset y < bits: { run_j : bit y of j set } (segments/2
+// elements); subset y == bits: every acc_j.  Block (chunk, y) sums elements
+// [chunk * kSubsetPerBlock, ...) of subset y into partial[y * chunks + chunk].
+constexpr int kSubsetThreads = 128;
+constexpr int kSubsetPerThread = 8;
+constexpr int kSubsetPerBlock = kSubsetThreads * kSubsetPerThread;
+
+__global__ void __launch_bounds__(kSubsetThreads) k_msm_subsets(const Xyzz *run, const Xyzz *acc,
+                                                                size_t segments, int bits, int chunks,
+                                                                Xyzz *partial) {
+    __shared__ Xyzz sm[kSubsetThreads];
+    const int y = blockIdx.y, t = threadIdx.x;
+    const size_t count = y < bits ? segments / 2 : segments;
+    const size_t first = size_t(blockIdx.x) * kSubsetPerBlock;
+    Xyzz s = xyzz_inf();
+    for (int k = 0; k < kSubsetPerThread; k++) {
+        size_t e = first + size_t(k) * kSubsetThreads + t;
+        if (e >= count) break;
+        Xyzz v;
+        if (y < bits) {
+            size_t j = ((e >> y) << (y + 1)) | (size_t(1) << y) | (e & ((size_t(1) << y) - 1));
+            v = load_xyzz(&run[j]);
+        } else {
+            v = load_xyzz(&acc[e]);
+        }
+        s = xyzz_add(s, v);
+    }
+    sm[t] = s;
+    __syncthreads();
+    for (int half = kSubsetThreads / 2; half > 0; half >>= 1) {
+        if (t < half) sm[t] = xyzz_add(sm[t], sm[t + half]);
+        __syncthreads();
+    }
+    if (t == 0) store_xyzz(&partial[size_t(y) * chunks + blockIdx.x], sm[0]);
+}
+
+// Row sums of a [rows][cols] partial matrix (cols <= 64) into out[rows].
+__global__ void k_msm_rows(const Xyzz *partial, int cols, Xyzz *out) {
+    __shared__ Xyzz sm[64];
+    const int y = blockIdx.x, t = threadIdx.x;
+    sm[t] = t < cols ? load_xyzz(&partial[size_t(y) * cols + t]) : xyzz_inf();
+    __syncthreads();
+    for (int half = 32; half > 0; half >>= 1) {
+        if (t < half) sm[t] = xyzz_add(sm[t], sm[t + half]);
+        __syncthreads();
+    }
+    if (t == 0) store_xyzz(&out[y], sm[0]);
+}
+
+void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz *out_partials) {
+    const size_t n = layer.n;
+    const MsmShape sh = msm_shape(layer);
+    const size_t B = sh.buckets;
+    const size_t records = size_t(layer.windows) * n;
+    Scratch counts(ctx, (B + 1) * 4), offsets(ctx, (B + 1) * 4), cursor(ctx, B * 4);
+    Scratch recs(ctx, records * 4), buckets(ctx, B * sizeof(Xyzz));
+    check_cuda(cudaMemsetAsync(counts.ptr, 0, (B + 1) * 4, ctx->stream));
+    k_msm_histogram<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(scalars, n, layer.c, layer.windows,
+                                                                    counts.as<uint32_t>());
+    check_launch();
+    k_msm_scan<<<1, 1024, 0, ctx->stream>>>(counts.as<uint32_t>(), B, offsets.as<uint32_t>(),
+                                            cursor.as<uint32_t>());
+    check_launch();
+    k_msm_scatter<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(scalars, n, layer.c, layer.windows,
+                                                                  cursor.as<uint32_t>(), recs.as<uint32_t>());
+    check_launch();
+    k_msm_accumulate<<<grid_for(ctx, B, 128, 16), 128, 0, ctx->stream>>>(
+        layer.bases, offsets.as<uint32_t>(), recs.as<uint32_t>(), B, buckets.as<Xyzz>());
+    check_launch();
+    Scratch acc(ctx, sh.segments * sizeof(Xyzz)), run(ctx, sh.segments * sizeof(Xyzz));
+    k_msm_segments<<<grid_for(ctx, sh.segments, 128, 16), 128, 0, ctx->stream>>>(
+        buckets.as<Xyzz>(), sh.segments, sh.seg, acc.as<Xyzz>(), run.as<Xyzz>());
+    check_launch();
+    const int chunks = int((sh.segments + kSubsetPerBlock - 1) / kSubsetPerBlock);
+    if (chunks == 1) {
+        k_msm_subsets<<<dim3(1, sh.partials), kSubsetThreads, 0, ctx->stream>>>(
+            run.as<Xyzz>(), acc.as<Xyzz>(), sh.segments, sh.seg_bits, 1, out_partials);
+        check_launch();
+    } else {
+        Scratch partial(ctx, size_t(chunks) * sh.partials * sizeof(Xyzz));
+        k_msm_subsets<<<dim3(chunks, sh.partials), kSubsetThreads, 0, ctx->stream>>>(
+            run.as<Xyzz>(), acc.as<Xyzz>(), sh.segments, sh.seg_bits, chunks, partial.as<Xyzz>());
+        check_launch();
+        if (chunks > 64) fail(HP_CUDA_STATUS_NOT_IMPLEMENTED);
+        k_msm_rows<<<sh.partials, 64, 0, ctx->stream>>>(partial.as<Xyzz>(), chunks, out_partials);
+        check_launch();
+    }
+}
+
+void msm_finalize_host(const MsmShape &shape, const host::Xyzz64 *partials, uint8_t *out97) {
+    // result = A + seg * sum_k 2^k T_k, A = partials[bits], T_k = partials[k]
+    host::Xyzz64 h = host::xyzz_inf();
+    for (int k = shape.seg_bits - 1; k >= 0; k--) {
+        h = host::xyzz_double(h);
+        h = host::xyzz_add(h, partials[k]);
+    }
+    for (size_t s = shape.seg; s > 1; s >>= 1) h = host::xyzz_double(h);
+    host::Xyzz64 r = host::xyzz_add(partials[shape.seg_bits], h);
+    host::xyzz_to_packet(r, out97);
+}
+
+}  // namespace hp

@@ -1,0 +1,53 @@
+// msm.cuh -- Pippenger MSM over prepared (precomputed-window) SRS layers.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include "g1.cuh"
+#include "host_ec.h"
+
+struct HpCudaContext;
+
+namespace hp {
+
+// One prepared SRS layer: window w of point i is 2^(c*w) * P_i in affine
+// Montgomery form at bases[w * n + i], so every window of a scalar's
+// signed-digit expansion indexes the same 2^(c-1) buckets and no per-window
+// combination is needed.  Built once by msm_prepare_layer().
+struct MsmLayer {
+    size_t n = 0;
+    int c = 0;        // window bits
+    int windows = 0;  // ceil(256 / c)
+    Affine *bases = nullptr;  // windows * n points (device, context scratch)
+};
+
+// Window width minimising ceil(256/c) * 10 n + 28 * 2^(c-1) for c in [4, 20]
+// (mixed additions into buckets + two XYZZ additions per bucket to reduce).
+int msm_window_bits(size_t n);
+inline int msm_windows(int c) { return (256 + c - 1) / c; }
+
+// Bucket reduction geometry: buckets are split into segments of `seg` and
+// the segment sums combined by bit subsets (see msm.cu).
+struct MsmShape {
+    size_t buckets;  // 2^(c-1)
+    size_t seg;      // buckets per segment
+    size_t segments; // buckets / seg
+    int seg_bits;    // log2(segments)
+    int partials;    // seg_bits + 1 XYZZ outputs per MSM
+};
+MsmShape msm_shape(const MsmLayer &layer);
+
+// Upload n 97-byte packets as window 0 and derive the other windows.
+// Returns false if a packet is malformed (bad tag / non-canonical coordinate).
+bool msm_prepare_layer(HpCudaContext *ctx, MsmLayer &layer, const uint8_t *packets, size_t n);
+void msm_release_layer(HpCudaContext *ctx, MsmLayer &layer);
+
+// Enqueue one MSM of the layer's n bases with n Montgomery scalars; writes
+// msm_shape(layer).partials XYZZ values to out_partials (device).  All work
+// is on the context stream; no synchronisation.
+void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz *out_partials);
+
+// Host: combine the partials of one MSM into a 97-byte G1 packet.
+void msm_finalize_host(const MsmShape &shape, const host::Xyzz64 *partials, uint8_t *out97);
+
+}  // namespace hp

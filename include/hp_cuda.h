@@ -176,6 +176,14 @@ HpCudaStatus hp_cuda_v1_mle_download(HpCudaContext *ctx, HpCudaDeviceAddress pol
                                      size_t num_vars, uint8_t *out_evaluations,
                                      size_t evaluation_count);
 
+/* One variable-base MSM sum_i scalars[i] * bases[i] over G1 from host
+ * buffers: `count` 97-byte base packets and `count` canonical Fr, any count
+ * (0 gives the point at infinity).  Counterpart of the reference's internal
+ * run_msm (backend/src/ascend910b3/native/msm.h:13-16), which its bridge does
+ * not export; commit/open use the prepared-layer path instead. */
+HpCudaStatus hp_cuda_v1_msm(HpCudaContext *ctx, const uint8_t *bases, const uint8_t *scalars,
+                            size_t count, uint8_t *out_point);
+
 /* The context's CUDA stream (a cudaStream_t), so a caller can order its own
  * work or timing events with the backend's. */
 HpCudaStatus hp_cuda_v1_context_stream(HpCudaContext *ctx, void **out_stream);

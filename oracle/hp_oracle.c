@@ -242,6 +242,7 @@ static void parallel_for(size_t n, range_fn fn, void *ctx) {
     }
     pthread_t th[256];
     range_job jobs[256];
+    memset(jobs, 0, sizeof jobs);
     if (t > 256) t = 256;
     size_t chunk = (n + t - 1) / t;
     int launched = 0;

@@ -1,0 +1,150 @@
+"""GPU parity of the MLE ABI entries against the oracle, byte for byte.
+
+Mirrors backend/src/ascend910b3/integration_tests.rs (device vs CpuBackend on
+the same inputs) with sizes chosen around the kernels' tile edges."""
+import random
+
+import pytest
+
+from hyperplonk_gb300.errors import InvalidParameters
+
+pytestmark = pytest.mark.gpu
+
+R = 0x73EDA753299D7D483339D80809A1D80553BDA402FFFE5BFEFFFFFFFF00000001
+
+
+def table(oracle, nv, seed, edges=True):
+    b = bytearray(oracle.random_fr(seed, 1 << nv))
+    if edges and nv >= 2:
+        b[0:32] = (0).to_bytes(32, "little")
+        b[-32:] = (R - 1).to_bytes(32, "little")
+    return bytes(b)
+
+
+def pair(gpu, cpu, oracle, nv, seed):
+    t = table(oracle, nv, seed)
+    return gpu.mle_from_evaluations(nv, t), cpu.mle_from_evaluations(nv, t)
+
+
+@pytest.mark.parametrize("nv", [0, 1, 2, 5, 10, 13])
+def test_upload_download_roundtrip(gpu, oracle, nv):
+    t = table(oracle, nv, 100 + nv)
+    m = gpu.mle_from_evaluations(nv, t)
+    assert gpu.download(m) == t
+
+
+def test_upload_rejects_noncanonical_and_bad_shape(gpu, oracle):
+    t = bytearray(table(oracle, 3, 1))
+    t[32 * 5:32 * 6] = R.to_bytes(32, "little")
+    with pytest.raises(InvalidParameters):
+        gpu.mle_from_evaluations(3, bytes(t))
+    with pytest.raises(InvalidParameters):
+        gpu.mle_from_evaluations(3, bytes(32 * 7))
+
+
+@pytest.mark.parametrize("nv,count", [(0, 2), (1, 1), (4, 3), (11, 5), (9, 40)])
+def test_linear_combination(gpu, cpu, oracle, nv, count):
+    rng = random.Random(nv * 100 + count)
+    gs, cs = [], []
+    for j in range(count):
+        g, c = pair(gpu, cpu, oracle, nv, 200 + j)
+        gs.append(g)
+        cs.append(c)
+    coefs = [rng.randrange(R) for _ in range(count)]
+    if count > 2:
+        coefs[1] = 0
+    got = gpu.download(gpu.linear_combination(gs, coefs))
+    assert got == cpu.linear_combination(cs, coefs).evaluations
+    zero = gpu.linear_combination(gs[:1], [0])
+    assert gpu.download(zero) == bytes(32 << nv)
+    assert zero.num_vars == nv
+
+
+@pytest.mark.parametrize("nv", [0, 1, 5, 10, 11, 12, 16])
+def test_evaluate(gpu, cpu, oracle, nv):
+    g, c = pair(gpu, cpu, oracle, nv, 300 + nv)
+    rng = random.Random(nv)
+    pt = [rng.randrange(R) for _ in range(nv)]
+    assert gpu.evaluate_mle(g, pt) == cpu.evaluate_mle(c, pt)
+    with pytest.raises(InvalidParameters):
+        gpu.evaluate_mle(g, pt + [1])
+
+
+@pytest.mark.parametrize("nv", [1, 2, 5, 12, 13, 17])
+def test_build_eq_x_r(gpu, cpu, nv):
+    rng = random.Random(40 + nv)
+    r = [rng.randrange(R) for _ in range(nv)]
+    r[0] = 0
+    assert gpu.download(gpu.build_eq_x_r(r)) == cpu.build_eq_x_r(r).evaluations
+    with pytest.raises(InvalidParameters):
+        gpu.build_eq_x_r([])
+
+
+@pytest.mark.parametrize("nv,count", [(0, 1), (1, 1), (3, 3), (11, 1), (12, 3), (16, 2)])
+def test_frac(gpu, cpu, oracle, nv, count):
+    fs = [pair(gpu, cpu, oracle, nv, 500 + j) for j in range(count)]
+    gs = []
+    for j in range(count):
+        t = bytearray(oracle.random_fr(600 + j, 1 << nv))
+        gs.append((gpu.mle_from_evaluations(nv, bytes(t)), cpu.mle_from_evaluations(nv, bytes(t))))
+    got = gpu.download(gpu.compute_frac_poly([f[0] for f in fs], [g[0] for g in gs]))
+    assert got == cpu.compute_frac_poly([f[1] for f in fs], [g[1] for g in gs]).evaluations
+
+
+def test_frac_zero_denominator_is_invalid_parameters(gpu, oracle):
+    nv = 10
+    f = gpu.mle_from_evaluations(nv, oracle.random_fr(1, 1 << nv))
+    t = bytearray(oracle.random_fr(2, 1 << nv))
+    t[32 * 777:32 * 778] = bytes(32)
+    g = gpu.mle_from_evaluations(nv, bytes(t))
+    with pytest.raises(InvalidParameters):
+        gpu.compute_frac_poly([f], [g])
+    # 0/0 too
+    z = gpu.mle_from_evaluations(1, bytes(64))
+    with pytest.raises(InvalidParameters):
+        gpu.compute_frac_poly([z], [z])
+
+
+@pytest.mark.parametrize("nv", [1, 2, 3, 9, 10, 11, 16])
+def test_product_poly_and_factors(gpu, cpu, oracle, nv):
+    f, c = pair(gpu, cpu, oracle, nv, 700 + nv)
+    pg, pc = gpu.compute_product_poly(f), cpu.compute_product_poly(c)
+    assert gpu.download(pg) == pc.evaluations
+    a, b = gpu.compute_product_factors(f, pg)
+    ea, eb = cpu.compute_product_factors(c, pc)
+    assert gpu.download(a) == ea.evaluations
+    assert gpu.download(b) == eb.evaluations
+
+
+def test_product_poly_kat(gpu):
+    from oracle import frs_ints
+    frac = gpu.mle_from_evaluations(3, [2, 3, 5, 7, 11, 13, 17, 19])
+    assert frs_ints(gpu.download(gpu.compute_product_poly(frac))) == [6, 35, 143, 323, 210, 46189, 9699690, 0]
+    with pytest.raises(InvalidParameters):
+        gpu.compute_product_poly(gpu.mle_from_evaluations(0, [2]))
+
+
+@pytest.mark.parametrize("nv", [0, 2, 10, 15])
+def test_nums_and_denoms(gpu, cpu, oracle, nv):
+    cols = 3
+    fx = [pair(gpu, cpu, oracle, nv, 800 + j) for j in range(cols)]
+    gx = [pair(gpu, cpu, oracle, nv, 810 + j) for j in range(cols)]
+    pm = [pair(gpu, cpu, oracle, nv, 820 + j) for j in range(cols)]
+    rng = random.Random(nv)
+    for beta, gamma in [(rng.randrange(R), rng.randrange(R)), (0, 5), (R - 2, 0)]:
+        ng, dg = gpu.compute_nums_and_denoms(beta, gamma, [x[0] for x in fx], [x[0] for x in gx], [x[0] for x in pm])
+        nc, dc = cpu.compute_nums_and_denoms(beta, gamma, [x[1] for x in fx], [x[1] for x in gx], [x[1] for x in pm])
+        for j in range(cols):
+            assert gpu.download(ng[j]) == nc[j].evaluations
+            assert gpu.download(dg[j]) == dc[j].evaluations
+
+
+def test_inputs_stay_immutable(gpu, oracle):
+    nv = 8
+    t = table(oracle, nv, 900)
+    m = gpu.mle_from_evaluations(nv, t)
+    gpu.linear_combination([m, m], [3, 4])
+    gpu.compute_product_poly(m)
+    gpu.compute_frac_poly([m], [gpu.mle_from_evaluations(nv, oracle.random_fr(901, 1 << nv))])
+    gpu.evaluate_mle(m, list(range(nv)))
+    assert gpu.download(m) == t

@@ -1,0 +1,133 @@
+"""GPU parity of the sumcheck prover state against the oracle, every round.
+
+Mirrors backend/src/ascend910b3/integration_tests.rs
+(sumcheck_round_messages_match_cpu_for_mixed_products,
+sumcheck_repeated_factors_mixed_arity_max_degree_34_are_independent) and the
+CPU KAT of backend/src/cpu/sum_check.rs:224-253."""
+import random
+
+import pytest
+
+from hyperplonk_gb300.errors import InvalidParameters, InvalidState
+from hyperplonk_gb300.virtual_polynomial import VirtualPolynomial
+
+pytestmark = pytest.mark.gpu
+
+R = 0x73EDA753299D7D483339D80809A1D80553BDA402FFFE5BFEFFFFFFFF00000001
+
+
+def build_pair(gpu, cpu, oracle, nv, n_mles, products, seed):
+    """products: list of (coef, [mle indices]) -> (gpu VP, cpu VP)."""
+    tables = [oracle.random_fr(seed, 1 << nv, first=j << nv) for j in range(n_mles)]
+    gm = [gpu.mle_from_evaluations(nv, t) for t in tables]
+    cm = [cpu.mle_from_evaluations(nv, t) for t in tables]
+    vg, vc = VirtualPolynomial(nv), VirtualPolynomial(nv)
+    for coef, ix in products:
+        vg.add_mle_list([gm[i] for i in ix], coef)
+        vc.add_mle_list([cm[i] for i in ix], coef)
+    return vg, vc, gm, cm
+
+
+def run_both(gpu, cpu, vg, vc, seed):
+    rng = random.Random(seed)
+    sg, sc = gpu.prover_init(vg), cpu.prover_init(vc)
+    ch = None
+    for _ in range(vg.aux_info.num_variables):
+        a = gpu.prove_round_and_update_state(sg, ch)
+        b = cpu.prove_round_and_update_state(sc, ch)
+        assert a == b
+        ch = rng.randrange(R)
+    assert gpu.final_evaluations(sg, ch) == cpu.final_evaluations(sc, ch)
+    return sg, ch
+
+
+def test_round_kat_and_ordering(gpu):
+    mle = gpu.mle_from_evaluations(2, [2, 3, 5, 7])
+    poly = VirtualPolynomial.new_from_mle(mle, 2)
+    poly.add_mle_list([mle, mle], 3)
+    st = gpu.prover_init(poly)
+    with pytest.raises(InvalidState):
+        gpu.prove_round_and_update_state(st, 2)
+    assert gpu.prove_round_and_update_state(st, None) == [101, 194, 317]
+    with pytest.raises(InvalidState):
+        gpu.prove_round_and_update_state(st, None)
+    assert gpu.prove_round_and_update_state(st, 2) == [56, 261, 616]
+    with pytest.raises(InvalidState):
+        gpu.prove_round_and_update_state(st, 2)
+    assert gpu.download(mle) == b"".join(v.to_bytes(32, "little") for v in (2, 3, 5, 7))
+
+
+@pytest.mark.parametrize("nv", [1, 2, 3, 10, 14])
+def test_degree2_four_products_over_six_mles(gpu, cpu, oracle, nv):
+    rng = random.Random(nv)
+    prods = [(rng.randrange(R), [0, 1]), (rng.randrange(R), [2, 3]), (rng.randrange(R), [4, 5]),
+             (rng.randrange(R), [0, 3])]
+    vg, vc, _, _ = build_pair(gpu, cpu, oracle, nv, 6, prods, 1)
+    run_both(gpu, cpu, vg, vc, nv)
+
+
+def test_mixed_products(gpu, cpu, oracle):
+    nv = 9
+    prods = [(5, [0, 1, 2]), (7, [3]), (R - 1, [1, 1]), (11, [4, 0, 2, 3]), (0, [2, 4])]
+    vg, vc, _, _ = build_pair(gpu, cpu, oracle, nv, 5, prods, 2)
+    run_both(gpu, cpu, vg, vc, 9)
+
+
+def test_repeated_factors_max_degree_34(gpu, cpu, oracle):
+    nv = 6
+    prods = [(3, [0] * 34), (5, [1, 0, 1]), (R - 7, [2] * 17 + [1] * 10), (9, [2])]
+    vg, vc, _, _ = build_pair(gpu, cpu, oracle, nv, 3, prods, 3)
+    assert vg.aux_info.max_degree == 34
+    run_both(gpu, cpu, vg, vc, 34)
+
+
+def test_zerocheck_shape_degree4(gpu, cpu, oracle):
+    """Gate polynomial times eq: q_L w1 + q_R w2 + q_O w3 + q_M w1 w2 + q_C, x eq."""
+    nv = 11
+    # 0..4 selectors, 5..7 witnesses, 8 eq
+    prods = [(1, [0, 5, 8]), (1, [1, 6, 8]), (1, [2, 7, 8]), (1, [3, 5, 6, 8]), (1, [4, 8])]
+    vg, vc, _, _ = build_pair(gpu, cpu, oracle, nv, 9, prods, 4)
+    run_both(gpu, cpu, vg, vc, 4)
+
+
+def test_empty_sum_and_state_independence(gpu, cpu, oracle):
+    nv = 4
+    vg = VirtualPolynomial(nv)
+    vg.aux_info.max_degree = 2
+    st = gpu.prover_init(vg)
+    assert gpu.prove_round_and_update_state(st, None) == [0, 0, 0]
+    # two states over the same factors advance independently
+    prods = [(1, [0, 1])]
+    vg, vc, gm, _ = build_pair(gpu, cpu, oracle, 6, 2, prods, 5)
+    s1, s2 = gpu.prover_init(vg), gpu.prover_init(vg)
+    a = gpu.prove_round_and_update_state(s1, None)
+    gpu.prove_round_and_update_state(s1, 3)
+    b = gpu.prove_round_and_update_state(s2, None)
+    assert a == b
+
+
+def test_state_outlives_retired_inputs(gpu, cpu, oracle):
+    nv = 8
+    prods = [(2, [0, 1]), (3, [1])]
+    vg, vc, gm, cm = build_pair(gpu, cpu, oracle, nv, 2, prods, 6)
+    sg, sc = gpu.prover_init(vg), cpu.prover_init(vc)
+    del vg, gm  # drop every Python handle: the buffers are retired
+    import gc
+    gc.collect()
+    ch = None
+    rng = random.Random(1)
+    for _ in range(nv):
+        assert gpu.prove_round_and_update_state(sg, ch) == cpu.prove_round_and_update_state(sc, ch)
+        ch = rng.randrange(R)
+
+
+def test_invalid_descriptions(gpu, oracle):
+    vg = VirtualPolynomial(0)
+    vg.aux_info.max_degree = 1
+    with pytest.raises(InvalidParameters):
+        gpu.prover_init(vg)
+    m = gpu.mle_from_evaluations(2, oracle.random_fr(1, 4))
+    vg = VirtualPolynomial.new_from_mle(m, 1)
+    vg.aux_info.max_degree = 0
+    with pytest.raises(InvalidParameters):
+        gpu.prover_init(vg)
