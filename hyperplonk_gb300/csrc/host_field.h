@@ -23,6 +23,8 @@ static const uint64_t kFrR2[4] = {0xc999e990f3f29c6dULL, 0x2b6cedcb87925c23ULL,
                                   0x05d314967254398fULL, 0x0748d9d99f59ff11ULL};
 static const uint64_t kFrOne[4] = {0x1fffffffeULL, 0x5884b7fa00034802ULL,
                                    0x998c4fefecbc4ff5ULL, 0x1824b159acc5056fULL};
+static const uint64_t kFrR3[4] = {0xc62c1807439b73afULL, 0x1b3e0d188cf06990ULL,
+                                  0x73d13c71c7b5f418ULL, 0x6e2a5bb9c8db33e9ULL};
 static const uint64_t kFrInv = 0xfffffffeffffffffULL;
 
 inline bool geq_p(const uint64_t *a) {
@@ -89,6 +91,29 @@ inline void to_canonical(const Fr64 &mont, uint8_t *bytes) {
 }
 
 inline bool is_zero(const Fr64 &a) { return (a.v[0] | a.v[1] | a.v[2] | a.v[3]) == 0; }
+
+inline Fr64 add(const Fr64 &a, const Fr64 &b) {
+    Fr64 r;
+    unsigned __int128 c = 0;
+    for (int i = 0; i < 4; i++) {
+        c += (unsigned __int128)a.v[i] + b.v[i];
+        r.v[i] = (uint64_t)c;
+        c >>= 64;
+    }
+    if (c || geq_p(r.v)) sub_p(r.v);
+    return r;
+}
+
+// Fr::from_le_bytes_mod_order of 64 bytes (ark-ff): (lo + hi * 2^256) mod r,
+// returned in Montgomery form: mont(lo * R2) + mont(hi * R3).
+inline Fr64 from_wide64(const uint8_t *bytes) {
+    Fr64 lo, hi, r2, r3;
+    std::memcpy(lo.v, bytes, 32);
+    std::memcpy(hi.v, bytes + 32, 32);
+    std::memcpy(r2.v, kFrR2, 32);
+    std::memcpy(r3.v, kFrR3, 32);
+    return add(mont_mul(lo, r2), mont_mul(hi, r3));
+}
 
 inline Fr64 one() {
     Fr64 r;

@@ -169,6 +169,12 @@ __global__ void __launch_bounds__(kNormBlock) k_normalize(const Xyzz *in, Affine
     }
 }
 
+void xyzz_to_affine(HpCudaContext *ctx, const Xyzz *in, Affine *out, Fq *pre, size_t n) {
+    size_t per_block = size_t(kNormBlock) * kNormChunk;
+    k_normalize<<<unsigned((n + per_block - 1) / per_block), kNormBlock, 0, ctx->stream>>>(in, out, pre, n);
+    check_launch();
+}
+
 bool msm_prepare_layer(HpCudaContext *ctx, MsmLayer &layer, const uint8_t *packets, size_t n) {
     layer.n = n;
     layer.c = msm_window_bits(n);

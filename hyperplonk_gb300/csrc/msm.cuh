@@ -47,6 +47,9 @@ void msm_release_layer(HpCudaContext *ctx, MsmLayer &layer);
 // is on the context stream; no synchronisation.
 void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz *out_partials);
 
+// Batch XYZZ -> affine (one field inversion per 512 points); pre: n Fq scratch.
+void xyzz_to_affine(HpCudaContext *ctx, const Xyzz *in, Affine *out, Fq *pre, size_t n);
+
 // Host: combine the partials of one MSM into a 97-byte G1 packet.
 void msm_finalize_host(const MsmShape &shape, const host::Xyzz64 *partials, uint8_t *out97);
 

@@ -184,6 +184,25 @@ HpCudaStatus hp_cuda_v1_mle_download(HpCudaContext *ctx, HpCudaDeviceAddress pol
 HpCudaStatus hp_cuda_v1_msm(HpCudaContext *ctx, const uint8_t *bases, const uint8_t *scalars,
                             size_t count, uint8_t *out_point);
 
+/* Synthetic workloads (no counterpart in the reference's bridge; the
+ * reference builds its fixtures with arkworks' StdRng in Rust:
+ * hyperplonk/examples/full_prove_bench.rs, subroutines/examples/sumcheck_bench.rs).
+ *
+ * fixture_random_fr: `count` canonical Fr of stream `seed`, elements
+ * [first, first + count); element i = Fr::from_le_bytes_mod_order of ChaCha20
+ * (RFC 8439) keystream block i, key words 0-1 = seed, counter = low 32 bits
+ * of i, first nonce word = high 32 bits.  Host-only: needs no context.
+ *
+ * srs_generate: the testing SRS of subroutines/src/pcs/multilinear_kzg/
+ * srs.rs:158-235 with this stream in place of StdRng: t_i = element i
+ * (i < num_vars), s = element num_vars, g = s * G1; layer i < num_vars is
+ * g * eq(t[i..], x) (t_i <-> bit 0), layer num_vars is [g].  Writes all
+ * layers back to back as 97-byte packets, point_count = 2^(num_vars+1) - 1.
+ * Computed on the device (fixed-base comb). */
+HpCudaStatus hp_cuda_v1_fixture_random_fr(uint64_t seed, uint64_t first, size_t count, uint8_t *out);
+HpCudaStatus hp_cuda_v1_srs_generate(HpCudaContext *ctx, size_t num_vars, uint64_t seed,
+                                     uint8_t *out_packets, size_t point_count);
+
 /* The context's CUDA stream (a cudaStream_t), so a caller can order its own
  * work or timing events with the backend's. */
 HpCudaStatus hp_cuda_v1_context_stream(HpCudaContext *ctx, void **out_stream);
