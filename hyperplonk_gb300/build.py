@@ -18,6 +18,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libhp_cuda.so"
+PROBE_LIB = BUILD / "libhp_probe.so"  # integer-pipe ceilings, read by bench.py
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", f"-I{ROOT / 'include'}"]
@@ -72,6 +73,11 @@ def build(verbose: bool = False, extra_flags: list[str] | None = None) -> pathli
         tmp = BUILD / "libhp_cuda.so.tmp"
         run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *objs])
         os.replace(tmp, LIB)
+    probe_src = CSRC / "probe" / "int_probe.cu"
+    if not PROBE_LIB.exists() or _stale(PROBE_LIB, probe_src, headers):
+        tmp = BUILD / "libhp_probe.so.tmp"
+        run([nvcc, *ARCH, *flags, "-shared", "-cudart", "static", str(probe_src), "-o", str(tmp)])
+        os.replace(tmp, PROBE_LIB)
     return LIB
 
 

@@ -381,6 +381,7 @@ void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz 
     const size_t records = size_t(layer.windows) * n;
     Scratch counts(ctx, (B + 1) * 4), offsets(ctx, (B + 1) * 4), cursor(ctx, B * 4);
     Scratch recs(ctx, records * 4), buckets(ctx, B * sizeof(Xyzz));
+    int whole = ctx->prof_begin("msm");
     check_cuda(cudaMemsetAsync(counts.ptr, 0, (B + 1) * 4, ctx->stream));
     k_msm_histogram<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(scalars, n, layer.c, layer.windows,
                                                                     counts.as<uint32_t>());
@@ -391,9 +392,11 @@ void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz 
     k_msm_scatter<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(scalars, n, layer.c, layer.windows,
                                                                   cursor.as<uint32_t>(), recs.as<uint32_t>());
     check_launch();
+    int tok = ctx->prof_begin("msm_accumulate");
     k_msm_accumulate<<<grid_for(ctx, B, 128, 16), 128, 0, ctx->stream>>>(
         layer.bases, offsets.as<uint32_t>(), recs.as<uint32_t>(), B, buckets.as<Xyzz>());
     check_launch();
+    ctx->prof_end(tok);
     Scratch acc(ctx, sh.segments * sizeof(Xyzz)), run(ctx, sh.segments * sizeof(Xyzz));
     k_msm_segments<<<grid_for(ctx, sh.segments, 128, 16), 128, 0, ctx->stream>>>(
         buckets.as<Xyzz>(), sh.segments, sh.seg, acc.as<Xyzz>(), run.as<Xyzz>());
@@ -412,6 +415,7 @@ void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz 
         k_msm_rows<<<sh.partials, 64, 0, ctx->stream>>>(partial.as<Xyzz>(), chunks, out_partials);
         check_launch();
     }
+    ctx->prof_end(whole);
 }
 
 void msm_finalize_host(const MsmShape &shape, const host::Xyzz64 *partials, uint8_t *out97) {

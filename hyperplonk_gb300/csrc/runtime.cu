@@ -1,6 +1,7 @@
 // runtime.cu -- context lifetime, buffer registry, retirement.
 // ABI: hp_cuda_v1_context_create / _destroy / _buffer_retire / _context_stream
 // (reference bridge.h:43-45, bridge_runtime.cpp).
+#include <atomic>
 #include <cstring>
 
 #include "runtime.cuh"
@@ -57,6 +58,45 @@ void HpCudaContext::retire(void *p) {
 size_t HpCudaContext::bytes_of(void *p) const {
     auto it = buffers.find(p);
     return it == buffers.end() ? 0 : it->second.bytes;
+}
+
+cudaEvent_t HpCudaContext::take_event() {
+    if (!event_pool.empty()) {
+        cudaEvent_t e = event_pool.back();
+        event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    check_cuda(cudaEventCreate(&e));
+    return e;
+}
+
+int HpCudaContext::prof_begin(const char *name) {
+    if (!profiling) return -1;
+    Pending p{name, take_event(), take_event()};
+    check_cuda(cudaEventRecord(p.start, stream));
+    pending.push_back(p);
+    return int(pending.size()) - 1;
+}
+
+void HpCudaContext::prof_end(int token) {
+    if (token < 0) return;
+    check_cuda(cudaEventRecord(pending[size_t(token)].stop, stream));
+}
+
+void HpCudaContext::prof_resolve() {
+    if (pending.empty()) return;
+    check_cuda(cudaStreamSynchronize(stream));
+    for (auto &p : pending) {
+        float ms = 0.f;
+        check_cuda(cudaEventElapsedTime(&ms, p.start, p.stop));
+        auto &t = totals[p.name];
+        t.first += double(ms);
+        t.second += 1;
+        event_pool.push_back(p.start);
+        event_pool.push_back(p.stop);
+    }
+    pending.clear();
 }
 
 void HpCudaContext::clear_flags() { check_cuda(cudaMemsetAsync(d_flags, 0, sizeof(uint32_t), stream)); }
@@ -125,6 +165,11 @@ extern "C" HpCudaStatus hp_cuda_v1_context_destroy(HpCudaContext *ctx) {
         ctx->buffers.clear();
         cudaError_t e = cudaStreamSynchronize(ctx->stream);
         if (first == cudaSuccess) first = e;
+        for (auto &p : ctx->pending) {
+            cudaEventDestroy(p.start);
+            cudaEventDestroy(p.stop);
+        }
+        for (auto e : ctx->event_pool) cudaEventDestroy(e);
         cudaFree(ctx->d_flags);
         cudaFreeHost(ctx->h_flags);
         cudaStreamDestroy(ctx->stream);
@@ -147,5 +192,37 @@ extern "C" HpCudaStatus hp_cuda_v1_context_stream(HpCudaContext *ctx, void **out
     return guard([&] {
         require(ctx != nullptr && out_stream != nullptr);
         *out_stream = static_cast<void *>(ctx->stream);
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_context_profile(HpCudaContext *ctx, int32_t enable) {
+    return guard([&] {
+        hp::require_ctx(ctx);
+        ctx->prof_resolve();
+        ctx->profiling = enable != 0;
+        ctx->totals.clear();
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_context_profile_read(HpCudaContext *ctx, const char *kernel, double *total_ms,
+                                                         uint64_t *launches) {
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(kernel != nullptr && total_ms != nullptr && launches != nullptr);
+        ctx->prof_resolve();
+        auto it = ctx->totals.find(kernel);
+        *total_ms = it == ctx->totals.end() ? 0.0 : it->second.first;
+        *launches = it == ctx->totals.end() ? 0 : it->second.second;
+    });
+}
+
+static std::atomic<uint64_t> g_kernel_launches{0};
+
+void hp::count_launch() { g_kernel_launches.fetch_add(1, std::memory_order_relaxed); }
+
+extern "C" HpCudaStatus hp_cuda_v1_kernel_launch_count(uint64_t *out) {
+    return guard([&] {
+        require(out != nullptr);
+        *out = g_kernel_launches.load(std::memory_order_relaxed);
     });
 }

@@ -16,7 +16,9 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <map>
 #include <new>
+#include <string>
 #include <unordered_map>
 #include <vector>
 
@@ -98,6 +100,21 @@ struct HpCudaContext {
     // Caller gives up its handle; storage lives while internal refs remain.
     void retire(void *p);
     size_t bytes_of(void *p) const;
+    // Kernel timing (off by default): CUDA events around named launches on
+    // the context stream, resolved into per-name totals on read.
+    bool profiling = false;
+    struct Pending {
+        const char *name;
+        cudaEvent_t start, stop;
+    };
+    std::vector<Pending> pending;
+    std::vector<cudaEvent_t> event_pool;
+    std::map<std::string, std::pair<double, uint64_t>> totals;  // ms, launches
+    cudaEvent_t take_event();
+    // Returns an index to pass to prof_end, or -1 when profiling is off.
+    int prof_begin(const char *name);
+    void prof_end(int token);
+    void prof_resolve();
     // Clear the device status word (stream ordered).
     void clear_flags();
     // Synchronize and return the status word.
@@ -178,8 +195,15 @@ inline unsigned grid_for(const HpCudaContext *ctx, size_t work_items, unsigned b
     return static_cast<unsigned>(need);
 }
 
-// Launch-error check after a kernel launch.
-inline void check_launch() { check_cuda(cudaGetLastError()); }
+// Kernels launched by this library since load (every launch site calls
+// check_launch right after the launch).
+void count_launch();
+
+// Launch-error check after a kernel launch; also counts the launch.
+inline void check_launch() {
+    count_launch();
+    check_cuda(cudaGetLastError());
+}
 
 // Canonical host Fr bytes -> device Montgomery values, in a small scratch.
 // Host side only validates canonical range; conversion happens on device.

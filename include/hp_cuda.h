@@ -203,6 +203,18 @@ HpCudaStatus hp_cuda_v1_fixture_random_fr(uint64_t seed, uint64_t first, size_t 
 HpCudaStatus hp_cuda_v1_srs_generate(HpCudaContext *ctx, size_t num_vars, uint64_t seed,
                                      uint8_t *out_packets, size_t point_count);
 
+/* Kernel timing (off by default; no counterpart in the reference, which
+ * profiles offline with msprof).  While enabled, named device phases are
+ * bracketed by CUDA events on the context stream; profile_read returns the
+ * accumulated milliseconds and launch count of one name ("msm",
+ * "msm_accumulate", "sumcheck_round", ...).  Enabling or disabling resets the
+ * totals. */
+HpCudaStatus hp_cuda_v1_context_profile(HpCudaContext *ctx, int32_t enable);
+HpCudaStatus hp_cuda_v1_context_profile_read(HpCudaContext *ctx, const char *kernel, double *total_ms,
+                                             uint64_t *launches);
+/* Number of kernels this library has launched in the process so far. */
+HpCudaStatus hp_cuda_v1_kernel_launch_count(uint64_t *out);
+
 /* The context's CUDA stream (a cudaStream_t), so a caller can order its own
  * work or timing events with the backend's. */
 HpCudaStatus hp_cuda_v1_context_stream(HpCudaContext *ctx, void **out_stream);

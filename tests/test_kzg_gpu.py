@@ -130,3 +130,18 @@ def test_kzg_errors(gpu, oracle, params):
     bad[0] = 7
     with pytest.raises(InvalidParameters):
         gpu.prepare_prover_param(1, [bytes(bad), oracle.affine_to_packets(oracle.g1_generator())])
+
+
+@pytest.mark.parametrize("nv", [1, 3, 8])
+def test_srs_generate_matches_oracle(gpu, oracle, nv):
+    total = (1 << (nv + 1)) - 1
+    out = (ctypes.c_uint8 * (97 * total))()
+    check_status(gpu.lib.hp_cuda_v1_srs_generate(gpu.ctx.raw, nv, 21, out, total), "srs_generate")
+    expect = b"".join(oracle.affine_to_packets(l) for l in oracle.srs_layers(nv, 21))
+    assert bytes(out) == expect
+
+
+def test_fixture_rng_matches_oracle(native_lib, oracle):
+    out = (ctypes.c_uint8 * (32 * 5000))()
+    check_status(native_lib.hp_cuda_v1_fixture_random_fr(3, 7, 5000, out), "fixture_random_fr")
+    assert bytes(out) == oracle.random_fr(3, 5000, first=7)
