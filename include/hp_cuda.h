@@ -184,6 +184,23 @@ HpCudaStatus hp_cuda_v1_mle_download(HpCudaContext *ctx, HpCudaDeviceAddress pol
 HpCudaStatus hp_cuda_v1_msm(HpCudaContext *ctx, const uint8_t *bases, const uint8_t *scalars,
                             size_t count, uint8_t *out_point);
 
+/* Evaluation of a resident MLE that allocates no device memory.  No
+ * counterpart in the reference.  For callers that cannot call cudaMalloc:
+ * hosts that own all device memory through their own pre-reserved arena, or
+ * code running inside a CUDA stream capture, where allocation is not allowed.
+ * `table` is a device pointer to 2^num_vars Fr in this library's layout (for
+ * example an address returned by hp_cuda_v1_mle_upload); `point` holds
+ * num_vars canonical Fr; the canonical result goes to out_evaluation (32
+ * bytes, host).  Work runs on `stream` (a cudaStream_t; null = the legacy
+ * default stream) of the current device, which the call synchronises.
+ * Intermediate values live in one fixed device array of ~513 KiB that every
+ * GPU loading this library holds until exit; num_vars above 24 returns
+ * InvalidParameters.  All calls on a device share that array: calls that
+ * overlap on the GPU race, so order them (one stream).  The first call on a
+ * device looks up the array's address; make it before any stream capture. */
+HpCudaStatus hp_cuda_v1_mle_evaluate_noalloc(const void *table, size_t num_vars, const uint8_t *point,
+                                             uint8_t *out_evaluation, void *stream);
+
 /* Synthetic workloads (no counterpart in the reference's bridge; the
  * reference builds its fixtures with arkworks' StdRng in Rust:
  * hyperplonk/examples/full_prove_bench.rs, subroutines/examples/sumcheck_bench.rs).
