@@ -57,6 +57,13 @@ SIGNATURES: dict[str, list] = {
     "hp_cuda_v1_kernel_launch_count": [ctypes.POINTER(ctypes.c_uint64)],
     "hp_cuda_v1_fixture_random_fr": [ctypes.c_uint64, ctypes.c_uint64, c_size, c_u8p],
     "hp_cuda_v1_srs_generate": [c_voidp, c_size, ctypes.c_uint64, c_u8p, c_size],
+    "hp_cuda_v1_fixture_vanilla_plonk": [ctypes.c_uint64, c_size, c_u8p, c_u8p, c_u8p],
+    "hp_host_v1_merlin_new": [c_u8p, c_size, c_voidpp],
+    "hp_host_v1_merlin_append": [c_voidp, c_u8p, c_size, c_u8p, c_size],
+    "hp_host_v1_merlin_challenge": [c_voidp, c_u8p, c_size, c_u8p, c_size],
+    "hp_host_v1_merlin_clone": [c_voidp, c_voidpp],
+    "hp_host_v1_merlin_free": [c_voidp],
+    "hp_host_v1_keccak_f1600": [c_u8p],
 }
 
 _lib = None

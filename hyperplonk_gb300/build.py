@@ -32,7 +32,8 @@ def _nvcc() -> str:
 
 
 def sources() -> list[pathlib.Path]:
-    return sorted(CSRC.glob("*.cu"))
+    """CUDA translation units plus host-only C++ (the transcript)."""
+    return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
 
 
 def _headers() -> list[pathlib.Path]:
@@ -51,6 +52,9 @@ def build(verbose: bool = False, extra_flags: list[str] | None = None) -> pathli
     BUILD.mkdir(exist_ok=True)
     nvcc = _nvcc()
     headers = _headers()
+    if extra_flags is None and os.environ.get("HP_EXTRA_NVCC_FLAGS"):
+        # tuning hook: e.g. HP_EXTRA_NVCC_FLAGS="-DHP_FQ_INLINE" (forces a full rebuild)
+        extra_flags = os.environ["HP_EXTRA_NVCC_FLAGS"].split()
     flags = NVCC_FLAGS + (extra_flags or [])
     jobs = []
     for src in sources():

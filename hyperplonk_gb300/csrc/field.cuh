@@ -184,7 +184,7 @@ __device__ __forceinline__ Field<P> dbl(const Field<P> &a) {
 // the low halves and one for the high halves of a*b_i, then the same for
 // m*p.  4N^2 + N multiply-adds per product.
 template <class P>
-__device__ __forceinline__ Field<P> operator*(const Field<P> &a, const Field<P> &b) {
+__device__ __forceinline__ Field<P> mont_mul_inline(const Field<P> &a, const Field<P> &b) {
     constexpr int N = P::N;
     uint32_t t[N + 2];
 #pragma unroll
@@ -224,6 +224,25 @@ __device__ __forceinline__ Field<P> operator*(const Field<P> &a, const Field<P> 
     for (int i = 0; i < N; i++) r.v[i] = t[i];
     reduce_once<P>(r, t[N]);
     return r;
+}
+
+// The 12-limb product is ~1,000 SASS instructions; inlined at every call site
+// of a curve formula it overflows the instruction cache (ncu: instruction
+// fetch stalls dominate the MSM bucket kernel), so Fq products go through one
+// out-of-line copy per translation unit.  Arguments travel by value in
+// registers.
+#ifndef HP_FQ_INLINE
+static __device__ __noinline__ Field<FqParams> fq_mul_call(Field<FqParams> a, Field<FqParams> b) {
+    return mont_mul_inline<FqParams>(a, b);
+}
+#endif
+
+template <class P>
+__device__ __forceinline__ Field<P> operator*(const Field<P> &a, const Field<P> &b) {
+#ifndef HP_FQ_INLINE
+    if constexpr (P::N == 12) return fq_mul_call(a, b);
+#endif
+    return mont_mul_inline<P>(a, b);
 }
 
 template <class P>

@@ -22,6 +22,7 @@
 //  5. the host finishes the short Horner chain over those subset sums and
 //     converts to affine (one inversion), see host_ec.h.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -31,6 +32,11 @@
 namespace hp {
 
 int msm_window_bits(size_t n) {
+    // tuning override (read when a layer is prepared): HP_MSM_WINDOW_BITS=c, 4 <= c <= 22
+    if (const char *env = std::getenv("HP_MSM_WINDOW_BITS")) {
+        int c = std::atoi(env);
+        if (c >= 4 && c <= 22) return c;
+    }
     int best = 4;
     double best_cost = 1e300;
     for (int c = 4; c <= 20; c++) {
@@ -289,7 +295,10 @@ __global__ void k_msm_scatter(const Fr *scalars, size_t n, int c, int windows, u
 // Bucket accumulation: one thread per bucket, XYZZ mixed additions
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(128) k_msm_accumulate(const Affine *bases, const uint32_t *offsets,
+#ifndef HP_ACC_MINBLOCKS
+#define HP_ACC_MINBLOCKS 3  // measured best on GB300 at 2^20 (13.9 ms vs 14.2 ms at 1)
+#endif
+__global__ void __launch_bounds__(128, HP_ACC_MINBLOCKS) k_msm_accumulate(const Affine *bases, const uint32_t *offsets,
                                                         const uint32_t *records, size_t buckets, Xyzz *out) {
     for (size_t b = blockIdx.x * size_t(blockDim.x) + threadIdx.x; b < buckets;
          b += size_t(gridDim.x) * blockDim.x) {

@@ -199,3 +199,51 @@ extern "C" HpCudaStatus hp_cuda_v1_srs_generate(HpCudaContext *ctx, size_t num_v
         ctx->sync();
     });
 }
+
+// Vanilla-plonk fixture (full-prove workload): see include/hp_cuda.h.
+extern "C" HpCudaStatus hp_cuda_v1_fixture_vanilla_plonk(uint64_t seed, size_t num_vars, uint8_t *selectors,
+                                                         uint8_t *witnesses, uint8_t *permutation) {
+    return guard([&] {
+        require(selectors != nullptr && witnesses != nullptr && permutation != nullptr && num_vars <= 28);
+        const size_t n = size_t(1) << num_vars;
+        hp::host::Fr64 minus_one;
+        {
+            uint8_t b[32];
+            hp::host::Fr64 one = hp::host::one();
+            // -1 = r - 1 in canonical form
+            const uint64_t rm1[4] = {0xffffffff00000000ULL, 0x53bda402fffe5bfeULL, 0x3339d80809a1d805ULL,
+                                     0x73eda753299d7d48ULL};
+            std::memcpy(b, rm1, 32);
+            require(hp::host::from_canonical(b, minus_one));
+            (void)one;
+        }
+        unsigned threads = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+        if (n < 4096) threads = 1;
+        std::vector<std::thread> pool;
+        size_t chunk = (n + threads - 1) / threads;
+        for (unsigned t = 0; t < threads; t++) {
+            size_t b = t * chunk, e = std::min(n, b + chunk);
+            if (b >= e) break;
+            pool.emplace_back([=] {
+                using namespace hp::host;
+                for (size_t i = b; i < e; i++) {
+                    Fr64 ql = hp::fixture_element(seed, i), qr = hp::fixture_element(seed, n + i);
+                    Fr64 qm = hp::fixture_element(seed, 2 * n + i), qc = hp::fixture_element(seed, 3 * n + i);
+                    Fr64 w1 = hp::fixture_element(seed, 4 * n + i), w2 = hp::fixture_element(seed, 5 * n + i);
+                    Fr64 w3 = add(add(mont_mul(ql, w1), mont_mul(qr, w2)), add(mont_mul(mont_mul(qm, w1), w2), qc));
+                    const Fr64 sel[5] = {ql, qr, minus_one, qm, qc};
+                    const Fr64 wit[3] = {w1, w2, w3};
+                    for (int k = 0; k < 5; k++) to_canonical(sel[k], selectors + (size_t(k) * n + i) * 32);
+                    for (int k = 0; k < 3; k++) {
+                        to_canonical(wit[k], witnesses + (size_t(k) * n + i) * 32);
+                        uint8_t *p = permutation + (size_t(k) * n + i) * 32;
+                        std::memset(p, 0, 32);
+                        uint64_t label = uint64_t(k) * n + i;
+                        std::memcpy(p, &label, 8);
+                    }
+                }
+            });
+        }
+        for (auto &th : pool) th.join();
+    });
+}

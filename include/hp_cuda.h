@@ -217,6 +217,28 @@ HpCudaStatus hp_cuda_v1_mle_evaluate_noalloc(const void *table, size_t num_vars,
  * layers back to back as 97-byte packets, point_count = 2^(num_vars+1) - 1.
  * Computed on the device (fixed-base comb). */
 HpCudaStatus hp_cuda_v1_fixture_random_fr(uint64_t seed, uint64_t first, size_t count, uint8_t *out);
+/* Vanilla-plonk circuit of 2^num_vars gates for the full-prove workload:
+ * q_L, q_R, q_M, q_C, w1, w2 are elements [k*N, (k+1)*N), k = 0..5, of stream
+ * `seed`; q_O = -1; w3 = q_L w1 + q_R w2 + q_M w1 w2 + q_C, so the repo's gate
+ * q_L w1 + q_R w2 + q_O w3 + q_M w1 w2 + q_C = 0 (hyperplonk/src/custom_gate.rs:86-96)
+ * holds on every row.  Writes selectors [q_L, q_R, q_O, q_M, q_C] (5 tables),
+ * witnesses [w1, w2, w3] (3 tables) and the identity permutation
+ * (column * 2^num_vars + row, hyperplonk/src/snark.rs:69-76) as canonical Fr
+ * tables back to back.  Host-only. */
+HpCudaStatus hp_cuda_v1_fixture_vanilla_plonk(uint64_t seed, size_t num_vars, uint8_t *selectors,
+                                              uint8_t *witnesses, uint8_t *permutation);
+/* Host Fiat-Shamir transcript used by the protocol drivers (Merlin 1.0 over
+ * STROBE-128 / Keccak-f[1600]; the reference wraps merlin 3.0.0,
+ * transcript/src/lib.rs:40-131).  Host-only, no device work. */
+typedef struct HpMerlinTranscript HpMerlinTranscript;
+HpCudaStatus hp_host_v1_merlin_new(const uint8_t *label, size_t label_len, HpMerlinTranscript **out);
+HpCudaStatus hp_host_v1_merlin_append(HpMerlinTranscript *t, const uint8_t *label, size_t label_len,
+                                      const uint8_t *msg, size_t msg_len);
+HpCudaStatus hp_host_v1_merlin_challenge(HpMerlinTranscript *t, const uint8_t *label, size_t label_len,
+                                         uint8_t *out, size_t out_len);
+HpCudaStatus hp_host_v1_merlin_clone(const HpMerlinTranscript *t, HpMerlinTranscript **out);
+HpCudaStatus hp_host_v1_merlin_free(HpMerlinTranscript *t);
+HpCudaStatus hp_host_v1_keccak_f1600(uint8_t *state200);
 HpCudaStatus hp_cuda_v1_srs_generate(HpCudaContext *ctx, size_t num_vars, uint64_t seed,
                                      uint8_t *out_packets, size_t point_count);
 

@@ -19,7 +19,7 @@ G = (368541675371338701678108831518307775796162079578254640989457837868860759237
 def declared_entries():
     names = set()
     for h in (ROOT / "include").glob("*.h"):
-        names |= set(re.findall(r"\b(hp_cuda_v1_\w+)\s*\(", h.read_text()))
+        names |= set(re.findall(r"\b(hp_(?:cuda|host)_v1_\w+)\s*\(", h.read_text()))
     return sorted(names)
 
 

@@ -1,0 +1,57 @@
+"""Host transcript: the native Merlin/STROBE/Keccak (csrc/transcript.cpp)
+against the oracle's independent pure-Python restatement; Keccak-f[1600]
+pinned through SHA3-256 against hashlib.  CPU only."""
+import ctypes
+import hashlib
+import random
+
+import pytest
+
+from hyperplonk_gb300 import _native
+from hyperplonk_gb300.errors import check_status
+from hyperplonk_gb300.transcript import IOPTranscript, MerlinTranscript, TranscriptError
+
+import transcript_ref as tref
+
+
+@pytest.mark.parametrize("msg", [b"", b"abc", bytes(135), bytes(136), bytes(137), bytes(range(256)) * 3])
+def test_keccak_pinned_by_sha3(msg):
+    assert tref.sha3_256(msg) == hashlib.sha3_256(msg).digest()
+
+
+def test_native_keccak_matches_oracle(native_lib):
+    rng = random.Random(1)
+    for _ in range(5):
+        st = bytearray(rng.getrandbits(8) for _ in range(200))
+        ref = bytearray(st)
+        tref.keccak_f1600(ref)
+        buf = (ctypes.c_uint8 * 200)(*st)
+        check_status(native_lib.hp_host_v1_keccak_f1600(buf), "keccak")
+        assert bytes(buf) == bytes(ref)
+
+
+def test_native_merlin_matches_oracle(native_lib):
+    rng = random.Random(2)
+    a, b = MerlinTranscript(b"test protocol"), tref.Merlin(b"test protocol")
+    for step in range(40):
+        label = b"label-%d" % step
+        if rng.random() < 0.6:
+            msg = bytes(rng.getrandbits(8) for _ in range(rng.choice([0, 1, 31, 32, 100, 165, 166, 167, 400])))
+            a.append_message(label, msg)
+            b.append_message(label, msg)
+        else:
+            n = rng.choice([1, 32, 64, 200])
+            assert a.challenge_bytes(label, n) == b.challenge_bytes(label, n)
+    c = a.clone()
+    assert c.challenge_bytes(b"x", 64) == a.challenge_bytes(b"x", 64)
+
+
+def test_iop_transcript_challenges_match():
+    a = IOPTranscript(b"Initializing SumCheck transcript")
+    b = tref.OracleIOPTranscript(b"Initializing SumCheck transcript")
+    with pytest.raises(TranscriptError):
+        a.get_and_append_challenge(b"Internal round")
+    for t in (a, b):
+        t.append_serializable_element(b"aux info", (2).to_bytes(8, "little") + (20).to_bytes(8, "little"))
+        t.append_field_element(b"x", 12345)
+    assert a.get_and_append_challenge_vectors(b"0check r", 5) == b.get_and_append_challenge_vectors(b"0check r", 5)
