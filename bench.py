@@ -1,25 +1,33 @@
 #!/usr/bin/env python3
-"""Benchmark of the GB300 HyperPlonk prover hot path: multilinear-KZG commit.
+"""Benchmark of the GB300 HyperPlonk prover hot path.
 
-Workload (one step): commit one MLE of 2^nv uniform Fr (fixture stream seed 0)
-against the prepared testing SRS of nv variables (fixture stream seed 0,
-generated on the device) -- i.e. one 2^nv-point G1 MSM through the
-reference-facing C ABI (hp_cuda_v1_multilinear_kzg_commit).  Default nv = 20,
-the 2^20-point MSM of the reference's published MSM numbers; --num-vars 16 is
-the configuration-1 size.  Metric: MSM pts/s (points per second).
+Workloads (--workload):
 
-  value : commit through the C ABI with the MLE already resident in HBM;
-  e2e   : the same through the C ABI from a pinned host buffer each step
-          (mle_upload H2D + commit + 97-byte result + retire).
+  prove  (default) -- full HyperPlonk prove of the vanilla-plonk circuit of
+         2^nv gates (configuration 3: q_L, q_R, q_M, q_C, w1, w2 uniform, q_O
+         = -1, w3 solving the gate, identity permutation over 3 columns, 16
+         public inputs, fixture seed 2, testing SRS of nv variables).  One step
+         = one proof through the reference-facing C ABI (witness commits,
+         gate zero-check, permutation check, 22 evaluations, batch opening),
+         proof serialized to bytes.  Metric: HyperPlonk proofs/s, with p50/p99
+         proof latency.  The MSM pts/s of a 2^nv commit on the same SRS is
+         reported beside it ("msm").
+  commit -- one multilinear-KZG commit of a 2^nv-point MLE (configuration 1
+         shape; nv = 16 is configuration 1 itself).  Metric: MSM pts/s.
+
+  value : inputs already resident in HBM (witness MLEs uploaded before the
+          timed loop);
+  e2e   : the same through the C ABI from pinned host buffers every step
+          (mle_upload of the inputs + the work + results back on the host).
 
 Timing: W warm-up steps, then K steps each bracketed by CUDA events on the
 backend's own stream (hp_cuda_v1_context_stream), a barrier and
-torch.cuda.synchronize() on both sides of the timed loop; between steps a
-256 MiB buffer is written to flush L2 (the MSM's precomputed base table,
-~1.3 GB at nv=20, is larger than L2 anyway).  The dominant kernel
-(msm_accumulate) is timed by the library's own event hooks on the same
-stream.  --impl reference times the CPU restatement of the reference's CPU
-path (oracle, all host threads) on a bounded sample of the workload.
+torch.cuda.synchronize() on both sides of the timed loop; a 256 MiB buffer is
+written between steps to flush L2 (the prepared SRS, ~2.6 GB at nv=20, is
+larger than L2 anyway).  The dominant kernel (k_msm_accumulate) is timed by
+the library's own CUDA-event hooks on the same stream.  --impl reference
+times the CPU restatement of the reference's CPU path (oracle, all host
+threads) on a bounded sample of the workload.
 """
 from __future__ import annotations
 
@@ -40,6 +48,7 @@ sys.path.insert(0, str(ROOT))
 
 FQ_MUL_IMAD = 588  # 32-bit-limb CIOS, n = 12: 2n^2 + 2n^2 + n
 FR_MUL_IMAD = 264
+PROVE_SEED = 2
 
 
 def parse():
@@ -48,9 +57,33 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=["prove", "commit"], default="prove")
     ap.add_argument("--num-vars", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
+
+
+def window_bits(n: int) -> int:
+    """Window width the library picks for an n-point layer (msm.cu)."""
+    env = os.environ.get("HP_MSM_WINDOW_BITS")
+    if env and 4 <= int(env) <= 22:
+        return int(env)
+    best, best_cost = 4, float("inf")
+    for c in range(4, 21):
+        top_bits = 255 - c * (math.ceil(256 / c) - 1)
+        top_buckets = float(1 << (top_bits - 1)) if top_bits >= 2 else 1.0
+        if c > 4 and n / top_buckets > 2048.0:
+            continue
+        cost = math.ceil(256 / c) * 10.0 * n + 28.0 * (1 << (c - 1))
+        if cost < best_cost:
+            best, best_cost = c, cost
+    return best
+
+
+def accumulate_imad(n: int) -> int:
+    """Algorithmic work of k_msm_accumulate for one n-point MSM: one XYZZ
+    mixed addition (10 Fq muls) per (point, window) record."""
+    return math.ceil(256 / window_bits(n)) * n * 10 * FQ_MUL_IMAD
 
 
 def msm_accounting_imad(n: int) -> float:
@@ -58,6 +91,12 @@ def msm_accounting_imad(n: int) -> float:
     Fq multiplications at 588 IMAD each."""
     best = min(math.ceil(255 / c) * (10 * n + 14 * (1 << c)) for c in range(8, 21))
     return best * FQ_MUL_IMAD
+
+
+def prove_msm_sizes(nv: int) -> list:
+    """MSMs of one proof: 3 witness commits, frac and prod commits (2^nv each)
+    and the batch opening's nv quotient MSMs (2^(nv-1) .. 1)."""
+    return [1 << nv] * 5 + [1 << (nv - 1 - i) for i in range(nv)]
 
 
 # ---------------------------------------------------------------------------
@@ -147,20 +186,23 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline (oracle restatement of the reference CPU path)
+# CPU baselines (oracle restatement of the reference CPU path)
 # ---------------------------------------------------------------------------
+
+def _oracle():
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as orc
+    return orc
+
 
 class CpuMsmSample:
     """The oracle's multithreaded Pippenger MSM (the CPU restatement of ark-ec
     msm_unchecked as used by backend/src/cpu/multilinear_kzg.rs:40-59) on a
-    2^log_n-point sample of the workload (testing SRS and fixture scalars,
-    seed 0), prepared once."""
+    2^log_n-point sample (testing SRS and fixture scalars, seed 0)."""
 
     def __init__(self, log_n: int = 16):
-        sys.path.insert(0, str(ROOT / "oracle"))
-        import oracle as orc
-        self.orc = orc
-        self.log_n = log_n
+        orc = _oracle()
+        self.orc, self.log_n = orc, log_n
         self.threads = orc.set_threads(0)
         self.bases = orc.srs_layers(log_n, 0)[0]
         self.scalars = orc.random_fr(0, 1 << log_n)
@@ -171,133 +213,209 @@ class CpuMsmSample:
         return time.perf_counter() - t0
 
 
-def cpu_msm_sample(steps: int, log_n: int = 16):
-    """(pts/s, threads, median seconds per MSM) over `steps` timed MSMs."""
-    s = CpuMsmSample(log_n)
-    per = statistics.median([s.step() for _ in range(steps)])
-    return (1 << log_n) / per, s.threads, per
+class CpuProveSample:
+    """The oracle prover: the same driver over the oracle's CpuBackend
+    (backend/src/cpu restated, multithreaded MSM) and the oracle's Python
+    transcript, on the configuration-3 circuit at 2^nv gates."""
+
+    def __init__(self, nv: int):
+        from hyperplonk_gb300 import snark
+        orc = _oracle()
+        import transcript_ref as tref  # oracle/transcript_ref.py (path set by _oracle)
+        self.snark, self.tcls = snark, tref.OracleIOPTranscript
+        self.threads = orc.set_threads(0)
+        self.cpu = orc.CpuBackend()
+        self.nv = nv
+        sel, self.wit, perm, self.pub = snark.vanilla_fixture(nv, PROVE_SEED)
+        self.pk = snark.preprocess(self.cpu, nv, min(16, 1 << nv), sel, perm, orc.srs_layers(nv, 0))
+
+    def step(self) -> float:
+        t0 = time.perf_counter()
+        self.snark.prove(self.cpu, self.pk, self.pub, self.wit, transcript_cls=self.tcls).to_bytes()
+        return time.perf_counter() - t0
 
 
 # ---------------------------------------------------------------------------
 # GB300 arm
 # ---------------------------------------------------------------------------
 
-def run_gb300(args, world, rank, local, pg):
-    import numpy as np
-    import torch
-    from hyperplonk_gb300 import _native
-    from hyperplonk_gb300.backend import CudaBackend, CudaMle
-    from hyperplonk_gb300.errors import check_status
+class Session:
+    def __init__(self, local: int):
+        import torch
+        from hyperplonk_gb300.backend import CudaBackend
+        self.torch = torch
+        torch.cuda.set_device(local)
+        self.local = local
+        self.be = CudaBackend(local)
+        self.lib = self.be.lib
+        self.stream = torch.cuda.ExternalStream(self.be.ctx.stream(), device=torch.device("cuda", local))
+        self.flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
-    torch.cuda.set_device(local)
-    nv = args.num_vars
-    n = 1 << nv
-    be = CudaBackend(local)
-    lib = be.lib
-    stream = torch.cuda.ExternalStream(be.ctx.stream(), device=torch.device("cuda", local))
+    def check(self, status, op):
+        from hyperplonk_gb300.errors import check_status
+        check_status(status, op)
 
-    # SRS (device-generated testing SRS, seed 0) -> prepared params
-    total = (1 << (nv + 1)) - 1
-    packets = np.empty(total * 97, dtype=np.uint8)
-    check_status(lib.hp_cuda_v1_srs_generate(be.ctx.raw, nv, 0, _native.buf(packets), total), "srs_generate")
-    layers, off = [], 0
-    for i in range(nv + 1):
-        cnt = 1 << (nv - i) if i < nv else 1
-        layers.append(packets[97 * off:97 * (off + cnt)])
-        off += cnt
-    params = be.prepare_prover_param(nv, layers)
-    del packets, layers
-
-    # scalars: fixture stream seed 0, in pinned host memory
-    host = torch.empty(32 * n, dtype=torch.uint8, pin_memory=True)
-    hv = host.numpy()
-    check_status(lib.hp_cuda_v1_fixture_random_fr(0, 0, n, _native.buf(hv)), "fixture_random_fr")
-    mle = be.mle_from_evaluations(nv, hv)
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
-
-    def launches() -> int:
+    def launches(self) -> int:
         c = ctypes.c_uint64()
-        check_status(lib.hp_cuda_v1_kernel_launch_count(ctypes.byref(c)), "kernel_launch_count")
+        self.check(self.lib.hp_cuda_v1_kernel_launch_count(ctypes.byref(c)), "kernel_launch_count")
         return c.value
 
-    def timed(fn, steps):
+    def profile(self, on: bool):
+        self.check(self.lib.hp_cuda_v1_context_profile(self.be.ctx.raw, 1 if on else 0), "context_profile")
+
+    def profile_read(self, name: bytes):
+        ms, cnt = ctypes.c_double(), ctypes.c_uint64()
+        self.check(self.lib.hp_cuda_v1_context_profile_read(self.be.ctx.raw, name, ctypes.byref(ms),
+                                                            ctypes.byref(cnt)), "profile_read")
+        return ms.value, cnt.value
+
+    def timed(self, fn, steps):
+        torch = self.torch
         per = []
-        with torch.cuda.stream(stream):
+        with torch.cuda.stream(self.stream):
             for _ in range(steps):
-                flush.fill_(1)
+                self.flush_buf.fill_(1)
                 a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                a.record(stream)
+                a.record(self.stream)
                 fn()
-                b.record(stream)
+                b.record(self.stream)
                 b.synchronize()
                 per.append(a.elapsed_time(b) / 1e3)
         return per
 
-    commit_once = lambda: be.commit(params, mle)  # noqa: E731
+    def srs_layers(self, nv: int, seed: int):
+        import numpy as np
+        from hyperplonk_gb300 import _native
+        total = (1 << (nv + 1)) - 1
+        packets = np.empty(total * 97, dtype=np.uint8)
+        self.check(self.lib.hp_cuda_v1_srs_generate(self.be.ctx.raw, nv, seed, _native.buf(packets), total),
+                   "srs_generate")
+        layers, off = [], 0
+        for i in range(nv + 1):
+            cnt = 1 << (nv - i) if i < nv else 1
+            layers.append(packets[97 * off:97 * (off + cnt)])
+            off += cnt
+        return layers
 
-    def e2e_once():
-        m = be.mle_from_evaluations(nv, hv)
-        be.commit(params, m)
-        del m
+    def pinned(self, arr):
+        t = self.torch.empty(arr.nbytes, dtype=self.torch.uint8, pin_memory=True)
+        t.numpy()[:] = arr.reshape(-1)
+        return t
 
-    for _ in range(args.warmup):
-        commit_once()
-        e2e_once()
+    def integer_rates(self):
+        probe = ctypes.CDLL(str(ROOT / "hyperplonk_gb300" / "_build" / "libhp_probe.so"))
+        probe.hp_probe_integer_rates.argtypes = [ctypes.c_int] + [ctypes.POINTER(ctypes.c_double)] * 3
+        imad, fqm, frm = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        rc = probe.hp_probe_integer_rates(self.local, ctypes.byref(imad), ctypes.byref(fqm), ctypes.byref(frm))
+        if rc != 0:
+            raise RuntimeError(f"integer probe failed ({rc})")
+        return imad.value, fqm.value, frm.value
 
-    # ---- value: device-resident input ----
-    check_status(lib.hp_cuda_v1_context_profile(be.ctx.raw, 1), "context_profile")
-    clocks = ClockSampler(local)
+
+def measure(s: Session, pg, steps: int, value_fn, e2e_fn):
+    """Timed loops; returns (value step seconds list, e2e list, launches, clocks, accumulate ms/launches)."""
+    s.profile(True)
+    clocks = ClockSampler(s.local)
     barrier(pg)
-    torch.cuda.synchronize()
+    s.torch.cuda.synchronize()
     clocks.start()
-    l0 = launches()
-    t0 = time.perf_counter()
-    per = timed(commit_once, args.steps)
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
-    l1 = launches()
+    l0 = s.launches()
+    per = s.timed(value_fn, steps)
+    s.torch.cuda.synchronize()
+    l1 = s.launches()
     barrier(pg)
     clk = clocks.stop()
-    step_s = max_over_ranks(pg, sum(per) / len(per))
-    ms = ctypes.c_double()
-    cnt = ctypes.c_uint64()
-    check_status(lib.hp_cuda_v1_context_profile_read(be.ctx.raw, b"msm_accumulate", ctypes.byref(ms),
-                                                     ctypes.byref(cnt)), "profile_read")
-    acc_ms = ms.value / max(1, cnt.value)
-    check_status(lib.hp_cuda_v1_context_profile_read(be.ctx.raw, b"msm", ctypes.byref(ms), ctypes.byref(cnt)),
-                 "profile_read")
-    msm_ms = ms.value / max(1, cnt.value)
-    check_status(lib.hp_cuda_v1_context_profile(be.ctx.raw, 0), "context_profile")
-
-    # ---- e2e: host buffer in, result out, every step ----
+    acc = s.profile_read(b"msm_accumulate")
+    msm = s.profile_read(b"msm")
+    s.profile(False)
     barrier(pg)
-    torch.cuda.synchronize()
-    per_e2e = timed(e2e_once, args.steps)
-    torch.cuda.synchronize()
+    s.torch.cuda.synchronize()
+    per_e2e = s.timed(e2e_fn, steps)
+    s.torch.cuda.synchronize()
     barrier(pg)
-    e2e_s = max_over_ranks(pg, sum(per_e2e) / len(per_e2e))
+    return per, per_e2e, l1 - l0, clk, acc, msm
 
-    # ---- integer-pipe ceilings on this GPU ----
-    probe = ctypes.CDLL(str(ROOT / "hyperplonk_gb300" / "_build" / "libhp_probe.so"))
-    probe.hp_probe_integer_rates.argtypes = [ctypes.c_int] + [ctypes.POINTER(ctypes.c_double)] * 3
-    imad, fqm, frm = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
-    rc = probe.hp_probe_integer_rates(local, ctypes.byref(imad), ctypes.byref(fqm), ctypes.byref(frm))
-    if rc != 0:
-        raise RuntimeError(f"integer probe failed ({rc})")
 
-    # dominant kernel roofline: W*n point-window records x one XYZZ mixed add
-    # (10 Fq muls) each
-    c_bits = next(c for c in range(4, 21) if c == _window_bits(n))
-    windows = math.ceil(256 / c_bits)
-    acc_imad = windows * n * 10 * FQ_MUL_IMAD
-    achieved = acc_imad / (acc_ms / 1e3) / 1e12
-    peak = imad.value / 1e12
+def run_gb300(args, world, rank, local, pg):
+    s = Session(local)
+    nv = args.num_vars
+    n = 1 << nv
+    be = s.be
+    layers = s.srs_layers(nv, 0)
+
+    if args.workload == "commit":
+        import numpy as np
+        from hyperplonk_gb300 import _native
+        params = be.prepare_prover_param(nv, layers)
+        del layers
+        hv = np.empty(32 * n, dtype=np.uint8)
+        s.check(s.lib.hp_cuda_v1_fixture_random_fr(0, 0, n, _native.buf(hv)), "fixture_random_fr")
+        host = s.pinned(hv)
+        hvp = host.numpy()
+        mle = be.mle_from_evaluations(nv, hvp)
+        value_fn = lambda: be.commit(params, mle)  # noqa: E731
+
+        def e2e_fn():
+            m = be.mle_from_evaluations(nv, hvp)
+            be.commit(params, m)
+
+        for _ in range(args.warmup):
+            value_fn()
+            e2e_fn()
+        per, per_e2e, nl, clk, acc, msm = measure(s, pg, args.steps, value_fn, e2e_fn)
+        units, metric, unit = n, "MSM pts/s", "pts/s"
+        acc_work = accumulate_imad(n) * acc[1]
+        workload = f"multilinear-KZG commit of one MLE, num_vars={nv} (one 2^{nv}-point G1 MSM)"
+        h2d, d2h = 32 * n, 97
+        extra = {}
+    else:
+        from hyperplonk_gb300 import snark
+        sel, wit, perm, pub = snark.vanilla_fixture(nv, PROVE_SEED)
+        pk = snark.preprocess(be, nv, min(16, n), sel, perm, layers)
+        del layers, sel, perm
+        pinned = [s.pinned(w) for w in wit]
+        wit_host = [p.numpy() for p in pinned]
+        resident = [be.mle_from_evaluations(nv, w) for w in wit_host]
+        out = {}
+
+        def value_fn():
+            out["proof"] = snark.prove(be, pk, pub, None, witness_mles=resident).to_bytes()
+
+        def e2e_fn():
+            out["proof"] = snark.prove(be, pk, pub, wit_host).to_bytes()
+
+        for _ in range(args.warmup):
+            value_fn()
+            e2e_fn()
+        per, per_e2e, nl, clk, acc, msm = measure(s, pg, args.steps, value_fn, e2e_fn)
+        units, metric, unit = 1, "HyperPlonk proofs/s", "proofs/s"
+        acc_work = sum(accumulate_imad(m) for m in prove_msm_sizes(nv)) * args.steps
+        workload = (f"full HyperPlonk prove, vanilla-plonk circuit of 2^{nv} gates (q_O = -1, w3 solves the gate, "
+                    f"identity permutation over 3 columns, 16 public inputs, seed {PROVE_SEED}), testing SRS nv={nv}")
+        h2d, d2h = 3 * 32 * n, len(out["proof"])
+        lat = sorted(per)
+        extra = {"latency_ms": {"p50": 1e3 * statistics.median(lat),
+                                "p99": 1e3 * lat[min(len(lat) - 1, math.ceil(0.99 * len(lat)) - 1)],
+                                "min": 1e3 * lat[0], "max": 1e3 * lat[-1]},
+                 "proof_bytes": len(out["proof"])}
+        # MSM pts/s of a 2^nv commit on the same prepared SRS (witness w1)
+        commit = lambda: be.commit(pk.pcs_param, resident[0])  # noqa: E731
+        commit()
+        cper = s.timed(commit, max(3, args.steps // 2))
+        extra["msm"] = {"metric": "MSM pts/s", "value": world * n / max_over_ranks(pg, statistics.mean(cper)),
+                        "unit": "pts/s", "points": n, "ms_per_msm": 1e3 * statistics.mean(cper)}
+
+    step_s = max_over_ranks(pg, statistics.mean(per))
+    e2e_s = max_over_ranks(pg, statistics.mean(per_e2e))
+    imad, fqm, frm = s.integer_rates()
+    acc_ms_total = acc[0]
+    achieved = acc_work / (acc_ms_total / 1e3) / 1e12 if acc_ms_total > 0 else 0.0
+    peak = imad / 1e12
     traffic = _profile_traffic(nv)
-
     result = {
-        "metric": "MSM pts/s",
-        "value": world * n / step_s,
-        "unit": "pts/s",
+        "metric": metric,
+        "value": world * units / step_s,
+        "unit": unit,
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
@@ -306,42 +424,47 @@ def run_gb300(args, world, rank, local, pg):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "u32 limbs (Fr 8x32, Fq 12x32 Montgomery)",
-        "data": "synthetic: ChaCha20 fixture stream seed 0, device-generated testing SRS (seed 0)",
-        "config": {"workload": f"multilinear-KZG commit of one MLE, num_vars={nv} (one 2^{nv}-point G1 MSM)",
-                   "num_vars": nv, "points": n, "window_bits": c_bits, "windows": windows,
-                   "l2": "256 MiB flush between steps; base table > L2",
+        "data": "synthetic: ChaCha20 fixture streams (seed 0 SRS/scalars, seed 2 circuit), device-generated "
+                "testing SRS",
+        "config": {"workload": workload, "num_vars": nv, "window_bits": window_bits(n),
+                   "l2": "256 MiB flush between steps; prepared SRS > L2",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
-        "e2e": {"value": world * n / e2e_s, "unit": "pts/s", "h2d_bytes_per_step": 32 * n,
-                "d2h_bytes_per_step": 97},
-        "gpu_launches": int(l1 - l0),
+        "e2e": {"value": world * units / e2e_s, "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(nl),
         "roofline": {"bound": "imad", "kernel": "k_msm_accumulate", "achieved": achieved, "peak": peak,
-                     "unit": "TIMAD/s", "frac": achieved / peak, "traffic": traffic,
+                     "unit": "TIMAD/s", "frac": achieved / peak if peak else None, "traffic": traffic,
                      "peak_source": "measured live: mad.lo.u32 issue rate on this GPU (libhp_probe)",
-                     "per_launch_ms": acc_ms, "algorithmic_imad_per_launch": acc_imad},
-        "msm_total": {"ms": msm_ms, "accounting_imad": msm_accounting_imad(n),
-                      "achieved_tiimad_s": msm_accounting_imad(n) / (msm_ms / 1e3) / 1e12,
-                      "frac_of_imad_peak": msm_accounting_imad(n) / (msm_ms / 1e3) / imad.value},
-        "field_rates": {"fq_mul_per_s": fqm.value, "fr_mul_per_s": frm.value,
-                        "fq_mul_imad_equiv_tiimad_s": fqm.value * FQ_MUL_IMAD / 1e12},
+                     "launches": acc[1], "per_launch_ms": acc_ms_total / max(1, acc[1]),
+                     "algorithmic_imad_per_launch": acc_work / max(1, acc[1])},
+        "msm_phase": {"ms_per_step": msm[0] / max(1, args.steps), "msm_launches": msm[1],
+                      "share_of_step": (msm[0] / max(1, args.steps)) / (step_s * 1e3)},
+        "field_rates": {"fq_mul_per_s": fqm, "fr_mul_per_s": frm, "fq_mul_imad_equiv_tiimad_s": fqm * FQ_MUL_IMAD / 1e12},
         "clocks": clk,
-        "wall_s_timed_loop": wall,
     }
+    result.update(extra)
+    if args.workload == "commit":
+        result["msm_total"] = {"ms": msm[0] / max(1, msm[1]), "accounting_imad": msm_accounting_imad(n),
+                               "frac_of_imad_peak": msm_accounting_imad(n) / (msm[0] / max(1, msm[1]) / 1e3) / imad}
     if rank == 0 and not args.no_cpu_baseline:
-        v, threads, per_s = cpu_msm_sample(3)
-        result["cpu_baseline"] = {"value": v, "unit": "pts/s", "cores": threads, "kind": "port",
-                                  "sample": f"oracle Pippenger MSM of 2^16 points (testing SRS nv=16, "
-                                            f"fixture seed 0), median of 3, {per_s:.3f} s each"}
+        result["cpu_baseline"] = cpu_baseline(args.workload, nv)
     if rank == 0:
         print(json.dumps(result))
 
 
-def _window_bits(n: int) -> int:
-    best, best_cost = 4, float("inf")
-    for c in range(4, 21):
-        cost = math.ceil(256 / c) * 10.0 * n + 28.0 * (1 << (c - 1))
-        if cost < best_cost:
-            best, best_cost = c, cost
-    return best
+def cpu_baseline(workload: str, nv: int) -> dict:
+    if workload == "commit":
+        sample = CpuMsmSample(16)
+        per = statistics.median([sample.step() for _ in range(3)])
+        return {"value": (1 << 16) / per, "unit": "pts/s", "cores": sample.threads, "kind": "port",
+                "sample": f"oracle Pippenger MSM of 2^16 points (testing SRS nv=16, fixture seed 0), median of 3, "
+                          f"{per:.3f} s each"}
+    snv = min(nv, 16)  # oracle prove time is linear in gates from 2^16 up (2.9 s at 16, 11.4 s at 18)
+    sample = CpuProveSample(snv)
+    per = statistics.median([sample.step() for _ in range(2)])
+    scale = 1 << (nv - snv)
+    return {"value": 1.0 / (per * scale), "unit": "proofs/s", "cores": sample.threads, "kind": "port",
+            "sample": f"oracle prover (CPU backend restatement + Python transcript) on the same circuit at 2^{snv} "
+                      f"gates, median of 2 = {per:.2f} s, scaled linearly by {scale} to 2^{nv} gates"}
 
 
 def _profile_traffic(nv: int):
@@ -365,23 +488,32 @@ def _profile_traffic(nv: int):
 def run_reference(args, world, rank):
     if rank != 0:
         return
-    sample = CpuMsmSample(16)
+    nv = args.num_vars
+    if args.workload == "commit":
+        sample, units, metric, unit, snv = CpuMsmSample(16), 1 << 16, "MSM pts/s", "pts/s", 16
+        desc = "oracle Pippenger MSM of 2^16 points per step"
+        scale = 1
+    else:
+        snv = min(nv, 16)  # oracle prove time is linear in gates from 2^16 up (2.9 s at 16, 11.4 s at 18)
+        sample, units, metric, unit = CpuProveSample(snv), 1, "HyperPlonk proofs/s", "proofs/s"
+        scale = 1 << (nv - snv)
+        desc = (f"oracle prover on the configuration-3 circuit at 2^{snv} gates per step, throughput scaled "
+                f"linearly by {scale} to 2^{nv} gates")
     for _ in range(args.warmup):
         sample.step()
     per = [sample.step() for _ in range(args.steps)]
-    step = sum(per) / len(per)
-    v = (1 << 16) / step
+    step = sum(per) / len(per) * scale
+    v = units / step
     print(json.dumps({
-        "impl": "reference", "metric": "MSM pts/s", "value": v, "unit": "pts/s", "n_gpus": world,
+        "impl": "reference", "metric": metric, "value": v, "unit": unit, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64 limbs (Montgomery)",
-        "data": "synthetic: ChaCha20 fixture stream seed 0, oracle testing SRS nv=16",
-        "config": {"workload": f"multilinear-KZG commit, num_vars={args.num_vars}: bounded sample of 2^16 points "
-                               "per step", "num_vars": args.num_vars},
-        "cpu_baseline": {"value": v, "unit": "pts/s", "cores": sample.threads, "kind": "port",
-                         "sample": "oracle Pippenger MSM of 2^16 points per step (the reference's Rust/arkworks "
-                                   "CPU path cannot be built here: no cargo, arkworks not vendored)"},
-        "e2e": {"value": v, "unit": "pts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "data": "synthetic: ChaCha20 fixture streams, oracle testing SRS",
+        "config": {"workload": f"{args.workload}, num_vars={nv}: bounded CPU sample (2^{snv})", "num_vars": nv},
+        "cpu_baseline": {"value": v, "unit": unit, "cores": sample.threads, "kind": "port",
+                         "sample": desc + " (the reference's Rust/arkworks CPU path cannot be built here: no cargo, "
+                                          "arkworks not vendored)"},
+        "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
 
 

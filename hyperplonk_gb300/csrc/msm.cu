@@ -40,6 +40,12 @@ int msm_window_bits(size_t n) {
     int best = 4;
     double best_cost = 1e300;
     for (int c = 4; c <= 20; c++) {
+        // The top window holds only 255 - c(W-1) bits of a scalar (< 2^255):
+        // its n records fall into that many bits' worth of buckets.  Skip
+        // widths that would pile more than 2048 records onto one bucket.
+        const int top_bits = 255 - c * (msm_windows(c) - 1);
+        const double top_buckets = top_bits >= 2 ? double(size_t(1) << (top_bits - 1)) : 1.0;
+        if (c > 4 && double(n) / top_buckets > 2048.0) continue;
         double cost = double(msm_windows(c)) * 10.0 * double(n) + 28.0 * double(size_t(1) << (c - 1));
         if (cost < best_cost) {
             best_cost = cost;
@@ -292,26 +298,80 @@ __global__ void k_msm_scatter(const Fr *scalars, size_t n, int c, int windows, u
 }
 
 // ---------------------------------------------------------------------------
-// Bucket accumulation: one thread per bucket, XYZZ mixed additions
+// Bucket accumulation: flat record chunks, XYZZ mixed additions
 // ---------------------------------------------------------------------------
+//
+// The records are grouped by bucket (CSR `offsets`).  Thread t owns records
+// [t*L, (t+1)*L) regardless of bucket boundaries, so every thread does the
+// same number of mixed additions (bucket sizes are Poisson distributed and a
+// top window with few bits can pile many records onto a few buckets).  A
+// bucket lying inside one chunk is written directly; a bucket cut by chunk
+// boundaries leaves one partial sum per chunk it touches (`pieces`, two slots
+// per chunk: [2t] = the chunk's first segment when it began before the chunk,
+// [2t+1] = its last segment when it runs past the chunk), which
+// k_msm_bucket_fixup adds up.
 
 #ifndef HP_ACC_MINBLOCKS
 #define HP_ACC_MINBLOCKS 3  // measured best on GB300 at 2^20 (13.9 ms vs 14.2 ms at 1)
 #endif
+constexpr uint32_t kChunkRecords = 32;
+
+// largest b in [0, buckets) with offsets[b] <= k (k < offsets[buckets])
+__device__ __forceinline__ uint32_t bucket_of(const uint32_t *offsets, uint32_t buckets, uint32_t k) {
+    uint32_t lo = 0, hi = buckets;  // offsets[lo] <= k < offsets[hi]
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (offsets[mid] <= k) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
 __global__ void __launch_bounds__(128, HP_ACC_MINBLOCKS) k_msm_accumulate(const Affine *bases, const uint32_t *offsets,
-                                                        const uint32_t *records, size_t buckets, Xyzz *out) {
-    for (size_t b = blockIdx.x * size_t(blockDim.x) + threadIdx.x; b < buckets;
-         b += size_t(gridDim.x) * blockDim.x) {
-        uint32_t begin = offsets[b], end = offsets[b + 1];
+                                                                          const uint32_t *records, uint32_t buckets,
+                                                                          Xyzz *bucket_sums, Xyzz *pieces) {
+    const uint32_t total = offsets[buckets];
+    const uint32_t chunks = (total + kChunkRecords - 1) / kChunkRecords;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < chunks; t += gridDim.x * blockDim.x) {
+        const uint32_t lo = t * kChunkRecords, hi = min(lo + kChunkRecords, total);
+        uint32_t b = bucket_of(offsets, buckets, lo);
+        uint32_t b_end = offsets[b + 1];
         Xyzz acc = xyzz_inf();
-        for (uint32_t k = begin; k < end; k++) {
+        for (uint32_t k = lo;; k++) {
+            if (k == hi || k == b_end) {
+                // flush the segment of bucket b that ends at k
+                const bool starts_inside = offsets[b] >= lo;
+                const bool ends_inside = b_end <= hi;
+                if (starts_inside && ends_inside) store_xyzz(&bucket_sums[b], acc);
+                else if (!starts_inside) store_xyzz(&pieces[2 * size_t(t)], acc);
+                else store_xyzz(&pieces[2 * size_t(t) + 1], acc);
+                if (k == hi) break;
+                // next non-empty bucket containing record k
+                do { b++; b_end = offsets[b + 1]; } while (b_end <= k);
+                acc = xyzz_inf();
+            }
             uint32_t rec = records[k];
             Affine a = load_affine(&bases[rec & 0x7fffffffu]);
             if (affine_is_inf(a)) continue;
             if (rec & 0x80000000u) a.y = neg(a.y);
             acc = xyzz_add_affine(acc, a.x, a.y);
         }
-        store_xyzz(&out[b], acc);
+    }
+}
+
+// Buckets cut by chunk boundaries: add their pieces; empty buckets: infinity.
+__global__ void k_msm_bucket_fixup(const uint32_t *offsets, uint32_t buckets, const Xyzz *pieces,
+                                   Xyzz *bucket_sums) {
+    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < buckets; b += gridDim.x * blockDim.x) {
+        const uint32_t begin = offsets[b], end = offsets[b + 1];
+        if (begin == end) {
+            store_xyzz(&bucket_sums[b], xyzz_inf());
+            continue;
+        }
+        const uint32_t t0 = begin / kChunkRecords, t1 = (end - 1) / kChunkRecords;
+        if (t0 == t1) continue;
+        Xyzz acc = load_xyzz(&pieces[2 * size_t(t0) + 1]);
+        for (uint32_t t = t0 + 1; t <= t1; t++) acc = xyzz_add(acc, load_xyzz(&pieces[2 * size_t(t)]));
+        store_xyzz(&bucket_sums[b], acc);
     }
 }
 
@@ -401,11 +461,17 @@ void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz 
     k_msm_scatter<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(scalars, n, layer.c, layer.windows,
                                                                   cursor.as<uint32_t>(), recs.as<uint32_t>());
     check_launch();
+    const size_t record_chunks = (records + kChunkRecords - 1) / kChunkRecords;
+    Scratch pieces(ctx, std::max<size_t>(2 * record_chunks, 1) * sizeof(Xyzz));
     int tok = ctx->prof_begin("msm_accumulate");
-    k_msm_accumulate<<<grid_for(ctx, B, 128, 16), 128, 0, ctx->stream>>>(
-        layer.bases, offsets.as<uint32_t>(), recs.as<uint32_t>(), B, buckets.as<Xyzz>());
+    k_msm_accumulate<<<grid_for(ctx, record_chunks, 128, 16), 128, 0, ctx->stream>>>(
+        layer.bases, offsets.as<uint32_t>(), recs.as<uint32_t>(), uint32_t(B), buckets.as<Xyzz>(),
+        pieces.as<Xyzz>());
     check_launch();
     ctx->prof_end(tok);
+    k_msm_bucket_fixup<<<grid_for(ctx, B, 128, 8), 128, 0, ctx->stream>>>(offsets.as<uint32_t>(), uint32_t(B),
+                                                                          pieces.as<Xyzz>(), buckets.as<Xyzz>());
+    check_launch();
     Scratch acc(ctx, sh.segments * sizeof(Xyzz)), run(ctx, sh.segments * sizeof(Xyzz));
     k_msm_segments<<<grid_for(ctx, sh.segments, 128, 16), 128, 0, ctx->stream>>>(
         buckets.as<Xyzz>(), sh.segments, sh.seg, acc.as<Xyzz>(), run.as<Xyzz>());

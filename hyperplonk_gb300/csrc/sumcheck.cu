@@ -106,6 +106,87 @@ __global__ void k_sumcheck_round(SumcheckDesc desc, FrPtrList src, FrMutPtrList 
     }
 }
 
+// Register-resident round for products of arity <= MAXM (every VP of the
+// prover: degree <= 5).  One pair per thread per iteration; the fold of all
+// factors is written to `dst` first, then each product re-reads its factors'
+// folded pair (an L2 hit: this thread just wrote it) and evaluates at
+// t = 0..m with running values in registers; each (product, t) value is
+// summed across the warp with shuffles and added into a per-warp shared slot.
+constexpr int kRoundThreads = 128;
+constexpr int kMaxSlotsV2 = 64;
+
+__device__ __forceinline__ Fr warp_sum(Fr v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        Fr o;
+#pragma unroll
+        for (int i = 0; i < 8; i++) o.v[i] = __shfl_down_sync(0xffffffffu, v.v[i], off);
+        v = v + o;
+    }
+    return v;
+}
+
+template <int MAXM>
+__global__ void __launch_bounds__(kRoundThreads) k_sumcheck_round_regs(SumcheckDesc desc, FrPtrList src,
+                                                                       FrMutPtrList dst, FrPtrList rd, bool fold,
+                                                                       Fr r, size_t pairs, Fr *partials) {
+    __shared__ Fr warp_slots[kRoundThreads / 32][kMaxSlotsV2];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int S = desc.slot_count, F = desc.factor_count;
+    for (int i = threadIdx.x; i < (kRoundThreads / 32) * S; i += blockDim.x) warp_slots[i / S][i % S] = Fr::zero();
+    __syncthreads();
+    for (size_t base = size_t(blockIdx.x) * kRoundThreads; base < pairs; base += size_t(gridDim.x) * kRoundThreads) {
+        const size_t b = base + threadIdx.x;
+        const bool active = b < pairs;
+        if (fold && active) {
+            for (int f = 0; f < F; f++) {
+                const Fr *s = src.p[f] + 4 * b;
+                Fr a0 = load_fr(s), a1 = load_fr(s + 1), a2 = load_fr(s + 2), a3 = load_fr(s + 3);
+                Fr *d = dst.p[f] + 2 * b;
+                store_fr(d, a0 + r * (a1 - a0));
+                store_fr(d + 1, a2 + r * (a3 - a2));
+            }
+        }
+        for (int p = 0; p < desc.product_count; p++) {
+            const int begin = desc.offsets[p], m = desc.offsets[p + 1] - begin, slot = desc.slot_base[p];
+            Fr e[MAXM], st[MAXM];
+            if (active) {
+#pragma unroll
+                for (int j = 0; j < MAXM; j++) {
+                    if (j < m) {
+                        const Fr *t = rd.p[desc.indices[begin + j]] + 2 * b;
+                        e[j] = load_fr(t);
+                        st[j] = load_fr(t + 1) - e[j];
+                    }
+                }
+            }
+            for (int k = 0; k <= m; k++) {
+                Fr v = Fr::zero();
+                if (active) {
+                    if (k > 0) {
+#pragma unroll
+                        for (int j = 0; j < MAXM; j++)
+                            if (j < m) e[j] = e[j] + st[j];
+                    }
+                    v = e[0];
+#pragma unroll
+                    for (int j = 1; j < MAXM; j++)
+                        if (j < m) v = v * e[j];
+                }
+                v = warp_sum(v);
+                if (lane == 0) warp_slots[warp][slot + k] = warp_slots[warp][slot + k] + v;
+            }
+        }
+    }
+    __syncthreads();
+    for (int s = threadIdx.x; s < S; s += blockDim.x) {
+        Fr a = warp_slots[0][s];
+#pragma unroll
+        for (int w = 1; w < kRoundThreads / 32; w++) a = a + warp_slots[w][s];
+        partials[size_t(blockIdx.x) * S + s] = a;
+    }
+}
+
 // One block: sum block partials per slot, extend each product to degree D by
 // forward differences, scale by its coefficient, accumulate, write canonical.
 __global__ void k_sumcheck_finalize(SumcheckDesc desc, const Fr *partials, int blocks,
@@ -296,19 +377,37 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_round(HpCudaContext *ct
                 src.p[f] = hp::state_table(s, src_which, f);
                 dst.p[f] = const_cast<Fr *>(hp::state_table(s, dst_which, f));
             }
-            size_t smem;
-            int T = hp::round_block_size(d, &smem);
-            if (smem > 48 * 1024)
-                check_cuda(cudaFuncSetAttribute(hp::k_sumcheck_round,
-                                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                int(smem)));
-            unsigned grid = hp::grid_for(ctx, pairs, unsigned(T), 2);
-            hp::Scratch partials(ctx, size_t(grid) * d.slot_count * sizeof(Fr));
-            hp::Scratch sums(ctx, d.slot_count * sizeof(Fr));
-            hp::Scratch outd(ctx, evaluation_count * sizeof(Fr));
-            hp::k_sumcheck_round<<<grid, T, smem, ctx->stream>>>(d, src, dst, fold, r, pairs,
-                                                                 partials.as<Fr>());
-            check_launch();
+            const bool regs = d.max_arity <= 8 && d.slot_count <= hp::kMaxSlotsV2;
+            unsigned grid;
+            hp::Scratch partials, sums(ctx, d.slot_count * sizeof(Fr)), outd(ctx, evaluation_count * sizeof(Fr));
+            int tok = ctx->prof_begin("sumcheck_round");
+            if (regs) {
+                hp::FrPtrList rd{};
+                for (int f = 0; f < d.factor_count; f++) rd.p[f] = fold ? dst.p[f] : src.p[f];
+                grid = hp::grid_for(ctx, pairs, hp::kRoundThreads, 8);
+                partials = hp::Scratch(ctx, size_t(grid) * d.slot_count * sizeof(Fr));
+                auto launch = [&](auto kernel) {
+                    kernel<<<grid, hp::kRoundThreads, 0, ctx->stream>>>(d, src, dst, rd, fold, r, pairs,
+                                                                        partials.as<Fr>());
+                };
+                if (d.max_arity <= 2) launch(hp::k_sumcheck_round_regs<2>);
+                else if (d.max_arity <= 4) launch(hp::k_sumcheck_round_regs<4>);
+                else if (d.max_arity <= 6) launch(hp::k_sumcheck_round_regs<6>);
+                else launch(hp::k_sumcheck_round_regs<8>);
+                check_launch();
+            } else {
+                size_t smem;
+                int T = hp::round_block_size(d, &smem);
+                if (smem > 48 * 1024)
+                    check_cuda(cudaFuncSetAttribute(hp::k_sumcheck_round,
+                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+                grid = hp::grid_for(ctx, pairs, unsigned(T), 2);
+                partials = hp::Scratch(ctx, size_t(grid) * d.slot_count * sizeof(Fr));
+                hp::k_sumcheck_round<<<grid, T, smem, ctx->stream>>>(d, src, dst, fold, r, pairs,
+                                                                     partials.as<Fr>());
+                check_launch();
+            }
+            ctx->prof_end(tok);
             hp::k_sumcheck_finalize<<<1, 256, 256 * sizeof(Fr), ctx->stream>>>(
                 d, partials.as<Fr>(), int(grid), static_cast<const Fr *>(s->coefs),
                 int(s->max_degree), sums.as<Fr>(), outd.as<Fr>());
