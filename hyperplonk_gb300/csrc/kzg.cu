@@ -50,8 +50,10 @@ static const MsmLayer &ready_layer(const HpCudaMultilinearKzgPreparedProverParam
 }
 
 // Download `total` XYZZ partials and finish each MSM into a packet.
-static void finish_msms(HpCudaContext *ctx, const Xyzz *dev, const std::vector<MsmShape> &shapes,
+static void finish_msms(HpCudaContext *ctx, const Xyzz *dev, const std::vector<const MsmLayer *> &layers,
                         uint8_t *out97) {
+    std::vector<MsmShape> shapes;
+    for (auto *l : layers) shapes.push_back(msm_shape(*l));
     size_t total = 0;
     for (auto &s : shapes) total += size_t(s.partials);
     std::vector<host::Xyzz64> hostp(std::max<size_t>(total, 1));
@@ -60,7 +62,7 @@ static void finish_msms(HpCudaContext *ctx, const Xyzz *dev, const std::vector<M
     ctx->sync();
     size_t off = 0;
     for (size_t i = 0; i < shapes.size(); i++) {
-        msm_finalize_host(shapes[i], hostp.data() + off, out97 + 97 * i);
+        msm_finalize_host(*layers[i], hostp.data() + off, out97 + 97 * i);
         off += size_t(shapes[i].partials);
     }
 }
@@ -127,7 +129,7 @@ extern "C" HpCudaStatus hp_cuda_v1_multilinear_kzg_commit(
         hp::MsmShape sh = hp::msm_shape(layer);
         hp::Scratch parts(ctx, size_t(sh.partials) * sizeof(hp::Xyzz));
         hp::msm_run(ctx, layer, scalars, parts.as<hp::Xyzz>());
-        hp::finish_msms(ctx, parts.as<hp::Xyzz>(), {sh}, out_commitment);
+        hp::finish_msms(ctx, parts.as<hp::Xyzz>(), {&layer}, out_commitment);
     });
 }
 
@@ -157,7 +159,7 @@ extern "C" HpCudaStatus hp_cuda_v1_multilinear_kzg_multi_commit(
             hp::msm_run(ctx, *layers[i], scalars[i], parts.as<hp::Xyzz>() + off);
             off += size_t(shapes[i].partials);
         }
-        hp::finish_msms(ctx, parts.as<hp::Xyzz>(), shapes, out_commitments);
+        hp::finish_msms(ctx, parts.as<hp::Xyzz>(), layers, out_commitments);
     });
 }
 
@@ -203,7 +205,7 @@ extern "C" HpCudaStatus hp_cuda_v1_multilinear_kzg_open(
             cur = next;
         }
         hp::download_canonical(ctx, cur, 1, out_evaluation);
-        hp::finish_msms(ctx, parts.as<hp::Xyzz>(), shapes, out_quotients);
+        hp::finish_msms(ctx, parts.as<hp::Xyzz>(), layers, out_quotients);
     });
 }
 
@@ -233,6 +235,6 @@ extern "C" HpCudaStatus hp_cuda_v1_msm(HpCudaContext *ctx, const uint8_t *bases,
         hp::MsmShape sh = hp::msm_shape(layer);
         hp::Scratch parts(ctx, size_t(sh.partials) * sizeof(hp::Xyzz));
         hp::msm_run(ctx, layer, s.as<Fr>(), parts.as<hp::Xyzz>());
-        hp::finish_msms(ctx, parts.as<hp::Xyzz>(), {sh}, out_point);
+        hp::finish_msms(ctx, parts.as<hp::Xyzz>(), {&layer}, out_point);
     });
 }

@@ -187,6 +187,33 @@ void xyzz_to_affine(HpCudaContext *ctx, const Xyzz *in, Affine *out, Fq *pre, si
     check_launch();
 }
 
+// d_i: 256 pseudo-random bits per index (SplitMix64 finaliser over (seed, i, k)),
+// top two bits cleared so d_i < 2^254 < r.
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+__global__ void k_msm_delta(Fr *out, size_t n, uint64_t seed) {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+        Fr d;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            uint64_t w = mix64(seed + 0x9e3779b97f4a7c15ull * (4 * uint64_t(i) + uint64_t(k) + 1));
+            d.v[2 * k] = uint32_t(w);
+            d.v[2 * k + 1] = uint32_t(w >> 32);
+        }
+        d.v[7] &= 0x3fffffffu;
+        store_fr(&out[i], d);
+    }
+}
+
+__global__ void k_msm_to_mont(Fr *data, size_t n) {
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+        store_fr(&data[i], to_mont(load_fr(&data[i])));
+}
+
 bool msm_prepare_layer(HpCudaContext *ctx, MsmLayer &layer, const uint8_t *packets, size_t n) {
     layer.n = n;
     layer.c = msm_window_bits(n);
@@ -211,12 +238,37 @@ bool msm_prepare_layer(HpCudaContext *ctx, MsmLayer &layer, const uint8_t *packe
         }
     }
     uint32_t flags = ctx->sync_flags();
-    return (flags & kFlagNonCanonical) == 0;
+    if (flags & kFlagNonCanonical) return false;
+    // randomiser d (canonical, < 2^254) and D = sum d_i P_i over this layer
+    layer.delta = static_cast<Fr *>(ctx->scratch(n * sizeof(Fr)));
+    k_msm_delta<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(layer.delta, n, uint64_t(n) * 0x9e3779b97f4a7c15ull);
+    check_launch();
+    {
+        Scratch dm(ctx, n * sizeof(Fr));
+        check_cuda(cudaMemcpyAsync(dm.ptr, layer.delta, n * sizeof(Fr), cudaMemcpyDeviceToDevice, ctx->stream));
+        k_msm_to_mont<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(dm.as<Fr>(), n);
+        check_launch();
+        MsmLayer plain = layer;
+        plain.delta = nullptr;
+        const MsmShape sh = msm_shape(plain);
+        Scratch parts(ctx, size_t(sh.partials) * sizeof(Xyzz));
+        msm_run(ctx, plain, dm.as<Fr>(), parts.as<Xyzz>());
+        std::vector<host::Xyzz64> hp_parts(size_t(sh.partials));
+        check_cuda(cudaMemcpyAsync(hp_parts.data(), parts.ptr, size_t(sh.partials) * sizeof(Xyzz),
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+        ctx->sync();
+        host::Xyzz64 d = msm_combine_host(sh, hp_parts.data());
+        d.y = host::fq_sub(host::Fq64{{0, 0, 0, 0, 0, 0}}, d.y);
+        layer.minus_d = d;
+    }
+    return true;
 }
 
 void msm_release_layer(HpCudaContext *ctx, MsmLayer &layer) {
     if (layer.bases) ctx->scratch_free(layer.bases);
+    if (layer.delta) ctx->scratch_free(layer.delta);
     layer.bases = nullptr;
+    layer.delta = nullptr;
 }
 
 // ---------------------------------------------------------------------------
@@ -250,10 +302,18 @@ __device__ __forceinline__ void for_each_digit(const Fr &canon, int c, int windo
     }
 }
 
-__global__ void k_msm_histogram(const Fr *scalars, size_t n, int c, int windows, uint32_t *counts) {
+// canonical scalar i, shifted by the layer's randomiser when present
+__device__ __forceinline__ Fr msm_scalar(const Fr *scalars, const Fr *delta, size_t i) {
+    Fr s = from_mont(load_fr(&scalars[i]));
+    if (delta) s = s + load_fr(&delta[i]);  // both < r: one conditional subtraction
+    return s;
+}
+
+__global__ void k_msm_histogram(const Fr *scalars, const Fr *delta, size_t n, int c, int windows,
+                                uint32_t *counts) {
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
          i += size_t(gridDim.x) * blockDim.x) {
-        Fr s = from_mont(load_fr(&scalars[i]));
+        Fr s = msm_scalar(scalars, delta, i);
         for_each_digit(s, c, windows, [&](int, uint32_t mag, bool) { atomicAdd(&counts[mag - 1], 1u); });
     }
 }
@@ -285,11 +345,11 @@ __global__ void __launch_bounds__(1024) k_msm_scan(const uint32_t *counts, size_
     if (t == 1023) offsets[m] = part[1023];
 }
 
-__global__ void k_msm_scatter(const Fr *scalars, size_t n, int c, int windows, uint32_t *cursor,
-                              uint32_t *records) {
+__global__ void k_msm_scatter(const Fr *scalars, const Fr *delta, size_t n, int c, int windows,
+                              uint32_t *cursor, uint32_t *records) {
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
          i += size_t(gridDim.x) * blockDim.x) {
-        Fr s = from_mont(load_fr(&scalars[i]));
+        Fr s = msm_scalar(scalars, delta, i);
         for_each_digit(s, c, windows, [&](int w, uint32_t mag, bool neg) {
             uint32_t pos = atomicAdd(&cursor[mag - 1], 1u);
             records[pos] = uint32_t(size_t(w) * n + i) | (neg ? 0x80000000u : 0u);
@@ -452,14 +512,15 @@ void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz 
     Scratch recs(ctx, records * 4), buckets(ctx, B * sizeof(Xyzz));
     int whole = ctx->prof_begin("msm");
     check_cuda(cudaMemsetAsync(counts.ptr, 0, (B + 1) * 4, ctx->stream));
-    k_msm_histogram<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(scalars, n, layer.c, layer.windows,
-                                                                    counts.as<uint32_t>());
+    k_msm_histogram<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(scalars, layer.delta, n, layer.c,
+                                                                    layer.windows, counts.as<uint32_t>());
     check_launch();
     k_msm_scan<<<1, 1024, 0, ctx->stream>>>(counts.as<uint32_t>(), B, offsets.as<uint32_t>(),
                                             cursor.as<uint32_t>());
     check_launch();
-    k_msm_scatter<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(scalars, n, layer.c, layer.windows,
-                                                                  cursor.as<uint32_t>(), recs.as<uint32_t>());
+    k_msm_scatter<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(scalars, layer.delta, n, layer.c,
+                                                                  layer.windows, cursor.as<uint32_t>(),
+                                                                  recs.as<uint32_t>());
     check_launch();
     const size_t record_chunks = (records + kChunkRecords - 1) / kChunkRecords;
     Scratch pieces(ctx, std::max<size_t>(2 * record_chunks, 1) * sizeof(Xyzz));
@@ -493,7 +554,7 @@ void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz 
     ctx->prof_end(whole);
 }
 
-void msm_finalize_host(const MsmShape &shape, const host::Xyzz64 *partials, uint8_t *out97) {
+host::Xyzz64 msm_combine_host(const MsmShape &shape, const host::Xyzz64 *partials) {
     // result = A + seg * sum_k 2^k T_k, A = partials[bits], T_k = partials[k]
     host::Xyzz64 h = host::xyzz_inf();
     for (int k = shape.seg_bits - 1; k >= 0; k--) {
@@ -501,7 +562,12 @@ void msm_finalize_host(const MsmShape &shape, const host::Xyzz64 *partials, uint
         h = host::xyzz_add(h, partials[k]);
     }
     for (size_t s = shape.seg; s > 1; s >>= 1) h = host::xyzz_double(h);
-    host::Xyzz64 r = host::xyzz_add(partials[shape.seg_bits], h);
+    return host::xyzz_add(partials[shape.seg_bits], h);
+}
+
+void msm_finalize_host(const MsmLayer &layer, const host::Xyzz64 *partials, uint8_t *out97) {
+    host::Xyzz64 r = msm_combine_host(msm_shape(layer), partials);
+    if (layer.delta) r = host::xyzz_add(r, layer.minus_d);
     host::xyzz_to_packet(r, out97);
 }
 

@@ -14,11 +14,19 @@ namespace hp {
 // Montgomery form at bases[w * n + i], so every window of a scalar's
 // signed-digit expansion indexes the same 2^(c-1) buckets and no per-window
 // combination is needed.  Built once by msm_prepare_layer().
+//
+// Scalar randomisation: the MSM is computed as sum (s_i + d_i) P_i - D with a
+// fixed pseudo-random d per layer and D = sum d_i P_i precomputed at prepare
+// time.  The value is the same group element; the bucket loads no longer
+// depend on the scalars' distribution (an all-ones table -- frac and prod of
+// an identity permutation -- would otherwise send every record to bucket 1).
 struct MsmLayer {
     size_t n = 0;
     int c = 0;        // window bits
     int windows = 0;  // ceil(256 / c)
     Affine *bases = nullptr;  // windows * n points (device, context scratch)
+    Fr *delta = nullptr;      // n canonical Fr < 2^254 (device), or null
+    host::Xyzz64 minus_d{};   // -sum d_i P_i, added by the host finish
 };
 
 // Window width minimising ceil(256/c) * 10 n + 28 * 2^(c-1) for c in [4, 20]
@@ -50,7 +58,10 @@ void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz 
 // Batch XYZZ -> affine (one field inversion per 512 points); pre: n Fq scratch.
 void xyzz_to_affine(HpCudaContext *ctx, const Xyzz *in, Affine *out, Fq *pre, size_t n);
 
-// Host: combine the partials of one MSM into a 97-byte G1 packet.
-void msm_finalize_host(const MsmShape &shape, const host::Xyzz64 *partials, uint8_t *out97);
+// Host: combine the partials of one MSM into a point.
+host::Xyzz64 msm_combine_host(const MsmShape &shape, const host::Xyzz64 *partials);
+// Host: combine the partials of one MSM over `layer` (removing its
+// randomisation offset) into a 97-byte G1 packet.
+void msm_finalize_host(const MsmLayer &layer, const host::Xyzz64 *partials, uint8_t *out97);
 
 }  // namespace hp
