@@ -320,8 +320,10 @@ def measure(s: Session, pg, steps: int, value_fn, e2e_fn):
     s.torch.cuda.synchronize()
     clocks.start()
     l0 = s.launches()
+    s.torch.cuda.nvtx.range_push("timed_value")  # ncu --nvtx --nvtx-include "timed_value/" selects this loop
     per = s.timed(value_fn, steps)
     s.torch.cuda.synchronize()
+    s.torch.cuda.nvtx.range_pop()
     l1 = s.launches()
     barrier(pg)
     clk = clocks.stop()

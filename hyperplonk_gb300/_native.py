@@ -50,6 +50,8 @@ SIGNATURES: dict[str, list] = {
     "hp_cuda_v1_sumcheck_prover_state_destroy": [c_voidp, c_voidp],
     "hp_cuda_v1_sumcheck_prover_state_final_evaluations": [c_voidp, c_voidp, c_u8p, c_u8p, c_size],
     "hp_cuda_v1_msm": [c_voidp, c_u8p, c_u8p, c_size, c_u8p],
+    "hp_cuda_v1_batch_msm": [c_voidp, c_voidp, c_size, c_voidpp, c_sizep, c_size, c_u8p],
+    "hp_cuda_v1_batch_sumcheck_round": [c_voidp, c_voidpp, c_voidpp, c_voidpp, c_sizep, c_size],
     "hp_cuda_v1_mle_evaluate_noalloc": [c_voidp, c_size, c_u8p, c_u8p, c_voidp],
     "hp_cuda_v1_context_profile": [c_voidp, ctypes.c_int32],
     "hp_cuda_v1_context_profile_read": [c_voidp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),

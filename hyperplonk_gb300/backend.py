@@ -408,6 +408,42 @@ class CudaBackend:
         raw = bytes(out)
         return [decode_fr(raw[32 * i:32 * i + 32]) for i in range(n)]
 
+    # ---- batched execution (no counterpart in the reference traits) ----
+    def batch_msm(self, prover_param: CudaPreparedProverParam, layer_index: int, scalars: Sequence[CudaMle]):
+        """MSM i = sum_j scalars[i][j] * (layer `layer_index` base j) over the
+        first 2^num_vars bases; all MSMs overlap on the device."""
+        if not scalars:
+            return []
+        for m in scalars:
+            self._check_mle(m)
+        nvs = (ctypes.c_size_t * len(scalars))(*[m.num_vars for m in scalars])
+        out = (ctypes.c_uint8 * (97 * len(scalars)))()
+        check_status(self.lib.hp_cuda_v1_batch_msm(self.ctx.raw, prover_param.raw, layer_index, _addr_array(scalars),
+                                                   nvs, len(scalars), out), "batch_msm")
+        raw = bytes(out)
+        return [decode_g1(raw[97 * i:97 * i + 97]) for i in range(len(scalars))]
+
+    def batch_prove_round(self, states: Sequence[CudaSumCheckProverState], challenges: Sequence[Optional[int]]):
+        """One round of every state (each with its own challenge or None),
+        overlapped on the device, one synchronisation."""
+        k = len(states)
+        if k == 0:
+            return []
+        sp = (ctypes.c_void_p * k)(*[s.raw.value for s in states])
+        keep = [encode_fr(c) if c is not None else None for c in challenges]
+        cp = (ctypes.c_void_p * k)(*[ctypes.cast(ctypes.c_char_p(b), ctypes.c_void_p).value if b else None
+                                     for b in keep])
+        outs = [(ctypes.c_uint8 * (32 * s.round_evaluation_count))() for s in states]
+        op = (ctypes.c_void_p * k)(*[ctypes.addressof(o) for o in outs])
+        counts = (ctypes.c_size_t * k)(*[s.round_evaluation_count for s in states])
+        check_status(self.lib.hp_cuda_v1_batch_sumcheck_round(self.ctx.raw, sp, cp, op, counts, k),
+                     "batch_sumcheck_round")
+        res = []
+        for o, s in zip(outs, states):
+            raw = bytes(o)
+            res.append([decode_fr(raw[32 * i:32 * i + 32]) for i in range(s.round_evaluation_count)])
+        return res
+
     def final_evaluations(self, state: CudaSumCheckProverState, challenge: int) -> list[int]:
         """Every distinct factor fixed at the full challenge point (after the
         last round), in factor order."""

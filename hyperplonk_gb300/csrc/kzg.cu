@@ -12,6 +12,7 @@
 //    the final scalar come back.
 #include <algorithm>
 #include <cstring>
+#include <map>
 #include <vector>
 
 #include "host_ec.h"
@@ -30,6 +31,9 @@ struct HpCudaMultilinearKzgPreparedProverParam {
     size_t num_vars = 0;
     std::vector<hp::MsmLayer> layers;
     std::vector<bool> uploaded;
+    // prefix layers for batched MSMs over the first n bases of layer k,
+    // keyed by (k, n), built on first use
+    std::map<std::pair<size_t, size_t>, hp::MsmLayer> prefixes;
 };
 
 namespace hp {
@@ -114,6 +118,7 @@ extern "C" HpCudaStatus hp_cuda_v1_multilinear_kzg_params_destroy(
         hp::require_ctx(ctx);
         require(params != nullptr);
         for (auto &l : params->layers) hp::msm_release_layer(ctx, l);
+        for (auto &kv : params->prefixes) hp::msm_release_layer(ctx, kv.second);
         delete params;
     });
 }
@@ -155,10 +160,14 @@ extern "C" HpCudaStatus hp_cuda_v1_multilinear_kzg_multi_commit(
         }
         hp::Scratch parts(ctx, total * sizeof(hp::Xyzz));
         size_t off = 0;
+        // independent MSMs overlap on the context's worker streams
+        const int k = int(std::min<size_t>(count, HpCudaContext::kWorkers));
+        ctx->fork(k);
         for (size_t i = 0; i < count; i++) {
-            hp::msm_run(ctx, *layers[i], scalars[i], parts.as<hp::Xyzz>() + off);
+            hp::msm_run(ctx, *layers[i], scalars[i], parts.as<hp::Xyzz>() + off, ctx->workers[i % size_t(k)]);
             off += size_t(shapes[i].partials);
         }
+        ctx->join(k);
         hp::finish_msms(ctx, parts.as<hp::Xyzz>(), layers, out_commitments);
     });
 }
@@ -190,20 +199,33 @@ extern "C" HpCudaStatus hp_cuda_v1_multilinear_kzg_open(
         hp::Scratch parts(ctx, total * sizeof(hp::Xyzz));
         hp::Scratch fa(ctx, hp::table_len(nv - 1) * sizeof(Fr));
         hp::Scratch fb(ctx, hp::table_len(nv >= 2 ? nv - 2 : 0) * sizeof(Fr));
-        hp::Scratch q(ctx, hp::table_len(nv - 1) * sizeof(Fr));
+        // all quotients first (q_i at offset 2^nv - 2^(nv-i)), then their MSMs
+        // overlap on the worker streams: the late rounds' MSMs are tiny and
+        // latency bound one at a time
+        hp::Scratch q(ctx, hp::table_len(nv) * sizeof(Fr));
         const Fr *cur = f;
         Fr *bufs[2] = {fa.as<Fr>(), fb.as<Fr>()};
-        size_t off = 0;
+        std::vector<size_t> q_off(nv);
+        size_t qo = 0;
         for (size_t i = 0; i < nv; i++) {
             size_t half = hp::table_len(nv - 1 - i);
             Fr *next = bufs[i & 1];
-            hp::k_open_fold<<<hp::grid_for(ctx, half, 256), 256, 0, ctx->stream>>>(cur, next, q.as<Fr>(), half,
-                                                                                   z[i]);
+            q_off[i] = qo;
+            hp::k_open_fold<<<hp::grid_for(ctx, half, 256), 256, 0, ctx->stream>>>(cur, next, q.as<Fr>() + qo,
+                                                                                   half, z[i]);
             check_launch();
-            hp::msm_run(ctx, *layers[i], q.as<Fr>(), parts.as<hp::Xyzz>() + off);
-            off += size_t(shapes[i].partials);
+            qo += half;
             cur = next;
         }
+        const int k = int(std::min<size_t>(nv, HpCudaContext::kWorkers));
+        ctx->fork(k);
+        size_t off = 0;
+        for (size_t i = 0; i < nv; i++) {
+            hp::msm_run(ctx, *layers[i], q.as<Fr>() + q_off[i], parts.as<hp::Xyzz>() + off,
+                        ctx->workers[i % size_t(k)]);
+            off += size_t(shapes[i].partials);
+        }
+        ctx->join(k);
         hp::download_canonical(ctx, cur, 1, out_evaluation);
         hp::finish_msms(ctx, parts.as<hp::Xyzz>(), layers, out_quotients);
     });
@@ -236,5 +258,62 @@ extern "C" HpCudaStatus hp_cuda_v1_msm(HpCudaContext *ctx, const uint8_t *bases,
         hp::Scratch parts(ctx, size_t(sh.partials) * sizeof(hp::Xyzz));
         hp::msm_run(ctx, layer, s.as<Fr>(), parts.as<hp::Xyzz>());
         hp::finish_msms(ctx, parts.as<hp::Xyzz>(), {&layer}, out_point);
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_batch_msm(HpCudaContext *ctx, HpCudaMultilinearKzgPreparedProverParam *params,
+                                             size_t layer_index, const HpCudaDeviceAddress *scalars,
+                                             const size_t *num_vars, size_t count, uint8_t *out_points) {
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(params != nullptr);
+        if (count == 0) return;
+        require(scalars != nullptr && num_vars != nullptr && out_points != nullptr);
+        const hp::MsmLayer &base = hp::ready_layer(params, layer_index);
+        std::vector<const Fr *> sc(count);
+        std::vector<const hp::MsmLayer *> layers(count);
+        size_t total = 0;
+        for (size_t i = 0; i < count; i++) {
+            const size_t n = hp::table_len(num_vars[i]);
+            require(num_vars[i] <= hp::kMaxNumVars && n <= base.n);
+            sc[i] = hp::mle_ptr(ctx, scalars[i], num_vars[i]);
+            if (n == base.n) {
+                layers[i] = &base;
+            } else {
+                auto key = std::make_pair(layer_index, n);
+                auto it = params->prefixes.find(key);
+                if (it == params->prefixes.end()) {
+                    hp::MsmLayer pl;
+                    try {
+                        hp::msm_prepare_prefix(ctx, pl, base, n);
+                    } catch (...) {
+                        hp::msm_release_layer(ctx, pl);
+                        throw;
+                    }
+                    it = params->prefixes.emplace(key, pl).first;
+                }
+                layers[i] = &it->second;
+            }
+            total += size_t(hp::msm_shape(*layers[i]).partials);
+        }
+        hp::Scratch parts(ctx, total * sizeof(hp::Xyzz));
+        // largest first, round-robin over the worker streams
+        std::vector<size_t> order(count);
+        for (size_t i = 0; i < count; i++) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return num_vars[a] > num_vars[b]; });
+        std::vector<size_t> part_off(count);
+        size_t off = 0;
+        for (size_t i = 0; i < count; i++) {
+            part_off[i] = off;
+            off += size_t(hp::msm_shape(*layers[i]).partials);
+        }
+        const int k = int(std::min<size_t>(count, HpCudaContext::kWorkers));
+        ctx->fork(k);
+        for (size_t j = 0; j < count; j++) {
+            const size_t i = order[j];
+            hp::msm_run(ctx, *layers[i], sc[i], parts.as<hp::Xyzz>() + part_off[i], ctx->workers[j % size_t(k)]);
+        }
+        ctx->join(k);
+        hp::finish_msms(ctx, parts.as<hp::Xyzz>(), layers, out_points);
     });
 }

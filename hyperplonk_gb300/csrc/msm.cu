@@ -214,17 +214,10 @@ __global__ void k_msm_to_mont(Fr *data, size_t n) {
         store_fr(&data[i], to_mont(load_fr(&data[i])));
 }
 
-bool msm_prepare_layer(HpCudaContext *ctx, MsmLayer &layer, const uint8_t *packets, size_t n) {
-    layer.n = n;
-    layer.c = msm_window_bits(n);
-    layer.windows = msm_windows(layer.c);
-    layer.bases = static_cast<Affine *>(ctx->scratch(size_t(layer.windows) * n * sizeof(Affine)));
-    Scratch raw(ctx, n * 97);
-    check_cuda(cudaMemcpyAsync(raw.ptr, packets, n * 97, cudaMemcpyHostToDevice, ctx->stream));
-    ctx->clear_flags();
-    k_unpack_packets<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(raw.as<uint8_t>(), n, layer.bases,
-                                                                     ctx->d_flags);
-    check_launch();
+// Windows 1..W-1 from window 0 (already in layer.bases), then the randomiser
+// d and D = sum d_i P_i.
+static void msm_finish_layer(HpCudaContext *ctx, MsmLayer &layer) {
+    const size_t n = layer.n;
     if (layer.windows > 1) {
         Scratch tmp(ctx, n * sizeof(Xyzz)), pre(ctx, n * sizeof(Fq));
         size_t per_block = size_t(kNormBlock) * kNormChunk;
@@ -237,31 +230,53 @@ bool msm_prepare_layer(HpCudaContext *ctx, MsmLayer &layer, const uint8_t *packe
             check_launch();
         }
     }
-    uint32_t flags = ctx->sync_flags();
-    if (flags & kFlagNonCanonical) return false;
-    // randomiser d (canonical, < 2^254) and D = sum d_i P_i over this layer
     layer.delta = static_cast<Fr *>(ctx->scratch(n * sizeof(Fr)));
     k_msm_delta<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(layer.delta, n, uint64_t(n) * 0x9e3779b97f4a7c15ull);
     check_launch();
-    {
-        Scratch dm(ctx, n * sizeof(Fr));
-        check_cuda(cudaMemcpyAsync(dm.ptr, layer.delta, n * sizeof(Fr), cudaMemcpyDeviceToDevice, ctx->stream));
-        k_msm_to_mont<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(dm.as<Fr>(), n);
-        check_launch();
-        MsmLayer plain = layer;
-        plain.delta = nullptr;
-        const MsmShape sh = msm_shape(plain);
-        Scratch parts(ctx, size_t(sh.partials) * sizeof(Xyzz));
-        msm_run(ctx, plain, dm.as<Fr>(), parts.as<Xyzz>());
-        std::vector<host::Xyzz64> hp_parts(size_t(sh.partials));
-        check_cuda(cudaMemcpyAsync(hp_parts.data(), parts.ptr, size_t(sh.partials) * sizeof(Xyzz),
-                                   cudaMemcpyDeviceToHost, ctx->stream));
-        ctx->sync();
-        host::Xyzz64 d = msm_combine_host(sh, hp_parts.data());
-        d.y = host::fq_sub(host::Fq64{{0, 0, 0, 0, 0, 0}}, d.y);
-        layer.minus_d = d;
-    }
+    Scratch dm(ctx, n * sizeof(Fr));
+    check_cuda(cudaMemcpyAsync(dm.ptr, layer.delta, n * sizeof(Fr), cudaMemcpyDeviceToDevice, ctx->stream));
+    k_msm_to_mont<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(dm.as<Fr>(), n);
+    check_launch();
+    MsmLayer plain = layer;
+    plain.delta = nullptr;
+    const MsmShape sh = msm_shape(plain);
+    Scratch parts(ctx, size_t(sh.partials) * sizeof(Xyzz));
+    msm_run(ctx, plain, dm.as<Fr>(), parts.as<Xyzz>());
+    std::vector<host::Xyzz64> hp_parts(size_t(sh.partials));
+    check_cuda(cudaMemcpyAsync(hp_parts.data(), parts.ptr, size_t(sh.partials) * sizeof(Xyzz),
+                               cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    host::Xyzz64 d = msm_combine_host(sh, hp_parts.data());
+    d.y = host::fq_sub(host::Fq64{{0, 0, 0, 0, 0, 0}}, d.y);
+    layer.minus_d = d;
+}
+
+bool msm_prepare_layer(HpCudaContext *ctx, MsmLayer &layer, const uint8_t *packets, size_t n) {
+    layer.n = n;
+    layer.c = msm_window_bits(n);
+    layer.windows = msm_windows(layer.c);
+    layer.bases = static_cast<Affine *>(ctx->scratch(size_t(layer.windows) * n * sizeof(Affine)));
+    Scratch raw(ctx, n * 97);
+    check_cuda(cudaMemcpyAsync(raw.ptr, packets, n * 97, cudaMemcpyHostToDevice, ctx->stream));
+    ctx->clear_flags();
+    k_unpack_packets<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(raw.as<uint8_t>(), n, layer.bases,
+                                                                     ctx->d_flags);
+    check_launch();
+    uint32_t flags = ctx->sync_flags();
+    if (flags & kFlagNonCanonical) return false;
+    msm_finish_layer(ctx, layer);
     return true;
+}
+
+void msm_prepare_prefix(HpCudaContext *ctx, MsmLayer &prefix, const MsmLayer &source, size_t n) {
+    require(n >= 1 && n <= source.n);
+    prefix.n = n;
+    prefix.c = msm_window_bits(n);
+    prefix.windows = msm_windows(prefix.c);
+    prefix.bases = static_cast<Affine *>(ctx->scratch(size_t(prefix.windows) * n * sizeof(Affine)));
+    check_cuda(cudaMemcpyAsync(prefix.bases, source.bases, n * sizeof(Affine), cudaMemcpyDeviceToDevice,
+                               ctx->stream));
+    msm_finish_layer(ctx, prefix);
 }
 
 void msm_release_layer(HpCudaContext *ctx, MsmLayer &layer) {
@@ -345,14 +360,14 @@ __global__ void __launch_bounds__(1024) k_msm_scan(const uint32_t *counts, size_
     if (t == 1023) offsets[m] = part[1023];
 }
 
-__global__ void k_msm_scatter(const Fr *scalars, const Fr *delta, size_t n, int c, int windows,
+__global__ void k_msm_scatter(const Fr *scalars, const Fr *delta, size_t n, size_t stride, int c, int windows,
                               uint32_t *cursor, uint32_t *records) {
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
          i += size_t(gridDim.x) * blockDim.x) {
         Fr s = msm_scalar(scalars, delta, i);
         for_each_digit(s, c, windows, [&](int w, uint32_t mag, bool neg) {
             uint32_t pos = atomicAdd(&cursor[mag - 1], 1u);
-            records[pos] = uint32_t(size_t(w) * n + i) | (neg ? 0x80000000u : 0u);
+            records[pos] = uint32_t(size_t(w) * stride + i) | (neg ? 0x80000000u : 0u);
         });
     }
 }
@@ -503,55 +518,56 @@ __global__ void k_msm_rows(const Xyzz *partial, int cols, Xyzz *out) {
     if (t == 0) store_xyzz(&out[y], sm[0]);
 }
 
-void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz *out_partials) {
-    const size_t n = layer.n;
+void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz *out_partials,
+             cudaStream_t stream, size_t count) {
+    const cudaStream_t st = stream ? stream : ctx->stream;
+    const size_t n = count ? count : layer.n;  // a prefix of the layer's bases
     const MsmShape sh = msm_shape(layer);
     const size_t B = sh.buckets;
     const size_t records = size_t(layer.windows) * n;
-    Scratch counts(ctx, (B + 1) * 4), offsets(ctx, (B + 1) * 4), cursor(ctx, B * 4);
-    Scratch recs(ctx, records * 4), buckets(ctx, B * sizeof(Xyzz));
-    int whole = ctx->prof_begin("msm");
-    check_cuda(cudaMemsetAsync(counts.ptr, 0, (B + 1) * 4, ctx->stream));
-    k_msm_histogram<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(scalars, layer.delta, n, layer.c,
-                                                                    layer.windows, counts.as<uint32_t>());
+    Scratch counts(ctx, (B + 1) * 4, st), offsets(ctx, (B + 1) * 4, st), cursor(ctx, B * 4, st);
+    Scratch recs(ctx, records * 4, st), buckets(ctx, B * sizeof(Xyzz), st);
+    int whole = ctx->prof_begin("msm", st);
+    check_cuda(cudaMemsetAsync(counts.ptr, 0, (B + 1) * 4, st));
+    k_msm_histogram<<<grid_for(ctx, n, 256), 256, 0, st>>>(scalars, layer.delta, n, layer.c, layer.windows,
+                                                          counts.as<uint32_t>());
     check_launch();
-    k_msm_scan<<<1, 1024, 0, ctx->stream>>>(counts.as<uint32_t>(), B, offsets.as<uint32_t>(),
-                                            cursor.as<uint32_t>());
+    k_msm_scan<<<1, 1024, 0, st>>>(counts.as<uint32_t>(), B, offsets.as<uint32_t>(), cursor.as<uint32_t>());
     check_launch();
-    k_msm_scatter<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(scalars, layer.delta, n, layer.c,
-                                                                  layer.windows, cursor.as<uint32_t>(),
-                                                                  recs.as<uint32_t>());
+    k_msm_scatter<<<grid_for(ctx, n, 256), 256, 0, st>>>(scalars, layer.delta, n, layer.n, layer.c, layer.windows,
+                                                        cursor.as<uint32_t>(), recs.as<uint32_t>());
     check_launch();
     const size_t record_chunks = (records + kChunkRecords - 1) / kChunkRecords;
-    Scratch pieces(ctx, std::max<size_t>(2 * record_chunks, 1) * sizeof(Xyzz));
-    int tok = ctx->prof_begin("msm_accumulate");
-    k_msm_accumulate<<<grid_for(ctx, record_chunks, 128, 16), 128, 0, ctx->stream>>>(
+    Scratch pieces(ctx, std::max<size_t>(2 * record_chunks, 1) * sizeof(Xyzz), st);
+    int tok = ctx->prof_begin("msm_accumulate", st);
+    k_msm_accumulate<<<grid_for(ctx, record_chunks, 128, 16), 128, 0, st>>>(
         layer.bases, offsets.as<uint32_t>(), recs.as<uint32_t>(), uint32_t(B), buckets.as<Xyzz>(),
         pieces.as<Xyzz>());
     check_launch();
-    ctx->prof_end(tok);
-    k_msm_bucket_fixup<<<grid_for(ctx, B, 128, 8), 128, 0, ctx->stream>>>(offsets.as<uint32_t>(), uint32_t(B),
-                                                                          pieces.as<Xyzz>(), buckets.as<Xyzz>());
+    ctx->prof_end(tok, st);
+    k_msm_bucket_fixup<<<grid_for(ctx, B, 128, 8), 128, 0, st>>>(offsets.as<uint32_t>(), uint32_t(B),
+                                                                pieces.as<Xyzz>(), buckets.as<Xyzz>());
     check_launch();
-    Scratch acc(ctx, sh.segments * sizeof(Xyzz)), run(ctx, sh.segments * sizeof(Xyzz));
-    k_msm_segments<<<grid_for(ctx, sh.segments, 128, 16), 128, 0, ctx->stream>>>(
-        buckets.as<Xyzz>(), sh.segments, sh.seg, acc.as<Xyzz>(), run.as<Xyzz>());
+    Scratch acc(ctx, sh.segments * sizeof(Xyzz), st), run(ctx, sh.segments * sizeof(Xyzz), st);
+    k_msm_segments<<<grid_for(ctx, sh.segments, 128, 16), 128, 0, st>>>(buckets.as<Xyzz>(), sh.segments, sh.seg,
+                                                                       acc.as<Xyzz>(), run.as<Xyzz>());
     check_launch();
     const int chunks = int((sh.segments + kSubsetPerBlock - 1) / kSubsetPerBlock);
     if (chunks == 1) {
-        k_msm_subsets<<<dim3(1, sh.partials), kSubsetThreads, 0, ctx->stream>>>(
-            run.as<Xyzz>(), acc.as<Xyzz>(), sh.segments, sh.seg_bits, 1, out_partials);
+        k_msm_subsets<<<dim3(1, sh.partials), kSubsetThreads, 0, st>>>(run.as<Xyzz>(), acc.as<Xyzz>(), sh.segments,
+                                                                       sh.seg_bits, 1, out_partials);
         check_launch();
     } else {
-        Scratch partial(ctx, size_t(chunks) * sh.partials * sizeof(Xyzz));
-        k_msm_subsets<<<dim3(chunks, sh.partials), kSubsetThreads, 0, ctx->stream>>>(
-            run.as<Xyzz>(), acc.as<Xyzz>(), sh.segments, sh.seg_bits, chunks, partial.as<Xyzz>());
-        check_launch();
         if (chunks > 64) fail(HP_CUDA_STATUS_NOT_IMPLEMENTED);
-        k_msm_rows<<<sh.partials, 64, 0, ctx->stream>>>(partial.as<Xyzz>(), chunks, out_partials);
+        Scratch partial(ctx, size_t(chunks) * sh.partials * sizeof(Xyzz), st);
+        k_msm_subsets<<<dim3(chunks, sh.partials), kSubsetThreads, 0, st>>>(run.as<Xyzz>(), acc.as<Xyzz>(),
+                                                                            sh.segments, sh.seg_bits, chunks,
+                                                                            partial.as<Xyzz>());
+        check_launch();
+        k_msm_rows<<<sh.partials, 64, 0, st>>>(partial.as<Xyzz>(), chunks, out_partials);
         check_launch();
     }
-    ctx->prof_end(whole);
+    ctx->prof_end(whole, st);
 }
 
 host::Xyzz64 msm_combine_host(const MsmShape &shape, const host::Xyzz64 *partials) {

@@ -49,11 +49,16 @@ MsmShape msm_shape(const MsmLayer &layer);
 // Returns false if a packet is malformed (bad tag / non-canonical coordinate).
 bool msm_prepare_layer(HpCudaContext *ctx, MsmLayer &layer, const uint8_t *packets, size_t n);
 void msm_release_layer(HpCudaContext *ctx, MsmLayer &layer);
+// A layer over the first n bases of `source` (its own window width, windows
+// and randomiser), built from source's device-resident window 0.
+void msm_prepare_prefix(HpCudaContext *ctx, MsmLayer &prefix, const MsmLayer &source, size_t n);
 
-// Enqueue one MSM of the layer's n bases with n Montgomery scalars; writes
-// msm_shape(layer).partials XYZZ values to out_partials (device).  All work
-// is on the context stream; no synchronisation.
-void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz *out_partials);
+// Enqueue one MSM of the first `count` bases of the layer (all n when 0) with
+// `count` Montgomery scalars; writes msm_shape(layer).partials XYZZ values to
+// out_partials (device).  All work, scratch included, is ordered on `stream`
+// (the context stream when null); no synchronisation.
+void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz *out_partials,
+             cudaStream_t stream = nullptr, size_t count = 0);
 
 // Batch XYZZ -> affine (one field inversion per 512 points); pre: n Fq scratch.
 void xyzz_to_affine(HpCudaContext *ctx, const Xyzz *in, Affine *out, Fq *pre, size_t n);

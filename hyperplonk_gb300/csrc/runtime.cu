@@ -23,14 +23,33 @@ void *HpCudaContext::alloc(size_t bytes) {
     return p;
 }
 
-void *HpCudaContext::scratch(size_t bytes) {
+void *HpCudaContext::scratch(size_t bytes, cudaStream_t s) {
     void *p = nullptr;
-    check_cuda(cudaMallocFromPoolAsync(&p, bytes ? bytes : 16, pool, stream));
+    check_cuda(cudaMallocFromPoolAsync(&p, bytes ? bytes : 16, pool, s ? s : stream));
     return p;
 }
 
-void HpCudaContext::scratch_free(void *p) {
-    if (p) cudaFreeAsync(p, stream);
+void HpCudaContext::scratch_free(void *p, cudaStream_t s) {
+    if (p) cudaFreeAsync(p, s ? s : stream);
+}
+
+void HpCudaContext::fork(int k) {
+    if (k > kWorkers) k = kWorkers;
+    if (!fork_event) check_cuda(cudaEventCreateWithFlags(&fork_event, cudaEventDisableTiming));
+    check_cuda(cudaEventRecord(fork_event, stream));
+    for (int i = 0; i < k; i++) {
+        if (!workers[i]) check_cuda(cudaStreamCreateWithFlags(&workers[i], cudaStreamNonBlocking));
+        if (!join_events[i]) check_cuda(cudaEventCreateWithFlags(&join_events[i], cudaEventDisableTiming));
+        check_cuda(cudaStreamWaitEvent(workers[i], fork_event, 0));
+    }
+}
+
+void HpCudaContext::join(int k) {
+    if (k > kWorkers) k = kWorkers;
+    for (int i = 0; i < k; i++) {
+        check_cuda(cudaEventRecord(join_events[i], workers[i]));
+        check_cuda(cudaStreamWaitEvent(stream, join_events[i], 0));
+    }
 }
 
 void HpCudaContext::ref(void *p) {
@@ -71,17 +90,17 @@ cudaEvent_t HpCudaContext::take_event() {
     return e;
 }
 
-int HpCudaContext::prof_begin(const char *name) {
+int HpCudaContext::prof_begin(const char *name, cudaStream_t s) {
     if (!profiling) return -1;
     Pending p{name, take_event(), take_event()};
-    check_cuda(cudaEventRecord(p.start, stream));
+    check_cuda(cudaEventRecord(p.start, s ? s : stream));
     pending.push_back(p);
     return int(pending.size()) - 1;
 }
 
-void HpCudaContext::prof_end(int token) {
+void HpCudaContext::prof_end(int token, cudaStream_t s) {
     if (token < 0) return;
-    check_cuda(cudaEventRecord(pending[size_t(token)].stop, stream));
+    check_cuda(cudaEventRecord(pending[size_t(token)].stop, s ? s : stream));
 }
 
 void HpCudaContext::prof_resolve() {
@@ -89,6 +108,7 @@ void HpCudaContext::prof_resolve() {
     check_cuda(cudaStreamSynchronize(stream));
     for (auto &p : pending) {
         float ms = 0.f;
+        check_cuda(cudaEventSynchronize(p.stop));
         check_cuda(cudaEventElapsedTime(&ms, p.start, p.stop));
         auto &t = totals[p.name];
         t.first += double(ms);
@@ -170,6 +190,11 @@ extern "C" HpCudaStatus hp_cuda_v1_context_destroy(HpCudaContext *ctx) {
             cudaEventDestroy(p.stop);
         }
         for (auto e : ctx->event_pool) cudaEventDestroy(e);
+        for (int i = 0; i < HpCudaContext::kWorkers; i++) {
+            if (ctx->workers[i]) cudaStreamDestroy(ctx->workers[i]);
+            if (ctx->join_events[i]) cudaEventDestroy(ctx->join_events[i]);
+        }
+        if (ctx->fork_event) cudaEventDestroy(ctx->fork_event);
         cudaFree(ctx->d_flags);
         cudaFreeHost(ctx->h_flags);
         cudaStreamDestroy(ctx->stream);

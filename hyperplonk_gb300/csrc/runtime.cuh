@@ -85,11 +85,23 @@ struct HpCudaContext {
     };
     std::unordered_map<void *, Buffer> buffers;
 
+    // Worker streams for independent work inside one call (fork from and
+    // join back into `stream` with events; created on first use).
+    static constexpr int kWorkers = 8;
+    cudaStream_t workers[kWorkers] = {};
+    cudaEvent_t fork_event = nullptr;
+    cudaEvent_t join_events[kWorkers] = {};
+    // Make the first k workers wait for everything queued on `stream`.
+    void fork(int k);
+    // Make `stream` wait for everything queued on the first k workers.
+    void join(int k);
+
     // Stream-ordered allocation registered with one reference.
     void *alloc(size_t bytes);
-    // Unregistered scratch (freed with scratch_free, stream ordered).
-    void *scratch(size_t bytes);
-    void scratch_free(void *p);
+    // Unregistered scratch (freed with scratch_free, stream ordered on `s`,
+    // the context stream by default).
+    void *scratch(size_t bytes, cudaStream_t s = nullptr);
+    void scratch_free(void *p, cudaStream_t s = nullptr);
     void ref(void *p);
     void unref(void *p);
     // True while `p` is a caller-owned handle (allocated, not yet retired).
@@ -112,8 +124,9 @@ struct HpCudaContext {
     std::map<std::string, std::pair<double, uint64_t>> totals;  // ms, launches
     cudaEvent_t take_event();
     // Returns an index to pass to prof_end, or -1 when profiling is off.
-    int prof_begin(const char *name);
-    void prof_end(int token);
+    // Events go on stream `s` (the context stream by default).
+    int prof_begin(const char *name, cudaStream_t s = nullptr);
+    void prof_end(int token, cudaStream_t s = nullptr);
     void prof_resolve();
     // Clear the device status word (stream ordered).
     void clear_flags();
@@ -124,26 +137,28 @@ struct HpCudaContext {
 
 namespace hp {
 
-// RAII scratch: stream-ordered free at scope exit.
+// RAII scratch: stream-ordered allocation and free on one stream.
 struct Scratch {
     HpCudaContext *ctx = nullptr;
     void *ptr = nullptr;
+    cudaStream_t stream = nullptr;  // null: the context stream
     Scratch() = default;
-    Scratch(HpCudaContext *c, size_t bytes) : ctx(c), ptr(c->scratch(bytes)) {}
+    Scratch(HpCudaContext *c, size_t bytes, cudaStream_t s = nullptr) : ctx(c), ptr(c->scratch(bytes, s)), stream(s) {}
     Scratch(const Scratch &) = delete;
     Scratch &operator=(const Scratch &) = delete;
-    Scratch(Scratch &&o) noexcept : ctx(o.ctx), ptr(o.ptr) { o.ptr = nullptr; }
+    Scratch(Scratch &&o) noexcept : ctx(o.ctx), ptr(o.ptr), stream(o.stream) { o.ptr = nullptr; }
     Scratch &operator=(Scratch &&o) noexcept {
         if (this != &o) {
-            if (ptr) ctx->scratch_free(ptr);
+            if (ptr) ctx->scratch_free(ptr, stream);
             ctx = o.ctx;
             ptr = o.ptr;
+            stream = o.stream;
             o.ptr = nullptr;
         }
         return *this;
     }
     ~Scratch() {
-        if (ptr) ctx->scratch_free(ptr);
+        if (ptr) ctx->scratch_free(ptr, stream);
     }
     template <class T>
     T *as() const { return static_cast<T *>(ptr); }

@@ -350,6 +350,77 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_create(
     });
 }
 
+namespace hp {
+
+// Checks a round request without touching the state (misuse -> InvalidState,
+// bad arguments -> InvalidParameters).
+static void check_round(HpCudaSumCheckProverState *s, const uint8_t *challenge_or_null, uint8_t *out,
+                        size_t evaluation_count) {
+    require(s != nullptr && out != nullptr);
+    if (s->poisoned) fail(HP_CUDA_STATUS_INVALID_STATE);
+    require(evaluation_count == s->max_degree + 1);
+    if (s->round >= s->num_vars) fail(HP_CUDA_STATUS_INVALID_STATE);
+    if (s->round == 0 && challenge_or_null != nullptr) fail(HP_CUDA_STATUS_INVALID_STATE);
+    if (s->round > 0 && challenge_or_null == nullptr) fail(HP_CUDA_STATUS_INVALID_STATE);
+}
+
+// Enqueues one round of state s on stream st: fold with r (rounds > 1) and
+// message into out_dev (degree + 1 canonical Fr, device).  Scratch is ordered
+// on st.  Does not advance the state.
+static void enqueue_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, const Fr &r, cudaStream_t st,
+                          Fr *out_dev) {
+    const SumcheckDesc &d = s->desc;
+    const bool fold = s->round > 0;
+    const int src_which = s->current;
+    const int dst_which = fold ? (src_which == 1 ? 2 : 1) : src_which;
+    size_t pairs = table_len(s->num_vars - s->round - 1);
+    FrPtrList src{}, rd{};
+    FrMutPtrList dst{};
+    for (int f = 0; f < d.factor_count; f++) {
+        src.p[f] = state_table(s, src_which, f);
+        dst.p[f] = const_cast<Fr *>(state_table(s, dst_which, f));
+        rd.p[f] = fold ? dst.p[f] : src.p[f];
+    }
+    const bool regs = d.max_arity <= 8 && d.slot_count <= kMaxSlotsV2;
+    unsigned grid;
+    Scratch partials, sums(ctx, d.slot_count * sizeof(Fr), st);
+    int tok = ctx->prof_begin("sumcheck_round", st);
+    if (regs) {
+        grid = grid_for(ctx, pairs, kRoundThreads, 8);
+        partials = Scratch(ctx, size_t(grid) * d.slot_count * sizeof(Fr), st);
+        auto launch = [&](auto kernel) {
+            kernel<<<grid, kRoundThreads, 0, st>>>(d, src, dst, rd, fold, r, pairs, partials.as<Fr>());
+        };
+        if (d.max_arity <= 2) launch(k_sumcheck_round_regs<2>);
+        else if (d.max_arity <= 4) launch(k_sumcheck_round_regs<4>);
+        else if (d.max_arity <= 6) launch(k_sumcheck_round_regs<6>);
+        else launch(k_sumcheck_round_regs<8>);
+        check_launch();
+    } else {
+        size_t smem;
+        int T = round_block_size(d, &smem);
+        if (smem > 48 * 1024)
+            check_cuda(cudaFuncSetAttribute(k_sumcheck_round, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            int(smem)));
+        grid = grid_for(ctx, pairs, unsigned(T), 2);
+        partials = Scratch(ctx, size_t(grid) * d.slot_count * sizeof(Fr), st);
+        k_sumcheck_round<<<grid, T, smem, st>>>(d, src, dst, fold, r, pairs, partials.as<Fr>());
+        check_launch();
+    }
+    ctx->prof_end(tok, st);
+    k_sumcheck_finalize<<<1, 256, 256 * sizeof(Fr), st>>>(d, partials.as<Fr>(), int(grid),
+                                                           static_cast<const Fr *>(s->coefs), int(s->max_degree),
+                                                           sums.as<Fr>(), out_dev);
+    check_launch();
+}
+
+static void advance(HpCudaSumCheckProverState *s) {
+    if (s->round > 0) s->current = s->current == 1 ? 2 : 1;
+    s->round++;
+}
+
+}  // namespace hp
+
 extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_round(HpCudaContext *ctx,
                                                                HpCudaSumCheckProverState *s,
                                                                const uint8_t *challenge_or_null,
@@ -357,68 +428,63 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_round(HpCudaContext *ct
                                                                size_t evaluation_count) {
     return guard([&] {
         hp::require_ctx(ctx);
-        require(s != nullptr && out_evaluations != nullptr);
-        if (s->poisoned) fail(HP_CUDA_STATUS_INVALID_STATE);
-        require(evaluation_count == s->max_degree + 1);
-        if (s->round >= s->num_vars) fail(HP_CUDA_STATUS_INVALID_STATE);
-        if (s->round == 0 && challenge_or_null != nullptr) fail(HP_CUDA_STATUS_INVALID_STATE);
-        if (s->round > 0 && challenge_or_null == nullptr) fail(HP_CUDA_STATUS_INVALID_STATE);
+        hp::check_round(s, challenge_or_null, out_evaluations, evaluation_count);
         Fr r = Fr::zero();
         if (challenge_or_null) r = hp::host_scalar(challenge_or_null);
         try {
-            const hp::SumcheckDesc &d = s->desc;
-            const bool fold = s->round > 0;
-            const int src_which = s->current;
-            const int dst_which = fold ? (src_which == 1 ? 2 : 1) : src_which;
-            size_t pairs = hp::table_len(s->num_vars - s->round - 1);
-            hp::FrPtrList src{};
-            hp::FrMutPtrList dst{};
-            for (int f = 0; f < d.factor_count; f++) {
-                src.p[f] = hp::state_table(s, src_which, f);
-                dst.p[f] = const_cast<Fr *>(hp::state_table(s, dst_which, f));
-            }
-            const bool regs = d.max_arity <= 8 && d.slot_count <= hp::kMaxSlotsV2;
-            unsigned grid;
-            hp::Scratch partials, sums(ctx, d.slot_count * sizeof(Fr)), outd(ctx, evaluation_count * sizeof(Fr));
-            int tok = ctx->prof_begin("sumcheck_round");
-            if (regs) {
-                hp::FrPtrList rd{};
-                for (int f = 0; f < d.factor_count; f++) rd.p[f] = fold ? dst.p[f] : src.p[f];
-                grid = hp::grid_for(ctx, pairs, hp::kRoundThreads, 8);
-                partials = hp::Scratch(ctx, size_t(grid) * d.slot_count * sizeof(Fr));
-                auto launch = [&](auto kernel) {
-                    kernel<<<grid, hp::kRoundThreads, 0, ctx->stream>>>(d, src, dst, rd, fold, r, pairs,
-                                                                        partials.as<Fr>());
-                };
-                if (d.max_arity <= 2) launch(hp::k_sumcheck_round_regs<2>);
-                else if (d.max_arity <= 4) launch(hp::k_sumcheck_round_regs<4>);
-                else if (d.max_arity <= 6) launch(hp::k_sumcheck_round_regs<6>);
-                else launch(hp::k_sumcheck_round_regs<8>);
-                check_launch();
-            } else {
-                size_t smem;
-                int T = hp::round_block_size(d, &smem);
-                if (smem > 48 * 1024)
-                    check_cuda(cudaFuncSetAttribute(hp::k_sumcheck_round,
-                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-                grid = hp::grid_for(ctx, pairs, unsigned(T), 2);
-                partials = hp::Scratch(ctx, size_t(grid) * d.slot_count * sizeof(Fr));
-                hp::k_sumcheck_round<<<grid, T, smem, ctx->stream>>>(d, src, dst, fold, r, pairs,
-                                                                     partials.as<Fr>());
-                check_launch();
-            }
-            ctx->prof_end(tok);
-            hp::k_sumcheck_finalize<<<1, 256, 256 * sizeof(Fr), ctx->stream>>>(
-                d, partials.as<Fr>(), int(grid), static_cast<const Fr *>(s->coefs),
-                int(s->max_degree), sums.as<Fr>(), outd.as<Fr>());
-            check_launch();
+            hp::Scratch outd(ctx, evaluation_count * sizeof(Fr));
+            hp::enqueue_round(ctx, s, r, ctx->stream, outd.as<Fr>());
             check_cuda(cudaMemcpyAsync(out_evaluations, outd.ptr, evaluation_count * sizeof(Fr),
                                        cudaMemcpyDeviceToHost, ctx->stream));
             ctx->sync();
-            s->current = dst_which;
-            s->round++;
+            hp::advance(s);
         } catch (const hp::Failure &f) {
             if (f.kind == HP_CUDA_STATUS_INVALID_STATE) s->poisoned = true;
+            throw;
+        }
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_batch_sumcheck_round(HpCudaContext *ctx, HpCudaSumCheckProverState *const *states,
+                                                        const uint8_t *const *challenges_or_null,
+                                                        uint8_t *const *out_evaluations,
+                                                        const size_t *evaluation_counts, size_t count) {
+    return guard([&] {
+        hp::require_ctx(ctx);
+        if (count == 0) return;
+        require(states != nullptr && challenges_or_null != nullptr && out_evaluations != nullptr &&
+                evaluation_counts != nullptr);
+        std::vector<Fr> rs(count, Fr::zero());
+        size_t total = 0;
+        for (size_t i = 0; i < count; i++) {
+            hp::check_round(states[i], challenges_or_null[i], out_evaluations[i], evaluation_counts[i]);
+            for (size_t j = 0; j < i; j++) require(states[j] != states[i]);
+            if (challenges_or_null[i]) rs[i] = hp::host_scalar(challenges_or_null[i]);
+            total += evaluation_counts[i];
+        }
+        try {
+            hp::Scratch outd(ctx, total * sizeof(Fr));
+            std::vector<Fr> host_out(total);
+            const int k = int(std::min<size_t>(count, HpCudaContext::kWorkers));
+            ctx->fork(k);
+            size_t off = 0;
+            for (size_t i = 0; i < count; i++) {
+                hp::enqueue_round(ctx, states[i], rs[i], ctx->workers[i % size_t(k)], outd.as<Fr>() + off);
+                off += evaluation_counts[i];
+            }
+            ctx->join(k);
+            check_cuda(cudaMemcpyAsync(host_out.data(), outd.ptr, total * sizeof(Fr), cudaMemcpyDeviceToHost,
+                                       ctx->stream));
+            ctx->sync();
+            off = 0;
+            for (size_t i = 0; i < count; i++) {
+                std::memcpy(out_evaluations[i], host_out.data() + off, evaluation_counts[i] * sizeof(Fr));
+                off += evaluation_counts[i];
+                hp::advance(states[i]);
+            }
+        } catch (const hp::Failure &f) {
+            if (f.kind == HP_CUDA_STATUS_INVALID_STATE)
+                for (size_t i = 0; i < count; i++) states[i]->poisoned = true;
             throw;
         }
     });

@@ -184,6 +184,29 @@ HpCudaStatus hp_cuda_v1_mle_download(HpCudaContext *ctx, HpCudaDeviceAddress pol
 HpCudaStatus hp_cuda_v1_msm(HpCudaContext *ctx, const uint8_t *bases, const uint8_t *scalars,
                             size_t count, uint8_t *out_point);
 
+/* Batched execution (no counterpart in the reference's bridge; its
+ * multi_commit, bridge_kzg.cpp:517-579, runs MSMs one after another).
+ *
+ * batch_msm: MSM i = sum_j s_i[j] * B[j] where s_i is the resident MLE
+ * scalars[i] (2^num_vars[i] entries) and B the first 2^num_vars[i] bases of
+ * prepared layer `layer_index` (prefix semantics).  A prefix shorter than the
+ * layer is prepared once (its own window width and precomputed windows) and
+ * cached in the parameter object.  All MSMs of the call overlap on the device;
+ * writes count 97-byte packets in input order.
+ *
+ * batch_sumcheck_round: one round of each of `count` distinct prover states
+ * (challenge_or_null per state, same rules as sumcheck_prover_state_round),
+ * overlapped on the device with one synchronisation; out_evaluations[i] gets
+ * evaluation_counts[i] canonical Fr.  A misuse of any state leaves every
+ * state unchanged. */
+HpCudaStatus hp_cuda_v1_batch_msm(HpCudaContext *ctx, HpCudaMultilinearKzgPreparedProverParam *params,
+                                  size_t layer_index, const HpCudaDeviceAddress *scalars, const size_t *num_vars,
+                                  size_t count, uint8_t *out_points);
+HpCudaStatus hp_cuda_v1_batch_sumcheck_round(HpCudaContext *ctx, HpCudaSumCheckProverState *const *states,
+                                             const uint8_t *const *challenges_or_null,
+                                             uint8_t *const *out_evaluations, const size_t *evaluation_counts,
+                                             size_t count);
+
 /* Evaluation of a resident MLE that allocates no device memory.  No
  * counterpart in the reference.  For callers that cannot call cudaMalloc:
  * hosts that own all device memory through their own pre-reserved arena, or
