@@ -60,6 +60,7 @@ SIGNATURES: dict[str, list] = {
     "hp_cuda_v1_fixture_random_fr": [ctypes.c_uint64, ctypes.c_uint64, c_size, c_u8p],
     "hp_cuda_v1_srs_generate": [c_voidp, c_size, ctypes.c_uint64, c_u8p, c_size],
     "hp_cuda_v1_fixture_vanilla_plonk": [ctypes.c_uint64, c_size, c_u8p, c_u8p, c_u8p],
+    "hp_cuda_v1_fixture_vanilla_plonk_witness": [ctypes.c_uint64, ctypes.c_uint64, c_size, c_u8p],
     "hp_host_v1_merlin_new": [c_u8p, c_size, c_voidpp],
     "hp_host_v1_merlin_append": [c_voidp, c_u8p, c_size, c_u8p, c_size],
     "hp_host_v1_merlin_challenge": [c_voidp, c_u8p, c_size, c_u8p, c_size],

@@ -14,6 +14,7 @@ None for the point at infinity.
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes
 from typing import Iterable, Optional, Sequence
 
@@ -98,6 +99,13 @@ class CudaContext:
                      "context_create")
         self.raw = raw
         self.device_id = device_id
+        # Set by a caller that drives this context from several host threads
+        # (one at a time): handle destructors then take it too, so a retire
+        # never overlaps another thread's call on the context.
+        self.lock = None
+
+    def held(self):
+        return self.lock if self.lock is not None else contextlib.nullcontext()
 
     def stream(self) -> int:
         out = ctypes.c_void_p()
@@ -139,7 +147,8 @@ class CudaMle:
         ctx = self._ctx
         if ctx is not None and ctx.raw is not None and self._addr:
             try:
-                ctx.lib.hp_cuda_v1_buffer_retire(ctx.raw, ctypes.c_void_p(self._addr))
+                with ctx.held():
+                    ctx.lib.hp_cuda_v1_buffer_retire(ctx.raw, ctypes.c_void_p(self._addr))
             except Exception:
                 pass
         self._addr = 0
@@ -153,7 +162,8 @@ class CudaPreparedProverParam:
         ctx = self._ctx
         if ctx is not None and ctx.raw is not None and self.raw is not None:
             try:
-                ctx.lib.hp_cuda_v1_multilinear_kzg_params_destroy(ctx.raw, self.raw)
+                with ctx.held():
+                    ctx.lib.hp_cuda_v1_multilinear_kzg_params_destroy(ctx.raw, self.raw)
             except Exception:
                 pass
         self.raw = None
@@ -169,7 +179,8 @@ class CudaSumCheckProverState:
         ctx = self._ctx
         if ctx is not None and ctx.raw is not None and self.raw is not None:
             try:
-                ctx.lib.hp_cuda_v1_sumcheck_prover_state_destroy(ctx.raw, self.raw)
+                with ctx.held():
+                    ctx.lib.hp_cuda_v1_sumcheck_prover_state_destroy(ctx.raw, self.raw)
             except Exception:
                 pass
         self.raw = None
@@ -210,6 +221,21 @@ class CudaBackend:
         check_status(self.lib.hp_cuda_v1_mle_upload(self.ctx.raw, num_vars, _native.buf(data), n // 32,
                                                     ctypes.byref(out)), "mle_upload")
         return self._new(out, num_vars)
+
+    def generate_srs(self, num_vars: int, seed: int) -> list:
+        """Testing SRS of num_vars variables from fixture seed `seed`, computed
+        on the device: num_vars + 1 layers of 97-byte packets (uint8 arrays),
+        layer i holding 2^(num_vars - i) points."""
+        total = (1 << (num_vars + 1)) - 1
+        packets = np.empty(total * 97, dtype=np.uint8)
+        check_status(self.lib.hp_cuda_v1_srs_generate(self.ctx.raw, num_vars, seed, _native.buf(packets), total),
+                     "srs_generate")
+        layers, off = [], 0
+        for i in range(num_vars + 1):
+            cnt = 1 << (num_vars - i) if i < num_vars else 1
+            layers.append(packets[97 * off:97 * (off + cnt)])
+            off += cnt
+        return layers
 
     def download(self, mle: CudaMle) -> bytes:
         """Canonical table bytes of a resident MLE (test/debug helper)."""

@@ -14,7 +14,8 @@
 //     (histogram -> exclusive scan -> atomic scatter) groups the
 //     (window, point, sign) records by bucket -- bucket order inside a group
 //     is irrelevant because field arithmetic is exact;
-//  3. accumulate: one thread per bucket, XYZZ mixed additions (8M + 2S);
+//  3. accumulate: flat chunks of L bucket-ordered records per thread, XYZZ
+//     mixed additions (8M + 2S), buckets cut by chunk edges fixed up after;
 //  4. reduce: sum_b (b+1) S_b via segments of `seg` buckets (running sums,
 //     two XYZZ additions per bucket), then the segment weights j are split
 //     into bits: sum_j j R_j = sum_k 2^k sum_{j : bit k} R_j, whose subset sums
@@ -22,6 +23,7 @@
 //  5. the host finishes the short Horner chain over those subset sums and
 //     converts to affine (one inversion), see host_ec.h.
 #include <algorithm>
+#include <atomic>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -333,31 +335,72 @@ __global__ void k_msm_histogram(const Fr *scalars, const Fr *delta, size_t n, in
     }
 }
 
-// Exclusive scan of `m` counts by one block of 1024 threads; writes offsets
-// [0..m] (offsets[m] = total) and a copy of offsets[0..m) into cursor.
-__global__ void __launch_bounds__(1024) k_msm_scan(const uint32_t *counts, size_t m, uint32_t *offsets,
-                                                   uint32_t *cursor) {
-    __shared__ uint32_t part[1024];
-    const int t = threadIdx.x;
-    size_t chunk = (m + 1023) / 1024;
-    size_t b = t * chunk, e = min(m, b + chunk);
-    uint32_t s = 0;
-    for (size_t i = b; i < e; i++) s += counts[i];
-    part[t] = s;
+// Exclusive scan of the m bucket counts, in tiles of kScanTile: k_msm_scan_sums
+// writes one total per tile, then k_msm_scan gives every tile its prefix
+// (the sum of the tile totals before it) and scans it, writing offsets[0..m]
+// (offsets[m] = total) and a copy of offsets[0..m) into cursor.  Thread i of
+// a tile owns counts [4i, 4i+4); loads and stores are coalesced.
+constexpr int kScanThreads = 1024;
+constexpr int kScanTile = 4 * kScanThreads;
+
+__device__ __forceinline__ uint32_t block_inclusive_scan(uint32_t v, uint32_t *warp_tot) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int off = 1; off < 32; off <<= 1) {
+        uint32_t u = __shfl_up_sync(0xffffffffu, v, off);
+        if (lane >= off) v += u;
+    }
+    if (lane == 31) warp_tot[warp] = v;
     __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        uint32_t v = t >= off ? part[t - off] : 0;
-        __syncthreads();
-        part[t] += v;
-        __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < int(blockDim.x >> 5) ? warp_tot[lane] : 0;
+        for (int off = 1; off < 32; off <<= 1) {
+            uint32_t u = __shfl_up_sync(0xffffffffu, w, off);
+            if (lane >= off) w += u;
+        }
+        warp_tot[lane] = w;  // inclusive over warps
     }
-    uint32_t run = part[t] - s;  // exclusive prefix of this chunk
-    for (size_t i = b; i < e; i++) {
-        offsets[i] = run;
-        cursor[i] = run;
-        run += counts[i];
+    __syncthreads();
+    return v + (warp > 0 ? warp_tot[warp - 1] : 0);
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_msm_scan_sums(const uint32_t *counts, size_t m,
+                                                                uint32_t *tile_sums) {
+    __shared__ uint32_t warp_tot[32];
+    const size_t i = size_t(blockIdx.x) * kScanTile + 4 * size_t(threadIdx.x);
+    uint32_t s = 0;
+    for (int k = 0; k < 4; k++) s += i + k < m ? counts[i + k] : 0;
+    s = block_inclusive_scan(s, warp_tot);
+    if (threadIdx.x == kScanThreads - 1) tile_sums[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_msm_scan(const uint32_t *counts, size_t m,
+                                                           const uint32_t *tile_sums, uint32_t *offsets,
+                                                           uint32_t *cursor) {
+    __shared__ uint32_t warp_tot[32];
+    __shared__ uint32_t tile_base;
+    // prefix of this tile: sum of the totals of tiles 0..blockIdx.x-1
+    uint32_t p = 0;
+    for (uint32_t t = threadIdx.x; t < blockIdx.x; t += kScanThreads) p += tile_sums[t];
+    p = block_inclusive_scan(p, warp_tot);
+    if (threadIdx.x == kScanThreads - 1) tile_base = p;
+    __syncthreads();
+    const uint32_t base = tile_base;
+    __syncthreads();  // warp_tot is reused below
+    const size_t i = size_t(blockIdx.x) * kScanTile + 4 * size_t(threadIdx.x);
+    uint32_t v[4], s = 0;
+    for (int k = 0; k < 4; k++) {
+        v[k] = i + k < m ? counts[i + k] : 0;
+        s += v[k];
     }
-    if (t == 1023) offsets[m] = part[1023];
+    uint32_t run = base + block_inclusive_scan(s, warp_tot) - s;
+    for (int k = 0; k < 4; k++) {
+        if (i + k < m) {
+            offsets[i + k] = run;
+            cursor[i + k] = run;
+        }
+        run += v[k];
+    }
+    if (i < m && m <= i + 4) offsets[m] = run;  // the thread holding the last count writes the total
 }
 
 __global__ void k_msm_scatter(const Fr *scalars, const Fr *delta, size_t n, size_t stride, int c, int windows,
@@ -389,7 +432,34 @@ __global__ void k_msm_scatter(const Fr *scalars, const Fr *delta, size_t n, size
 #ifndef HP_ACC_MINBLOCKS
 #define HP_ACC_MINBLOCKS 3  // measured best on GB300 at 2^20 (13.9 ms vs 14.2 ms at 1)
 #endif
-constexpr uint32_t kChunkRecords = 32;
+
+// Chunk length L: the grid is exactly the resident blocks of k_msm_accumulate
+// and every thread takes the same number k of chunks, so there is no partial
+// last wave; k is the whole number of chunks per thread that puts L nearest
+// 64 records (fewer, longer chunks cut fewer buckets).  L stays in [16, 256].
+struct AccumulateGeometry {
+    uint32_t chunk;   // records per chunk (L)
+    size_t chunks;    // ceil(records / L)
+    unsigned grid;    // blocks of 128 threads
+};
+
+static int accumulate_blocks_per_sm();
+
+AccumulateGeometry accumulate_geometry(const HpCudaContext *ctx, size_t records) {
+    const size_t resident = size_t(ctx->sm_count > 0 ? ctx->sm_count : 152) * accumulate_blocks_per_sm() * 128;
+    const size_t per_wave = resident * 64;
+    size_t k = (records + per_wave / 2) / per_wave;
+    if (k == 0) k = 1;
+    size_t L = (records + resident * k - 1) / (resident * k);
+    if (L < 16) L = 16;
+    if (L > 256) L = 256;
+    AccumulateGeometry g;
+    g.chunk = uint32_t(L);
+    g.chunks = (records + L - 1) / L;
+    g.grid = unsigned(std::min<size_t>((g.chunks + 127) / 128, resident / 128));
+    if (g.grid == 0) g.grid = 1;
+    return g;
+}
 
 // largest b in [0, buckets) with offsets[b] <= k (k < offsets[buckets])
 __device__ __forceinline__ uint32_t bucket_of(const uint32_t *offsets, uint32_t buckets, uint32_t k) {
@@ -403,11 +473,12 @@ __device__ __forceinline__ uint32_t bucket_of(const uint32_t *offsets, uint32_t 
 
 __global__ void __launch_bounds__(128, HP_ACC_MINBLOCKS) k_msm_accumulate(const Affine *bases, const uint32_t *offsets,
                                                                           const uint32_t *records, uint32_t buckets,
-                                                                          Xyzz *bucket_sums, Xyzz *pieces) {
+                                                                          uint32_t chunk, Xyzz *bucket_sums,
+                                                                          Xyzz *pieces) {
     const uint32_t total = offsets[buckets];
-    const uint32_t chunks = (total + kChunkRecords - 1) / kChunkRecords;
+    const uint32_t chunks = (total + chunk - 1) / chunk;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < chunks; t += gridDim.x * blockDim.x) {
-        const uint32_t lo = t * kChunkRecords, hi = min(lo + kChunkRecords, total);
+        const uint32_t lo = t * chunk, hi = min(lo + chunk, total);
         uint32_t b = bucket_of(offsets, buckets, lo);
         uint32_t b_end = offsets[b + 1];
         Xyzz acc = xyzz_inf();
@@ -433,8 +504,19 @@ __global__ void __launch_bounds__(128, HP_ACC_MINBLOCKS) k_msm_accumulate(const 
     }
 }
 
+static int accumulate_blocks_per_sm() {
+    static std::atomic<int> cached{0};
+    int v = cached.load(std::memory_order_relaxed);
+    if (v > 0) return v;
+    int blocks = 0;
+    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_msm_accumulate, 128, 0));
+    v = blocks > 0 ? blocks : 1;
+    cached.store(v, std::memory_order_relaxed);
+    return v;
+}
+
 // Buckets cut by chunk boundaries: add their pieces; empty buckets: infinity.
-__global__ void k_msm_bucket_fixup(const uint32_t *offsets, uint32_t buckets, const Xyzz *pieces,
+__global__ void k_msm_bucket_fixup(const uint32_t *offsets, uint32_t buckets, uint32_t chunk, const Xyzz *pieces,
                                    Xyzz *bucket_sums) {
     for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < buckets; b += gridDim.x * blockDim.x) {
         const uint32_t begin = offsets[b], end = offsets[b + 1];
@@ -442,7 +524,7 @@ __global__ void k_msm_bucket_fixup(const uint32_t *offsets, uint32_t buckets, co
             store_xyzz(&bucket_sums[b], xyzz_inf());
             continue;
         }
-        const uint32_t t0 = begin / kChunkRecords, t1 = (end - 1) / kChunkRecords;
+        const uint32_t t0 = begin / chunk, t1 = (end - 1) / chunk;
         if (t0 == t1) continue;
         Xyzz acc = load_xyzz(&pieces[2 * size_t(t0) + 1]);
         for (uint32_t t = t0 + 1; t <= t1; t++) acc = xyzz_add(acc, load_xyzz(&pieces[2 * size_t(t)]));
@@ -532,20 +614,26 @@ void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz 
     k_msm_histogram<<<grid_for(ctx, n, 256), 256, 0, st>>>(scalars, layer.delta, n, layer.c, layer.windows,
                                                           counts.as<uint32_t>());
     check_launch();
-    k_msm_scan<<<1, 1024, 0, st>>>(counts.as<uint32_t>(), B, offsets.as<uint32_t>(), cursor.as<uint32_t>());
+    const unsigned tiles = unsigned((B + kScanTile - 1) / kScanTile);
+    Scratch tile_sums(ctx, size_t(tiles) * 4, st);
+    if (tiles > 1) {
+        k_msm_scan_sums<<<tiles, kScanThreads, 0, st>>>(counts.as<uint32_t>(), B, tile_sums.as<uint32_t>());
+        check_launch();
+    }
+    k_msm_scan<<<tiles, kScanThreads, 0, st>>>(counts.as<uint32_t>(), B, tile_sums.as<uint32_t>(),
+                                              offsets.as<uint32_t>(), cursor.as<uint32_t>());
     check_launch();
     k_msm_scatter<<<grid_for(ctx, n, 256), 256, 0, st>>>(scalars, layer.delta, n, layer.n, layer.c, layer.windows,
                                                         cursor.as<uint32_t>(), recs.as<uint32_t>());
     check_launch();
-    const size_t record_chunks = (records + kChunkRecords - 1) / kChunkRecords;
-    Scratch pieces(ctx, std::max<size_t>(2 * record_chunks, 1) * sizeof(Xyzz), st);
+    const AccumulateGeometry geo = accumulate_geometry(ctx, records);
+    Scratch pieces(ctx, std::max<size_t>(2 * geo.chunks, 1) * sizeof(Xyzz), st);
     int tok = ctx->prof_begin("msm_accumulate", st);
-    k_msm_accumulate<<<grid_for(ctx, record_chunks, 128, 16), 128, 0, st>>>(
-        layer.bases, offsets.as<uint32_t>(), recs.as<uint32_t>(), uint32_t(B), buckets.as<Xyzz>(),
-        pieces.as<Xyzz>());
+    k_msm_accumulate<<<geo.grid, 128, 0, st>>>(layer.bases, offsets.as<uint32_t>(), recs.as<uint32_t>(),
+                                               uint32_t(B), geo.chunk, buckets.as<Xyzz>(), pieces.as<Xyzz>());
     check_launch();
     ctx->prof_end(tok, st);
-    k_msm_bucket_fixup<<<grid_for(ctx, B, 128, 8), 128, 0, st>>>(offsets.as<uint32_t>(), uint32_t(B),
+    k_msm_bucket_fixup<<<grid_for(ctx, B, 128, 8), 128, 0, st>>>(offsets.as<uint32_t>(), uint32_t(B), geo.chunk,
                                                                 pieces.as<Xyzz>(), buckets.as<Xyzz>());
     check_launch();
     Scratch acc(ctx, sh.segments * sizeof(Xyzz), st), run(ctx, sh.segments * sizeof(Xyzz), st);

@@ -201,10 +201,12 @@ extern "C" HpCudaStatus hp_cuda_v1_srs_generate(HpCudaContext *ctx, size_t num_v
 }
 
 // Vanilla-plonk fixture (full-prove workload): see include/hp_cuda.h.
-extern "C" HpCudaStatus hp_cuda_v1_fixture_vanilla_plonk(uint64_t seed, size_t num_vars, uint8_t *selectors,
-                                                         uint8_t *witnesses, uint8_t *permutation) {
-    return guard([&] {
-        require(selectors != nullptr && witnesses != nullptr && permutation != nullptr && num_vars <= 28);
+// Selectors from stream `seed` elements [k n, (k+1) n) for q_L, q_R, q_M, q_C
+// (k = 0..3); w1, w2 from stream `witness_seed` elements [4n, 5n) and [5n, 6n);
+// w3 solves the gate.  selectors / permutation may be null (witnesses only).
+static void vanilla_fixture(uint64_t seed, uint64_t witness_seed, size_t num_vars, uint8_t *selectors,
+                            uint8_t *witnesses, uint8_t *permutation) {
+    {
         const size_t n = size_t(1) << num_vars;
         hp::host::Fr64 minus_one;
         {
@@ -229,13 +231,16 @@ extern "C" HpCudaStatus hp_cuda_v1_fixture_vanilla_plonk(uint64_t seed, size_t n
                 for (size_t i = b; i < e; i++) {
                     Fr64 ql = hp::fixture_element(seed, i), qr = hp::fixture_element(seed, n + i);
                     Fr64 qm = hp::fixture_element(seed, 2 * n + i), qc = hp::fixture_element(seed, 3 * n + i);
-                    Fr64 w1 = hp::fixture_element(seed, 4 * n + i), w2 = hp::fixture_element(seed, 5 * n + i);
+                    Fr64 w1 = hp::fixture_element(witness_seed, 4 * n + i);
+                    Fr64 w2 = hp::fixture_element(witness_seed, 5 * n + i);
                     Fr64 w3 = add(add(mont_mul(ql, w1), mont_mul(qr, w2)), add(mont_mul(mont_mul(qm, w1), w2), qc));
                     const Fr64 sel[5] = {ql, qr, minus_one, qm, qc};
                     const Fr64 wit[3] = {w1, w2, w3};
-                    for (int k = 0; k < 5; k++) to_canonical(sel[k], selectors + (size_t(k) * n + i) * 32);
+                    if (selectors)
+                        for (int k = 0; k < 5; k++) to_canonical(sel[k], selectors + (size_t(k) * n + i) * 32);
                     for (int k = 0; k < 3; k++) {
                         to_canonical(wit[k], witnesses + (size_t(k) * n + i) * 32);
+                        if (!permutation) continue;
                         uint8_t *p = permutation + (size_t(k) * n + i) * 32;
                         std::memset(p, 0, 32);
                         uint64_t label = uint64_t(k) * n + i;
@@ -245,5 +250,21 @@ extern "C" HpCudaStatus hp_cuda_v1_fixture_vanilla_plonk(uint64_t seed, size_t n
             });
         }
         for (auto &th : pool) th.join();
+    }
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_fixture_vanilla_plonk(uint64_t seed, size_t num_vars, uint8_t *selectors,
+                                                         uint8_t *witnesses, uint8_t *permutation) {
+    return guard([&] {
+        require(selectors != nullptr && witnesses != nullptr && permutation != nullptr && num_vars <= 28);
+        vanilla_fixture(seed, seed, num_vars, selectors, witnesses, permutation);
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_fixture_vanilla_plonk_witness(uint64_t circuit_seed, uint64_t witness_seed,
+                                                                 size_t num_vars, uint8_t *witnesses) {
+    return guard([&] {
+        require(witnesses != nullptr && num_vars <= 28);
+        vanilla_fixture(circuit_seed, witness_seed, num_vars, nullptr, witnesses, nullptr);
     });
 }

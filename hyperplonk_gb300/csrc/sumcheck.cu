@@ -187,46 +187,60 @@ __global__ void __launch_bounds__(kRoundThreads) k_sumcheck_round_regs(SumcheckD
     }
 }
 
-// One block: sum block partials per slot, extend each product to degree D by
-// forward differences, scale by its coefficient, accumulate, write canonical.
+// One block.  Warp w sums the block partials of slots w, w + warps, ... (lane
+// strided loads, then shuffles) into shared memory.  Then thread x evaluates
+// the round polynomial at t = x: product p of arity m contributes
+// coef_p * v_p(x), where v_p(x) is its slot sum at x <= m and otherwise the
+// Newton forward-difference extension sum_j C(x, j) Delta^j v_p(0) of the m+1
+// sums -- the unique polynomial of degree <= m through them, as the
+// reference's barycentric extrapolation (backend/src/cpu/sum_check.rs:183-217).
+// Writes the slot sums (Montgomery) and the d+1 canonical evaluations.
 __global__ void k_sumcheck_finalize(SumcheckDesc desc, const Fr *partials, int blocks,
                                     const Fr *coefs, int degree, Fr *slot_sums, Fr *out) {
-    extern __shared__ Fr red[];
-    const int T = blockDim.x, t = threadIdx.x, S = desc.slot_count;
-    for (int s = 0; s < S; s++) {
+    extern __shared__ Fr sums[];
+    const int S = desc.slot_count;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+    for (int s = warp; s < S; s += warps) {
         Fr a = Fr::zero();
-        for (int b = t; b < blocks; b += T) a = a + partials[size_t(b) * S + s];
-        red[t] = a;
-        __syncthreads();
-        for (int half = T / 2; half > 0; half >>= 1) {
-            if (t < half) red[t] = red[t] + red[t + half];
-            __syncthreads();
-        }
-        if (t == 0) slot_sums[s] = red[0];
-        __syncthreads();
-    }
-    if (t != 0) return;
-    for (int k = 0; k <= degree; k++) out[k] = Fr::zero();
-    for (int p = 0; p < desc.product_count; p++) {
-        const int m = desc.offsets[p + 1] - desc.offsets[p];
-        const Fr *v = slot_sums + desc.slot_base[p];
-        Fr c = coefs[p];
-        // diagonal of the forward-difference table: last[k] = Delta^k v at m-k
-        Fr last[kMaxDegree + 1];
-        Fr row[kMaxDegree + 1];
-        for (int i = 0; i <= m; i++) row[i] = v[i];
-        last[0] = row[m];
-        for (int k = 1; k <= m; k++) {
-            for (int i = 0; i + k <= m; i++) row[i] = row[i + 1] - row[i];
-            last[k] = row[m - k];
-        }
-        for (int k = 0; k <= m; k++) out[k] = out[k] + c * v[k];
-        for (int x = m + 1; x <= degree; x++) {
-            for (int k = m - 1; k >= 0; k--) last[k] = last[k] + last[k + 1];
-            out[x] = out[x] + c * last[0];
+        for (int b = lane; b < blocks; b += 32) a = a + partials[size_t(b) * S + s];
+        a = warp_sum(a);
+        if (lane == 0) {
+            sums[s] = a;
+            slot_sums[s] = a;
         }
     }
-    for (int k = 0; k <= degree; k++) out[k] = from_mont(out[k]);
+    __syncthreads();
+    for (int x = threadIdx.x; x <= degree; x += blockDim.x) {
+        // C(x, j) for j <= x by Pascal's rule (x <= 64: every entry < 2^63)
+        uint64_t binom[kMaxDegree + 1];
+        binom[0] = 1;
+        for (int r = 1; r <= x; r++) {
+            binom[r] = 1;
+            for (int j = r - 1; j > 0; j--) binom[j] += binom[j - 1];
+        }
+        Fr acc = Fr::zero();
+        for (int p = 0; p < desc.product_count; p++) {
+            const int m = desc.offsets[p + 1] - desc.offsets[p];
+            const Fr *v = sums + desc.slot_base[p];
+            Fr val;
+            if (x <= m) {
+                val = v[x];
+            } else {
+                Fr d[kMaxDegree + 1];
+                for (int i = 0; i <= m; i++) d[i] = v[i];
+                val = d[0];
+                for (int j = 1; j <= m; j++) {
+                    for (int i = 0; i + j <= m; i++) d[i] = d[i + 1] - d[i];  // d[0] = Delta^j v(0)
+                    Fr cj = Fr::zero();
+                    cj.v[0] = uint32_t(binom[j]);
+                    cj.v[1] = uint32_t(binom[j] >> 32);
+                    val = val + to_mont(cj) * d[0];
+                }
+            }
+            acc = acc + coefs[p] * val;
+        }
+        out[x] = from_mont(acc);
+    }
 }
 
 __global__ void k_sumcheck_final_fold(FrPtrList tables, int count, Fr r, Fr *out) {
@@ -408,7 +422,7 @@ static void enqueue_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, cons
         check_launch();
     }
     ctx->prof_end(tok, st);
-    k_sumcheck_finalize<<<1, 256, 256 * sizeof(Fr), st>>>(d, partials.as<Fr>(), int(grid),
+    k_sumcheck_finalize<<<1, 256, size_t(d.slot_count) * sizeof(Fr), st>>>(d, partials.as<Fr>(), int(grid),
                                                            static_cast<const Fr *>(s->coefs), int(s->max_degree),
                                                            sums.as<Fr>(), out_dev);
     check_launch();

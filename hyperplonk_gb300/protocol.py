@@ -16,6 +16,7 @@ Values: Fr as ints, G1 as (x, y) / None, MLEs as backend handles.
 """
 from __future__ import annotations
 
+import time
 from dataclasses import dataclass, field
 
 from . import serialize as ser
@@ -85,6 +86,43 @@ def sumcheck_prove(backend, poly: VirtualPolynomial, transcript, final_evaluatio
     return IOPProof(point, msgs)
 
 
+def batch_sumcheck_prove(backend, polys: list, transcripts: list, final_evaluations: list | None = None) -> list:
+    """Independent sumcheck proofs of `polys` (uneven num_vars allowed), each
+    under its own transcript, advanced in lockstep: round k of every instance
+    still running goes to the device in one batch_prove_round call.  Each
+    proof equals sumcheck_prove(backend, polys[i], transcripts[i]); with
+    `final_evaluations` a list, one list of final factor values per instance
+    is appended to it."""
+    if len(polys) != len(transcripts):
+        raise InvalidParameters("one transcript per polynomial")
+    for p in polys:
+        if p.aux_info.num_variables == 0 or p.aux_info.max_degree == 0:
+            raise PolyIOPError("SumCheck requires positive variable count and degree.")
+    for p, t in zip(polys, transcripts):
+        t.append_serializable_element(b"aux info", ser.aux_info(p.aux_info.max_degree, p.aux_info.num_variables))
+    states = [backend.prover_init(p) for p in polys]
+    nvs = [p.aux_info.num_variables for p in polys]
+    challenges = [None] * len(polys)
+    msgs = [[] for _ in polys]
+    points = [[] for _ in polys]
+    batched = hasattr(backend, "batch_prove_round")
+    for rnd in range(max(nvs, default=0)):
+        live = [i for i, nv in enumerate(nvs) if rnd < nv]
+        if batched:
+            out = backend.batch_prove_round([states[i] for i in live], [challenges[i] for i in live])
+        else:
+            out = [backend.prove_round_and_update_state(states[i], challenges[i]) for i in live]
+        for i, msg in zip(live, out):
+            transcripts[i].append_serializable_element(b"prover msg", ser.vec_fr(msg))
+            msgs[i].append(msg)
+            challenges[i] = transcripts[i].get_and_append_challenge(b"Internal round")
+            points[i].append(challenges[i])
+    if final_evaluations is not None:
+        for s, c in zip(states, challenges):
+            final_evaluations.append(backend.final_evaluations(s, c))
+    return [IOPProof(pt, m) for pt, m in zip(points, msgs)]
+
+
 def zerocheck_prove(backend, poly: VirtualPolynomial, transcript) -> IOPProof:
     r = transcript.get_and_append_challenge_vectors(b"0check r", poly.aux_info.num_variables)
     eq = backend.build_eq_x_r(r)
@@ -136,6 +174,25 @@ def permcheck_prove(backend, pcs_param, fxs, gxs, perms, transcript):
 # PCS batch opening
 # ---------------------------------------------------------------------------
 
+class PhaseClock:
+    """Adds the host wall time since the previous mark to phases[name]
+    (seconds); a no-op when `phases` is None."""
+
+    def __init__(self, phases: dict | None):
+        self.phases = phases
+        self.t = time.perf_counter()
+
+    def __call__(self, name: str) -> None:
+        if self.phases is None:
+            return
+        now = time.perf_counter()
+        self.phases[name] = self.phases.get(name, 0.0) + now - self.t
+        self.t = now
+
+    def restart(self) -> None:
+        self.t = time.perf_counter()
+
+
 def ceil_log2(k: int) -> int:
     """ark_std::log2: number of bits to index k items (0 for k <= 1)."""
     return 0 if k <= 1 else (k - 1).bit_length()
@@ -166,7 +223,8 @@ def eq_table(point) -> list:
     return out
 
 
-def multi_open(backend, pcs_param, polynomials, points, evals, transcript) -> BatchProof:
+def multi_open(backend, pcs_param, polynomials, points, evals, transcript, phases: dict | None = None) -> BatchProof:
+    mark = PhaseClock(phases)
     k = len(polynomials)
     if k == 0 or len(points) != k or len(evals) != k:
         raise InvalidParameters("batch polynomials, points, and evaluations must have equal nonzero lengths")
@@ -193,9 +251,12 @@ def multi_open(backend, pcs_param, polynomials, points, evals, transcript) -> Ba
     vp = VirtualPolynomial(nv)
     for g, e in zip(merged, tilde_eqs):
         vp.add_mle_list([g, e], 1)
+    mark("batch_open.merge")
     proof = sumcheck_prove(backend, vp, transcript)
+    mark("batch_open.sumcheck")
     a2 = proof.point
     coefs = [eq_eval(a2, pt) for pt in deduped]
     g_prime = backend.linear_combination(merged, coefs)
     g_prime_proof, _ = backend.open(pcs_param, g_prime, a2)
+    mark("batch_open.pcs_open")
     return BatchProof(proof, list(evals), g_prime_proof)

@@ -15,7 +15,8 @@ import numpy as np
 
 from . import serialize as ser
 from .errors import InvalidParameters
-from .protocol import BatchProof, IOPProof, ProductCheckProof, ceil_log2, multi_open, permcheck_prove, zerocheck_prove
+from .protocol import (BatchProof, IOPProof, PhaseClock, ProductCheckProof, ceil_log2, multi_open, permcheck_prove,
+                       zerocheck_prove)
 from .transcript import IOPTranscript
 from .virtual_polynomial import R_MODULUS, VirtualPolynomial
 
@@ -81,14 +82,18 @@ class PcsAccumulator:
         self.polynomials.append(poly)
         self.points.append(list(point))
 
-    def multi_open(self, backend, pcs_param, transcript) -> BatchProof:
-        return multi_open(backend, pcs_param, self.polynomials, self.points, self.evals, transcript)
+    def multi_open(self, backend, pcs_param, transcript, phases: dict | None = None) -> BatchProof:
+        return multi_open(backend, pcs_param, self.polynomials, self.points, self.evals, transcript, phases)
 
 
 def prove(backend, pk: ProvingKey, pub_input: list, witnesses: list, transcript_cls=IOPTranscript,
-          witness_mles: list | None = None) -> HyperPlonkProof:
+          witness_mles: list | None = None, phases: dict | None = None) -> HyperPlonkProof:
     """snark.rs:156-341.  `witnesses` are table packets (or already-resident
-    MLEs passed as `witness_mles`); `pub_input` the public values."""
+    MLEs passed as `witness_mles`); `pub_input` the public values.  When
+    `phases` is a dict, the host wall time of each prover phase (seconds) is
+    added to it; every phase ends on a host read of a device result, so the
+    phases partition the proof."""
+    mark = PhaseClock(phases)
     transcript = transcript_cls(b"hyperplonk")
     nv = pk.num_vars
     ell = ceil_log2(pk.num_pub_input)
@@ -97,14 +102,17 @@ def prove(backend, pk: ProvingKey, pub_input: list, witnesses: list, transcript_
     if witness_mles is None:
         witness_mles = [backend.mle_from_evaluations(nv, w) for w in witnesses]
     commits = backend.multi_commit(pk.pcs_param, witness_mles)
+    mark("witness_commit")
     for c in commits:
         transcript.append_serializable_element(b"w", ser.g1_compressed(c))
     # 2. gate zero-check
     fx = build_f(pk.gate, nv, pk.selector_oracles, witness_mles)
     zc = zerocheck_prove(backend, fx, transcript)
+    mark("gate_zerocheck")
     # 3. permutation check
     pc, prod_x, frac = permcheck_prove(backend, pk.pcs_param, witness_mles, witness_mles,
                                        pk.permutation_oracles, transcript)
+    mark("perm_check")
     pcp = pc.zero_check_proof.point
     p0 = [0] + pcp[:nv - 1]
     p1 = [1] + pcp[:nv - 1]
@@ -123,7 +131,9 @@ def prove(backend, pk: ProvingKey, pub_input: list, witnesses: list, transcript_
         acc.insert_poly_and_points(backend, s, zc.point)
     r_pi = transcript.get_and_append_challenge_vectors(b"r_pi", ell)
     acc.insert_poly_and_points(backend, witness_mles[0], r_pi + [0] * (nv - ell))
-    batch = acc.multi_open(backend, pk.pcs_param, transcript)
+    mark("evaluations")
+    batch = acc.multi_open(backend, pk.pcs_param, transcript, phases)
+    mark.restart()
     return HyperPlonkProof(commits, batch, zc, pc)
 
 
@@ -154,3 +164,18 @@ def vanilla_fixture(num_vars: int, seed: int, num_pub_input: int = 16):
         "fixture_vanilla_plonk")
     pub = [int.from_bytes(wit[0, 32 * i:32 * i + 32].tobytes(), "little") for i in range(min(num_pub_input, n))]
     return list(sel), list(wit), list(perm), pub
+
+
+def vanilla_witness(num_vars: int, circuit_seed: int, witness_seed: int) -> list:
+    """Witnesses [w1, w2, w3] of the vanilla_fixture(num_vars, circuit_seed)
+    circuit with w1, w2 drawn from fixture stream `witness_seed` (elements
+    [4N, 6N)) and w3 solving the gate; equal to that fixture's own witnesses
+    when the seeds are equal."""
+    from . import _native
+    from .errors import check_status
+    n = 1 << num_vars
+    wit = np.empty((3, 32 * n), dtype=np.uint8)
+    check_status(_native.load().hp_cuda_v1_fixture_vanilla_plonk_witness(
+        ctypes.c_uint64(circuit_seed), ctypes.c_uint64(witness_seed), num_vars,
+        wit.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))), "fixture_vanilla_plonk_witness")
+    return list(wit)

@@ -250,6 +250,14 @@ HpCudaStatus hp_cuda_v1_fixture_random_fr(uint64_t seed, uint64_t first, size_t 
  * tables back to back.  Host-only. */
 HpCudaStatus hp_cuda_v1_fixture_vanilla_plonk(uint64_t seed, size_t num_vars, uint8_t *selectors,
                                               uint8_t *witnesses, uint8_t *permutation);
+/* Another satisfying witness of the same circuit (serving workload: one
+ * circuit per num_vars, independent witnesses per request): selectors from
+ * stream `circuit_seed` as above, w1 and w2 from elements [4N, 5N) and
+ * [5N, 6N) of stream `witness_seed`, w3 solving the gate.  Writes the 3
+ * witness tables; equals the witnesses above when the seeds are equal.
+ * No counterpart in the reference.  Host-only. */
+HpCudaStatus hp_cuda_v1_fixture_vanilla_plonk_witness(uint64_t circuit_seed, uint64_t witness_seed,
+                                                      size_t num_vars, uint8_t *witnesses);
 /* Host Fiat-Shamir transcript used by the protocol drivers (Merlin 1.0 over
  * STROBE-128 / Keccak-f[1600]; the reference wraps merlin 3.0.0,
  * transcript/src/lib.rs:40-131).  Host-only, no device work. */

@@ -5,6 +5,7 @@ import random
 
 import pytest
 
+from hyperplonk_gb300 import protocol
 from hyperplonk_gb300.errors import InvalidState
 from hyperplonk_gb300.virtual_polynomial import VirtualPolynomial
 
@@ -55,3 +56,29 @@ def test_batch_sumcheck_rounds_match_oracle(gpu, cpu, oracle):
     # misuse in a batch leaves every state unchanged
     with pytest.raises(InvalidState):
         gpu.batch_prove_round([sg[0]], [None])
+
+
+def test_batch_workload_batched_equals_plain_and_oracle(gpu, cpu, oracle):
+    """The batch plan's shape at small sizes (MSMs 2^4..2^10 on a nv=10 SRS,
+    sumchecks of 3..8 variables): the batched run (one batch_msm call, rounds
+    in lockstep) equals the plain one-at-a-time run and the oracle's
+    per-instance results."""
+    import transcript_ref as tref
+    from hyperplonk_gb300 import workloads
+    from hyperplonk_gb300.transcript import IOPTranscript
+    nv_srs = 10
+    layers = oracle.srs_layers(nv_srs, 5)
+    pg = gpu.prepare_prover_param(nv_srs, [oracle.affine_to_packets(l) for l in layers])
+    ks, nvs = workloads.batch_plan(3, msm_count=10, msm_k=(4, nv_srs), sumcheck_count=6, sumcheck_nv=(3, 8))
+    wl = workloads.BatchWorkload(gpu, pg, ks, nvs)
+    batched = wl.run_batched(IOPTranscript)
+    plain = wl.run_plain(IOPTranscript)
+    assert batched == plain
+    commits, sumchecks = batched
+    for k, s, got in zip(ks, workloads.batch_msm_scalars(ks), commits):
+        assert got == oracle.affine_to_point(oracle.msm(layers[0][:96 * (1 << k)], s.tobytes()))
+    ref = workloads.BatchWorkload(cpu, None, [], nvs)
+    for i, (vp, (proof, finals)) in enumerate(zip(ref.polynomials(), sumchecks)):
+        fc = []
+        pc = protocol.sumcheck_prove(cpu, vp, tref.OracleIOPTranscript(workloads.SUMCHECK_LABEL), fc)
+        assert (proof, finals) == (pc, fc), i

@@ -30,6 +30,18 @@ def test_fixture_satisfies_the_gate(native_lib):
     assert pub == w1[:16]
 
 
+def test_request_witnesses_satisfy_the_same_circuit(native_lib):
+    nv = 5
+    sel, wit, _, _ = snark.vanilla_fixture(nv, 2)
+    assert all((a == b).all() for a, b in zip(snark.vanilla_witness(nv, 2, 2), wit))
+    ql, qr, qo, qm, qc = (ints(s) for s in sel)
+    for seed in (4 << 32, (4 << 32) + 1):
+        w1, w2, w3 = (ints(w) for w in snark.vanilla_witness(nv, 2, seed))
+        assert w1 != ints(wit[0])
+        for i in range(1 << nv):
+            assert (ql[i] * w1[i] + qr[i] * w2[i] + qo[i] * w3[i] + qm[i] * w1[i] * w2[i] + qc[i]) % R == 0
+
+
 def oracle_prove(oracle, nv, seed, num_pub=16):
     import transcript_ref as tref
     cpu = oracle.CpuBackend()
