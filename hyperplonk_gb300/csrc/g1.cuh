@@ -44,17 +44,20 @@ __device__ __forceinline__ Xyzz xyzz_from_affine(const Affine &a) {
     return r;
 }
 
+// Independent products are issued in pairs (mul2), so the two multiply
+// chains of each pair interleave.
+
 // mdbl-2008-s-1: 2 * (x, y) for an affine input.
 __device__ __forceinline__ Xyzz xyzz_double_affine(const Fq &x, const Fq &y) {
     Fq u = y + y;
-    Fq v = u * u;
-    Fq w = u * v;
-    Fq s = x * v;
-    Fq xx = x * x;
+    Fq v, xx, w, s, mm, wy;
+    mul2(v, xx, u, u, x, x);
+    mul2(w, s, u, v, x, v);
     Fq m = xx + xx + xx;
+    mul2(mm, wy, m, m, w, y);
     Xyzz r;
-    r.x = m * m - (s + s);
-    r.y = m * (s - r.x) - w * y;
+    r.x = mm - (s + s);
+    r.y = m * (s - r.x) - wy;
     r.zz = v;
     r.zzz = w;
     return r;
@@ -64,16 +67,17 @@ __device__ __forceinline__ Xyzz xyzz_double_affine(const Fq &x, const Fq &y) {
 __device__ __forceinline__ Xyzz xyzz_double(const Xyzz &p) {
     if (xyzz_is_inf(p)) return p;
     Fq u = p.y + p.y;
-    Fq v = u * u;
-    Fq w = u * v;
-    Fq s = p.x * v;
-    Fq xx = p.x * p.x;
+    Fq v, xx, w, s, mm, zzz, t1, t2;
+    mul2(v, xx, u, u, p.x, p.x);
+    mul2(w, s, u, v, p.x, v);
     Fq m = xx + xx + xx;
+    mul2(mm, zzz, m, m, w, p.zzz);
     Xyzz r;
-    r.x = m * m - (s + s);
-    r.y = m * (s - r.x) - w * p.y;
+    r.x = mm - (s + s);
+    mul2(t1, t2, m, s - r.x, w, p.y);
+    r.y = t1 - t2;
     r.zz = v * p.zz;
-    r.zzz = w * p.zzz;
+    r.zzz = zzz;
     return r;
 }
 
@@ -87,22 +91,22 @@ __device__ __forceinline__ Xyzz xyzz_add_affine(const Xyzz &p, const Fq &x2, con
         r.zzz = Fq::one();
         return r;
     }
-    Fq u2 = x2 * p.zz;
-    Fq s2 = y2 * p.zzz;
+    Fq u2, s2;
+    mul2(u2, s2, x2, p.zz, y2, p.zzz);
     Fq pp_ = u2 - p.x;
     Fq rr = s2 - p.y;
     if (pp_.is_zero()) {
         if (rr.is_zero()) return xyzz_double_affine(x2, y2);
         return xyzz_inf();
     }
-    Fq pp = pp_ * pp_;
-    Fq ppp = pp_ * pp;
-    Fq q = p.x * pp;
+    Fq pp, r2, ppp, q, t1, t2;
+    mul2(pp, r2, pp_, pp_, rr, rr);
+    mul2(ppp, q, pp_, pp, p.x, pp);
     Xyzz r;
-    r.x = rr * rr - ppp - (q + q);
-    r.y = rr * (q - r.x) - p.y * ppp;
-    r.zz = p.zz * pp;
-    r.zzz = p.zzz * ppp;
+    r.x = r2 - ppp - (q + q);
+    mul2(r.zz, r.zzz, p.zz, pp, p.zzz, ppp);
+    mul2(t1, t2, rr, q - r.x, p.y, ppp);
+    r.y = t1 - t2;
     return r;
 }
 
@@ -110,24 +114,24 @@ __device__ __forceinline__ Xyzz xyzz_add_affine(const Xyzz &p, const Fq &x2, con
 __device__ __forceinline__ Xyzz xyzz_add(const Xyzz &p, const Xyzz &q) {
     if (xyzz_is_inf(p)) return q;
     if (xyzz_is_inf(q)) return p;
-    Fq u1 = p.x * q.zz;
-    Fq u2 = q.x * p.zz;
-    Fq s1 = p.y * q.zzz;
-    Fq s2 = q.y * p.zzz;
+    Fq u1, u2, s1, s2;
+    mul2(u1, u2, p.x, q.zz, q.x, p.zz);
+    mul2(s1, s2, p.y, q.zzz, q.y, p.zzz);
     Fq pp_ = u2 - u1;
     Fq rr = s2 - s1;
     if (pp_.is_zero()) {
         if (rr.is_zero()) return xyzz_double(p);
         return xyzz_inf();
     }
-    Fq pp = pp_ * pp_;
-    Fq ppp = pp_ * pp;
-    Fq qq = u1 * pp;
+    Fq pp, r2, ppp, qq, zz, zzz, t1, t2;
+    mul2(pp, r2, pp_, pp_, rr, rr);
+    mul2(ppp, qq, pp_, pp, u1, pp);
+    mul2(zz, zzz, p.zz, q.zz, p.zzz, q.zzz);
     Xyzz r;
-    r.x = rr * rr - ppp - (qq + qq);
-    r.y = rr * (qq - r.x) - s1 * ppp;
-    r.zz = p.zz * q.zz * pp;
-    r.zzz = p.zzz * q.zzz * ppp;
+    r.x = r2 - ppp - (qq + qq);
+    mul2(r.zz, r.zzz, zz, pp, zzz, ppp);
+    mul2(t1, t2, rr, qq - r.x, s1, ppp);
+    r.y = t1 - t2;
     return r;
 }
 

@@ -23,7 +23,6 @@
 //  5. the host finishes the short Horner chain over those subset sums and
 //     converts to affine (one inversion), see host_ec.h.
 #include <algorithm>
-#include <atomic>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -433,31 +432,29 @@ __global__ void k_msm_scatter(const Fr *scalars, const Fr *delta, size_t n, size
 #define HP_ACC_MINBLOCKS 3  // measured best on GB300 at 2^20 (13.9 ms vs 14.2 ms at 1)
 #endif
 
-// Chunk length L: the grid is exactly the resident blocks of k_msm_accumulate
-// and every thread takes the same number k of chunks, so there is no partial
-// last wave; k is the whole number of chunks per thread that puts L nearest
-// 64 records (fewer, longer chunks cut fewer buckets).  L stays in [16, 256].
+// Chunk length L = 32 records per thread, one block per 128 chunks, blocks
+// scheduled dynamically (measured at 2^20 points, c = 20: L = 32 9.56 ms per
+// MSM, 48 9.70, 64 9.60, 96 10.33; a grid of exactly the resident blocks with
+// L near 64 9.81).
+constexpr uint32_t kChunkRecords = 32;
+
 struct AccumulateGeometry {
     uint32_t chunk;   // records per chunk (L)
     size_t chunks;    // ceil(records / L)
     unsigned grid;    // blocks of 128 threads
 };
 
-static int accumulate_blocks_per_sm();
-
-AccumulateGeometry accumulate_geometry(const HpCudaContext *ctx, size_t records) {
-    const size_t resident = size_t(ctx->sm_count > 0 ? ctx->sm_count : 152) * accumulate_blocks_per_sm() * 128;
-    const size_t per_wave = resident * 64;
-    size_t k = (records + per_wave / 2) / per_wave;
-    if (k == 0) k = 1;
-    size_t L = (records + resident * k - 1) / (resident * k);
-    if (L < 16) L = 16;
-    if (L > 256) L = 256;
+AccumulateGeometry accumulate_geometry(size_t records) {
+    size_t L = kChunkRecords;
+    // tuning override: HP_ACC_CHUNK=L (8 <= L <= 1024)
+    if (const char *env = std::getenv("HP_ACC_CHUNK")) {
+        const long v = std::atol(env);
+        if (v >= 8 && v <= 1024) L = size_t(v);
+    }
     AccumulateGeometry g;
     g.chunk = uint32_t(L);
     g.chunks = (records + L - 1) / L;
-    g.grid = unsigned(std::min<size_t>((g.chunks + 127) / 128, resident / 128));
-    if (g.grid == 0) g.grid = 1;
+    g.grid = unsigned(std::max<size_t>(1, (g.chunks + 127) / 128));
     return g;
 }
 
@@ -502,17 +499,6 @@ __global__ void __launch_bounds__(128, HP_ACC_MINBLOCKS) k_msm_accumulate(const 
             acc = xyzz_add_affine(acc, a.x, a.y);
         }
     }
-}
-
-static int accumulate_blocks_per_sm() {
-    static std::atomic<int> cached{0};
-    int v = cached.load(std::memory_order_relaxed);
-    if (v > 0) return v;
-    int blocks = 0;
-    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_msm_accumulate, 128, 0));
-    v = blocks > 0 ? blocks : 1;
-    cached.store(v, std::memory_order_relaxed);
-    return v;
 }
 
 // Buckets cut by chunk boundaries: add their pieces; empty buckets: infinity.
@@ -626,7 +612,7 @@ void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz 
     k_msm_scatter<<<grid_for(ctx, n, 256), 256, 0, st>>>(scalars, layer.delta, n, layer.n, layer.c, layer.windows,
                                                         cursor.as<uint32_t>(), recs.as<uint32_t>());
     check_launch();
-    const AccumulateGeometry geo = accumulate_geometry(ctx, records);
+    const AccumulateGeometry geo = accumulate_geometry(records);
     Scratch pieces(ctx, std::max<size_t>(2 * geo.chunks, 1) * sizeof(Xyzz), st);
     int tok = ctx->prof_begin("msm_accumulate", st);
     k_msm_accumulate<<<geo.grid, 128, 0, st>>>(layer.bases, offsets.as<uint32_t>(), recs.as<uint32_t>(),
