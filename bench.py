@@ -759,9 +759,11 @@ def cpu_baseline(workload: str, nv: int) -> dict:
 
 def _profile_traffic(nv: int):
     """DRAM bytes per k_msm_accumulate launch from the committed ncu summary
-    (profiles/msm_accumulate.md, line 'traffic_bytes_per_launch nv=<k>: <bytes>'),
-    scaled by the point count when captured at a smaller size; None if absent."""
-    p = ROOT / "profiles" / "msm_accumulate.md"
+    (profiles/msm_accumulate_commit.md, line 'traffic_bytes_per_launch nv=<k>:
+    <bytes>'), scaled to 2^nv points by the (point, window) record count --
+    each record reads one 96-byte base -- when captured at a smaller size;
+    None if absent."""
+    p = ROOT / "profiles" / "msm_accumulate_commit.md"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
@@ -769,7 +771,8 @@ def _profile_traffic(nv: int):
             try:
                 k = int(line.split("nv=")[1].split(":")[0])
                 b = float(line.split(":")[1].strip().split()[0])
-                return b * (1 << nv) / (1 << k)
+                rec = lambda v: math.ceil(256 / window_bits(1 << v)) * (1 << v)  # noqa: E731
+                return b * rec(nv) / rec(k)
             except (IndexError, ValueError):
                 return None
     return None

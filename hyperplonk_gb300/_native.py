@@ -53,6 +53,7 @@ SIGNATURES: dict[str, list] = {
     "hp_cuda_v1_batch_msm": [c_voidp, c_voidp, c_size, c_voidpp, c_sizep, c_size, c_u8p],
     "hp_cuda_v1_batch_sumcheck_round": [c_voidp, c_voidpp, c_voidpp, c_voidpp, c_sizep, c_size],
     "hp_cuda_v1_mle_evaluate_noalloc": [c_voidp, c_size, c_u8p, c_u8p, c_voidp],
+    "hp_cuda_v1_mle_evaluate_many": [c_voidp, c_size, c_voidpp, c_sizep, c_u8p, c_u8p],
     "hp_cuda_v1_context_profile": [c_voidp, ctypes.c_int32],
     "hp_cuda_v1_context_profile_read": [c_voidp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
                                         ctypes.POINTER(ctypes.c_uint64)],
@@ -67,6 +68,7 @@ SIGNATURES: dict[str, list] = {
     "hp_host_v1_merlin_clone": [c_voidp, c_voidpp],
     "hp_host_v1_merlin_free": [c_voidp],
     "hp_host_v1_keccak_f1600": [c_u8p],
+    "hp_cuda_v1_sumcheck_prove_rounds": [c_voidp, c_voidp, c_voidp, c_size, c_u8p, c_u8p],
 }
 
 _lib = None

@@ -271,6 +271,25 @@ class CudaBackend:
                                                       _native.buf(pt), out), "mle_evaluate")
         return decode_fr(bytes(out))
 
+    def evaluate_many(self, mles: Sequence[CudaMle], points: Sequence[Sequence[int]]) -> list[int]:
+        """evaluate_mle of every (mle, point) pair with one synchronisation."""
+        if len(mles) != len(points):
+            raise InvalidParameters("one point per polynomial")
+        if not mles:
+            return []
+        for m, pt in zip(mles, points):
+            self._check_mle(m)
+            if len(pt) != m.num_vars:
+                raise InvalidParameters(f"wrong number of variables {m.num_vars} vs {len(pt)}")
+        nvs = (ctypes.c_size_t * len(mles))(*[m.num_vars for m in mles])
+        flat = b"".join(encode_frs(pt) for pt in points)
+        out = (ctypes.c_uint8 * (32 * len(mles)))()
+        check_status(self.lib.hp_cuda_v1_mle_evaluate_many(self.ctx.raw, len(mles), _addr_array(mles), nvs,
+                                                           _native.buf(flat) if flat else None, out),
+                     "mle_evaluate_many")
+        raw = bytes(out)
+        return [decode_fr(raw[32 * i:32 * i + 32]) for i in range(len(mles))]
+
     def build_eq_x_r(self, r: Sequence[int]) -> CudaMle:
         if len(r) == 0:
             raise InvalidParameters("r length is 0")
@@ -433,6 +452,20 @@ class CudaBackend:
                      "sumcheck_prover_state_round")
         raw = bytes(out)
         return [decode_fr(raw[32 * i:32 * i + 32]) for i in range(n)]
+
+    def prove_rounds(self, state: CudaSumCheckProverState, transcript, rounds: int):
+        """All rounds of a fresh state with the Fiat-Shamir step inside the
+        library: `transcript` is a native MerlinTranscript.  Returns (round
+        messages, challenges)."""
+        d1 = state.round_evaluation_count
+        msgs = (ctypes.c_uint8 * (32 * d1 * rounds))()
+        chs = (ctypes.c_uint8 * (32 * rounds))()
+        check_status(self.lib.hp_cuda_v1_sumcheck_prove_rounds(self.ctx.raw, state.raw, transcript.raw, rounds,
+                                                              msgs, chs), "sumcheck_prove_rounds")
+        mb, cb = bytes(msgs), bytes(chs)
+        messages = [[int.from_bytes(mb[32 * (d1 * k + j):32 * (d1 * k + j) + 32], "little") for j in range(d1)]
+                    for k in range(rounds)]
+        return messages, [int.from_bytes(cb[32 * k:32 * k + 32], "little") for k in range(rounds)]
 
     # ---- batched execution (no counterpart in the reference traits) ----
     def batch_msm(self, prover_param: CudaPreparedProverParam, layer_index: int, scalars: Sequence[CudaMle]):

@@ -274,6 +274,69 @@ __device__ __forceinline__ Field<P> mont_mul_wide(const Field<P> &a, const Field
     return r;
 }
 
+// Montgomery squaring, separated operand scanning: the 2N-limb square from
+// the N(N-1)/2 cross products (doubled by one shift) plus the N diagonal
+// squares -- (N^2 + N)/2 wide products instead of N^2 -- then N rows of
+// Montgomery reduction; the carry out of each row's top limb is held in c2
+// and added one limb higher in the next row.
+template <class P>
+__device__ __forceinline__ Field<P> mont_sqr_wide(const Field<P> &a) {
+    constexpr int N = P::N;
+    uint32_t T[2 * N];
+#pragma unroll
+    for (int i = 0; i < 2 * N; i++) T[i] = 0;
+#pragma unroll
+    for (int i = 0; i < N - 1; i++) {
+        uint32_t carry = 0;
+#pragma unroll
+        for (int j = i + 1; j < N; j++) {
+            const uint64_t d = uint64_t(a.v[i]) * a.v[j] + (uint64_t(T[i + j]) + carry);
+            T[i + j] = uint32_t(d);
+            carry = uint32_t(d >> 32);
+        }
+        T[i + N] = carry;
+    }
+    // T = 2 T (cross products < 2^(64N - 1), so no bit is lost)
+#pragma unroll
+    for (int k = 2 * N - 1; k > 0; k--) T[k] = (T[k] << 1) | (T[k - 1] >> 31);
+    T[0] <<= 1;
+    // + diagonal squares a_i^2 at limb 2i
+    {
+        uint32_t dg[2 * N];
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            const uint64_t d = uint64_t(a.v[i]) * a.v[i];
+            dg[2 * i] = uint32_t(d);
+            dg[2 * i + 1] = uint32_t(d >> 32);
+        }
+        T[0] = add_cc(T[0], dg[0]);
+#pragma unroll
+        for (int k = 1; k < 2 * N; k++) T[k] = addc_cc(T[k], dg[k]);
+    }
+    uint32_t c2 = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const uint32_t m = T[i] * P::INV;
+        uint32_t carry = 0;
+#pragma unroll
+        for (int j = 0; j < N; j++) {
+            const uint64_t d = uint64_t(m) * P::p(j) + (uint64_t(T[i + j]) + carry);
+            T[i + j] = uint32_t(d);
+            carry = uint32_t(d >> 32);
+        }
+        // T[i+N] += carry + c2 (c2: carries still owed to limb i+N)
+        T[i + N] = add_cc(T[i + N], carry);
+        uint32_t c = addc(0, 0);
+        T[i + N] = add_cc(T[i + N], c2);
+        c2 = addc(c, 0);
+    }
+    Field<P> r;
+#pragma unroll
+    for (int i = 0; i < N; i++) r.v[i] = T[N + i];
+    reduce_once<P>(r, c2);
+    return r;
+}
+
 struct FqPair;
 
 // The 12-limb product is ~700 SASS instructions; inlined at every call site
@@ -334,8 +397,26 @@ __device__ __forceinline__ void mul2(Field<FqParams> &x, Field<FqParams> &y, con
 #endif
 }
 
+// Fq squaring: HP_FQ_SQR=0 multiplies (a * a), 1 calls an out-of-line
+// squaring, 2 inlines it.
+#ifndef HP_FQ_SQR
+#define HP_FQ_SQR 0
+#endif
+#if HP_FQ_SQR == 1 && !defined(HP_FQ_INLINE)
+static __device__ __noinline__ Field<FqParams> fq_sqr_call(Field<FqParams> a) {
+    return mont_sqr_wide<FqParams>(a);
+}
+#endif
+
 template <class P>
 __device__ __forceinline__ Field<P> sqr(const Field<P> &a) {
+    if constexpr (P::N == 12) {
+#if HP_FQ_SQR == 1 && !defined(HP_FQ_INLINE)
+        return fq_sqr_call(a);
+#elif HP_FQ_SQR >= 1
+        return mont_sqr_wide<P>(a);
+#endif
+    }
     return a * a;
 }
 

@@ -50,11 +50,11 @@ __device__ __forceinline__ Xyzz xyzz_from_affine(const Affine &a) {
 // mdbl-2008-s-1: 2 * (x, y) for an affine input.
 __device__ __forceinline__ Xyzz xyzz_double_affine(const Fq &x, const Fq &y) {
     Fq u = y + y;
-    Fq v, xx, w, s, mm, wy;
-    mul2(v, xx, u, u, x, x);
+    Fq v = sqr(u), xx = sqr(x), w, s, wy;
     mul2(w, s, u, v, x, v);
     Fq m = xx + xx + xx;
-    mul2(mm, wy, m, m, w, y);
+    Fq mm = sqr(m);
+    wy = w * y;
     Xyzz r;
     r.x = mm - (s + s);
     r.y = m * (s - r.x) - wy;
@@ -67,11 +67,10 @@ __device__ __forceinline__ Xyzz xyzz_double_affine(const Fq &x, const Fq &y) {
 __device__ __forceinline__ Xyzz xyzz_double(const Xyzz &p) {
     if (xyzz_is_inf(p)) return p;
     Fq u = p.y + p.y;
-    Fq v, xx, w, s, mm, zzz, t1, t2;
-    mul2(v, xx, u, u, p.x, p.x);
+    Fq v = sqr(u), xx = sqr(p.x), w, s, t1, t2;
     mul2(w, s, u, v, p.x, v);
     Fq m = xx + xx + xx;
-    mul2(mm, zzz, m, m, w, p.zzz);
+    Fq mm = sqr(m), zzz = w * p.zzz;
     Xyzz r;
     r.x = mm - (s + s);
     mul2(t1, t2, m, s - r.x, w, p.y);
@@ -99,8 +98,7 @@ __device__ __forceinline__ Xyzz xyzz_add_affine(const Xyzz &p, const Fq &x2, con
         if (rr.is_zero()) return xyzz_double_affine(x2, y2);
         return xyzz_inf();
     }
-    Fq pp, r2, ppp, q, t1, t2;
-    mul2(pp, r2, pp_, pp_, rr, rr);
+    Fq pp = sqr(pp_), r2 = sqr(rr), ppp, q, t1, t2;
     mul2(ppp, q, pp_, pp, p.x, pp);
     Xyzz r;
     r.x = r2 - ppp - (q + q);
@@ -123,8 +121,7 @@ __device__ __forceinline__ Xyzz xyzz_add(const Xyzz &p, const Xyzz &q) {
         if (rr.is_zero()) return xyzz_double(p);
         return xyzz_inf();
     }
-    Fq pp, r2, ppp, qq, zz, zzz, t1, t2;
-    mul2(pp, r2, pp_, pp_, rr, rr);
+    Fq pp = sqr(pp_), r2 = sqr(rr), ppp, qq, zz, zzz, t1, t2;
     mul2(ppp, qq, pp_, pp, u1, pp);
     mul2(zz, zzz, p.zz, q.zz, p.zzz, q.zzz);
     Xyzz r;

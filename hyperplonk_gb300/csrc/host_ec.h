@@ -11,6 +11,7 @@
 #pragma once
 #include <cstdint>
 #include <cstring>
+#include <vector>
 
 namespace hp {
 namespace host {
@@ -181,6 +182,35 @@ inline void xyzz_to_packet(const Xyzz64 &p, uint8_t *out97) {
     Fq64 y = fq_mul(p.y, fq_mul(inv, p.zz));
     fq_to_canonical(x, out97 + 1);
     fq_to_canonical(y, out97 + 49);
+}
+
+// Many points to packets with one inversion (Montgomery's trick over the
+// finite points' ZZ * ZZZ); equal to xyzz_to_packet point by point.
+inline void xyzz_to_packets(const Xyzz64 *p, size_t n, uint8_t *out97) {
+    std::vector<Fq64> prefix(n);
+    Fq64 acc = fq_one();
+    bool any = false;
+    for (size_t i = 0; i < n; i++) {
+        prefix[i] = acc;
+        if (!xyzz_is_inf(p[i])) {
+            acc = fq_mul(acc, fq_mul(p[i].zz, p[i].zzz));
+            any = true;
+        }
+    }
+    Fq64 inv = any ? fq_inverse(acc) : acc;
+    for (size_t i = n; i-- > 0;) {
+        uint8_t *o = out97 + 97 * i;
+        std::memset(o, 0, 97);
+        if (xyzz_is_inf(p[i])) {
+            o[0] = 1;
+            continue;
+        }
+        const Fq64 v = fq_mul(p[i].zz, p[i].zzz);
+        const Fq64 vinv = fq_mul(inv, prefix[i]);  // (zz zzz)^-1
+        inv = fq_mul(inv, v);
+        fq_to_canonical(fq_mul(p[i].x, fq_mul(vinv, p[i].zzz)), o + 1);
+        fq_to_canonical(fq_mul(p[i].y, fq_mul(vinv, p[i].zz)), o + 49);
+    }
 }
 
 }  // namespace host

@@ -64,11 +64,14 @@ static void finish_msms(HpCudaContext *ctx, const Xyzz *dev, const std::vector<c
     if (total)
         check_cuda(cudaMemcpyAsync(hostp.data(), dev, total * sizeof(Xyzz), cudaMemcpyDeviceToHost, ctx->stream));
     ctx->sync();
+    // every result's Horner chain, then one inversion for all affine conversions
+    std::vector<host::Xyzz64> results(shapes.size());
     size_t off = 0;
     for (size_t i = 0; i < shapes.size(); i++) {
-        msm_finalize_host(*layers[i], hostp.data() + off, out97 + 97 * i);
+        results[i] = msm_result_host(*layers[i], hostp.data() + off);
         off += size_t(shapes[i].partials);
     }
+    host::xyzz_to_packets(results.data(), results.size(), out97);
 }
 
 }  // namespace hp

@@ -67,11 +67,13 @@ __global__ void k_fold(const Fr *src, Fr *dst, size_t half, Fr r) {
     }
 }
 
-// Fold the last `levels` variables of a table of 2^levels entries in one block
-// (levels <= 10, 32 KiB), shared-memory resident; writes the single result.
+// Block b folds `levels` variables (levels <= 10, 32 KiB) of the 2^levels
+// entries src[b 2^levels ..] in shared memory and writes the value to dst[b].
 __global__ void k_fold_tail(const Fr *src, Fr *dst, int levels, FrScalarList r) {
     extern __shared__ Fr sm[];
     size_t n = size_t(1) << levels;
+    src += size_t(blockIdx.x) << levels;
+    dst += blockIdx.x;
     for (size_t i = threadIdx.x; i < n; i += blockDim.x) sm[i] = load_fr(&src[i]);
     __syncthreads();
     for (int l = 0; l < levels; l++) {
@@ -307,7 +309,8 @@ void download_canonical(HpCudaContext *ctx, const Fr *src, size_t n, uint8_t *ou
 }
 
 void fold_to_scalar(HpCudaContext *ctx, const Fr *table, size_t nv, const Fr *point, Fr *dst) {
-    // Levels above the tail fold through global ping-pong buffers.
+    // Ten variables per pass: block b folds entries [b 2^10, (b+1) 2^10) in
+    // shared memory (one launch per ten variables instead of one per variable).
     constexpr int kTail = 10;
     if (nv == 0) {
         check_cuda(cudaMemcpyAsync(dst, table, sizeof(Fr), cudaMemcpyDeviceToDevice, ctx->stream));
@@ -317,18 +320,20 @@ void fold_to_scalar(HpCudaContext *ctx, const Fr *table, size_t nv, const Fr *po
     const Fr *cur = table;
     size_t level = 0;
     if (nv > kTail) {
-        a = Scratch(ctx, table_len(nv - 1) * sizeof(Fr));
-        b = Scratch(ctx, table_len(nv - 2) * sizeof(Fr));
+        a = Scratch(ctx, table_len(nv - kTail) * sizeof(Fr));
+        b = Scratch(ctx, table_len(nv > 2 * kTail ? nv - 2 * kTail : 0) * sizeof(Fr));
         Fr *bufs[2] = {a.as<Fr>(), b.as<Fr>()};
         int which = 0;
         while (nv - level > size_t(kTail)) {
-            size_t half = table_len(nv - level - 1);
+            const size_t blocks = table_len(nv - level - kTail);
+            FrScalarList r;
+            for (int l = 0; l < kTail; l++) r.s[l] = point[level + l];
             Fr *dstb = bufs[which];
-            k_fold<<<grid_for(ctx, half, 256), 256, 0, ctx->stream>>>(cur, dstb, half, point[level]);
+            k_fold_tail<<<unsigned(blocks), 512, table_len(kTail) * sizeof(Fr), ctx->stream>>>(cur, dstb, kTail, r);
             check_launch();
             cur = dstb;
             which ^= 1;
-            level++;
+            level += kTail;
         }
     }
     int rest = int(nv - level);
@@ -478,6 +483,31 @@ extern "C" HpCudaStatus hp_cuda_v1_mle_evaluate(HpCudaContext *ctx, HpCudaDevice
         Scratch res(ctx, sizeof(Fr));
         hp::fold_to_scalar(ctx, table, num_vars, pt.data(), res.as<Fr>());
         hp::download_canonical(ctx, res.as<Fr>(), 1, out_evaluation);
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_mle_evaluate_many(HpCudaContext *ctx, size_t count,
+                                                     const HpCudaDeviceAddress *polynomials,
+                                                     const size_t *num_vars, const uint8_t *points,
+                                                     uint8_t *out_evaluations) {
+    return guard([&] {
+        hp::require_ctx(ctx);
+        if (count == 0) return;
+        require(polynomials != nullptr && num_vars != nullptr && out_evaluations != nullptr);
+        std::vector<const Fr *> tables(count);
+        std::vector<std::vector<Fr>> pts(count);
+        size_t off = 0;
+        for (size_t k = 0; k < count; k++) {
+            tables[k] = hp::mle_ptr(ctx, polynomials[k], num_vars[k]);
+            require(num_vars[k] == 0 || points != nullptr);
+            pts[k].resize(num_vars[k]);
+            for (size_t i = 0; i < num_vars[k]; i++) pts[k][i] = hp::host_scalar(points + 32 * (off + i));
+            off += num_vars[k];
+        }
+        Scratch res(ctx, count * sizeof(Fr));
+        for (size_t k = 0; k < count; k++)
+            hp::fold_to_scalar(ctx, tables[k], num_vars[k], pts[k].data(), res.as<Fr>() + k);
+        hp::download_canonical(ctx, res.as<Fr>(), count, out_evaluations);
     });
 }
 

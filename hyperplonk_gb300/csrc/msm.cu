@@ -59,7 +59,10 @@ int msm_window_bits(size_t n) {
 MsmShape msm_shape(const MsmLayer &layer) {
     MsmShape s;
     s.buckets = size_t(1) << (layer.c - 1);
-    s.seg = s.buckets >= 16 ? 16 : s.buckets;
+    // 16-bucket segments once there are >= 2^16 buckets (thread count is not
+    // the limit there); shorter segments below, because a segment is a chain
+    // of 2 seg dependent additions and small MSMs are latency-bound
+    s.seg = std::min<size_t>(16, std::max<size_t>(1, s.buckets >> 12));
     s.segments = s.buckets / s.seg;
     s.seg_bits = 0;
     while ((size_t(1) << s.seg_bits) < s.segments) s.seg_bits++;
@@ -435,7 +438,10 @@ __global__ void k_msm_scatter(const Fr *scalars, const Fr *delta, size_t n, size
 // Chunk length L = 32 records per thread, one block per 128 chunks, blocks
 // scheduled dynamically (measured at 2^20 points, c = 20: L = 32 9.56 ms per
 // MSM, 48 9.70, 64 9.60, 96 10.33; a grid of exactly the resident blocks with
-// L near 64 9.81).
+// L near 64 9.81).  A chunk is a chain of L dependent mixed additions, so an
+// MSM too small to give every SM eight blocks of 32-record chunks uses
+// shorter chunks (down to 2); when it also has few buckets (<= 8192), each
+// cut bucket's pieces are summed by a warp.
 constexpr uint32_t kChunkRecords = 32;
 
 struct AccumulateGeometry {
@@ -444,8 +450,9 @@ struct AccumulateGeometry {
     unsigned grid;    // blocks of 128 threads
 };
 
-AccumulateGeometry accumulate_geometry(size_t records) {
-    size_t L = kChunkRecords;
+AccumulateGeometry accumulate_geometry(const HpCudaContext *ctx, size_t records) {
+    const size_t threads = size_t(ctx->sm_count > 0 ? ctx->sm_count : 152) * 8 * 128;
+    size_t L = std::min<size_t>(kChunkRecords, std::max<size_t>(2, (records + threads - 1) / threads));
     // tuning override: HP_ACC_CHUNK=L (8 <= L <= 1024)
     if (const char *env = std::getenv("HP_ACC_CHUNK")) {
         const long v = std::atol(env);
@@ -518,6 +525,43 @@ __global__ void k_msm_bucket_fixup(const uint32_t *offsets, uint32_t buckets, ui
     }
 }
 
+// The same with a warp per bucket (short chunks: many pieces per bucket):
+// lane i sums pieces i, i + 32, ..., then a shuffle tree of 5 additions.
+__device__ __forceinline__ Xyzz shfl_down_xyzz(const Xyzz &p, int off) {
+    Xyzz r;
+#pragma unroll
+    for (int i = 0; i < 12; i++) {
+        r.x.v[i] = __shfl_down_sync(0xffffffffu, p.x.v[i], off);
+        r.y.v[i] = __shfl_down_sync(0xffffffffu, p.y.v[i], off);
+        r.zz.v[i] = __shfl_down_sync(0xffffffffu, p.zz.v[i], off);
+        r.zzz.v[i] = __shfl_down_sync(0xffffffffu, p.zzz.v[i], off);
+    }
+    return r;
+}
+
+__global__ void __launch_bounds__(128) k_msm_bucket_fixup_warp(const uint32_t *offsets, uint32_t buckets,
+                                                               uint32_t chunk, const Xyzz *pieces,
+                                                               Xyzz *bucket_sums) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); b < buckets; b += warps) {
+        const uint32_t begin = offsets[b], end = offsets[b + 1];
+        if (begin == end) {
+            if (lane == 0) store_xyzz(&bucket_sums[b], xyzz_inf());
+            continue;
+        }
+        const uint32_t t0 = begin / chunk, t1 = (end - 1) / chunk;
+        if (t0 == t1) continue;  // warp-uniform
+        // piece k = 0 is [2 t0 + 1], piece k >= 1 is [2 (t0 + k)]
+        Xyzz acc = xyzz_inf();
+        for (uint32_t k = lane; k <= t1 - t0; k += 32)
+            acc = xyzz_add(acc, load_xyzz(&pieces[k == 0 ? 2 * size_t(t0) + 1 : 2 * (size_t(t0) + k)]));
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) acc = xyzz_add(acc, shfl_down_xyzz(acc, off));
+        if (lane == 0) store_xyzz(&bucket_sums[b], acc);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Bucket reduction
 // ---------------------------------------------------------------------------
@@ -544,16 +588,20 @@ constexpr int kSubsetThreads = 128;
 constexpr int kSubsetPerThread = 8;
 constexpr int kSubsetPerBlock = kSubsetThreads * kSubsetPerThread;
 
+// Blocks of T threads (a power of two <= kSubsetThreads), `per` elements per
+// thread: T * per = kSubsetPerBlock when there are several chunks; a single
+// chunk of few elements takes fewer threads and elements per thread (the
+// dependent-addition depth is per + log2 T).
 __global__ void __launch_bounds__(kSubsetThreads) k_msm_subsets(const Xyzz *run, const Xyzz *acc,
-                                                                size_t segments, int bits, int chunks,
+                                                                size_t segments, int bits, int chunks, int per,
                                                                 Xyzz *partial) {
     __shared__ Xyzz sm[kSubsetThreads];
-    const int y = blockIdx.y, t = threadIdx.x;
+    const int y = blockIdx.y, t = threadIdx.x, T = blockDim.x;
     const size_t count = y < bits ? segments / 2 : segments;
-    const size_t first = size_t(blockIdx.x) * kSubsetPerBlock;
+    const size_t first = size_t(blockIdx.x) * size_t(T) * per;
     Xyzz s = xyzz_inf();
-    for (int k = 0; k < kSubsetPerThread; k++) {
-        size_t e = first + size_t(k) * kSubsetThreads + t;
+    for (int k = 0; k < per; k++) {
+        size_t e = first + size_t(k) * T + t;
         if (e >= count) break;
         Xyzz v;
         if (y < bits) {
@@ -566,7 +614,7 @@ __global__ void __launch_bounds__(kSubsetThreads) k_msm_subsets(const Xyzz *run,
     }
     sm[t] = s;
     __syncthreads();
-    for (int half = kSubsetThreads / 2; half > 0; half >>= 1) {
+    for (int half = T / 2; half > 0; half >>= 1) {
         if (t < half) sm[t] = xyzz_add(sm[t], sm[t + half]);
         __syncthreads();
     }
@@ -612,15 +660,20 @@ void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz 
     k_msm_scatter<<<grid_for(ctx, n, 256), 256, 0, st>>>(scalars, layer.delta, n, layer.n, layer.c, layer.windows,
                                                         cursor.as<uint32_t>(), recs.as<uint32_t>());
     check_launch();
-    const AccumulateGeometry geo = accumulate_geometry(records);
+    const AccumulateGeometry geo = accumulate_geometry(ctx, records);
     Scratch pieces(ctx, std::max<size_t>(2 * geo.chunks, 1) * sizeof(Xyzz), st);
     int tok = ctx->prof_begin("msm_accumulate", st);
     k_msm_accumulate<<<geo.grid, 128, 0, st>>>(layer.bases, offsets.as<uint32_t>(), recs.as<uint32_t>(),
                                                uint32_t(B), geo.chunk, buckets.as<Xyzz>(), pieces.as<Xyzz>());
     check_launch();
     ctx->prof_end(tok, st);
-    k_msm_bucket_fixup<<<grid_for(ctx, B, 128, 8), 128, 0, st>>>(offsets.as<uint32_t>(), uint32_t(B), geo.chunk,
-                                                                pieces.as<Xyzz>(), buckets.as<Xyzz>());
+    // a warp per bucket only pays when buckets are few and cut into many pieces
+    if (geo.chunk == kChunkRecords || B > 8192)
+        k_msm_bucket_fixup<<<grid_for(ctx, B, 128, 8), 128, 0, st>>>(offsets.as<uint32_t>(), uint32_t(B), geo.chunk,
+                                                                    pieces.as<Xyzz>(), buckets.as<Xyzz>());
+    else
+        k_msm_bucket_fixup_warp<<<grid_for(ctx, 32 * B, 128, 8), 128, 0, st>>>(
+            offsets.as<uint32_t>(), uint32_t(B), geo.chunk, pieces.as<Xyzz>(), buckets.as<Xyzz>());
     check_launch();
     Scratch acc(ctx, sh.segments * sizeof(Xyzz), st), run(ctx, sh.segments * sizeof(Xyzz), st);
     k_msm_segments<<<grid_for(ctx, sh.segments, 128, 16), 128, 0, st>>>(buckets.as<Xyzz>(), sh.segments, sh.seg,
@@ -628,15 +681,19 @@ void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz 
     check_launch();
     const int chunks = int((sh.segments + kSubsetPerBlock - 1) / kSubsetPerBlock);
     if (chunks == 1) {
-        k_msm_subsets<<<dim3(1, sh.partials), kSubsetThreads, 0, st>>>(run.as<Xyzz>(), acc.as<Xyzz>(), sh.segments,
-                                                                       sh.seg_bits, 1, out_partials);
+        // depth per + log2 T: T = the power of two >= segments, 32..128
+        int T = 32;
+        while (T < kSubsetThreads && size_t(T) < sh.segments) T *= 2;
+        const int per = int((sh.segments + T - 1) / T);
+        k_msm_subsets<<<dim3(1, sh.partials), T, 0, st>>>(run.as<Xyzz>(), acc.as<Xyzz>(), sh.segments,
+                                                          sh.seg_bits, 1, per, out_partials);
         check_launch();
     } else {
         if (chunks > 64) fail(HP_CUDA_STATUS_NOT_IMPLEMENTED);
         Scratch partial(ctx, size_t(chunks) * sh.partials * sizeof(Xyzz), st);
         k_msm_subsets<<<dim3(chunks, sh.partials), kSubsetThreads, 0, st>>>(run.as<Xyzz>(), acc.as<Xyzz>(),
                                                                             sh.segments, sh.seg_bits, chunks,
-                                                                            partial.as<Xyzz>());
+                                                                            kSubsetPerThread, partial.as<Xyzz>());
         check_launch();
         k_msm_rows<<<sh.partials, 64, 0, st>>>(partial.as<Xyzz>(), chunks, out_partials);
         check_launch();
@@ -655,10 +712,14 @@ host::Xyzz64 msm_combine_host(const MsmShape &shape, const host::Xyzz64 *partial
     return host::xyzz_add(partials[shape.seg_bits], h);
 }
 
-void msm_finalize_host(const MsmLayer &layer, const host::Xyzz64 *partials, uint8_t *out97) {
+host::Xyzz64 msm_result_host(const MsmLayer &layer, const host::Xyzz64 *partials) {
     host::Xyzz64 r = msm_combine_host(msm_shape(layer), partials);
     if (layer.delta) r = host::xyzz_add(r, layer.minus_d);
-    host::xyzz_to_packet(r, out97);
+    return r;
+}
+
+void msm_finalize_host(const MsmLayer &layer, const host::Xyzz64 *partials, uint8_t *out97) {
+    host::xyzz_to_packet(msm_result_host(layer, partials), out97);
 }
 
 }  // namespace hp

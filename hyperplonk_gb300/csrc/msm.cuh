@@ -66,7 +66,8 @@ void xyzz_to_affine(HpCudaContext *ctx, const Xyzz *in, Affine *out, Fq *pre, si
 // Host: combine the partials of one MSM into a point.
 host::Xyzz64 msm_combine_host(const MsmShape &shape, const host::Xyzz64 *partials);
 // Host: combine the partials of one MSM over `layer` (removing its
-// randomisation offset) into a 97-byte G1 packet.
+// randomisation offset) into its result point / a 97-byte G1 packet.
+host::Xyzz64 msm_result_host(const MsmLayer &layer, const host::Xyzz64 *partials);
 void msm_finalize_host(const MsmLayer &layer, const host::Xyzz64 *partials, uint8_t *out97);
 
 }  // namespace hp

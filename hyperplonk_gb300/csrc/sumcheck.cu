@@ -24,6 +24,7 @@
 #include "mle.cuh"
 #include "runtime.cuh"
 #include "sumcheck.cuh"
+#include "transcript.h"
 
 using hp::check_cuda;
 using hp::check_launch;
@@ -102,18 +103,20 @@ __global__ void k_sumcheck_round(SumcheckDesc desc, FrPtrList src, FrMutPtrList 
             if (t < half) acc[s * T + t] = acc[s * T + t] + acc[s * T + t + half];
             __syncthreads();
         }
-        if (t == 0) partials[size_t(blockIdx.x) * S + s] = acc[s * T];
+        if (t == 0) partials[size_t(s) * gridDim.x + blockIdx.x] = acc[s * T];  // slot-major
     }
 }
 
 // Register-resident round for products of arity <= MAXM (every VP of the
 // prover: degree <= 5).  One pair per thread per iteration; the fold of all
 // factors is written to `dst` first, then each product re-reads its factors'
-// folded pair (an L2 hit: this thread just wrote it) and evaluates at
-// t = 0..m with running values in registers; each (product, t) value is
-// summed across the warp with shuffles and added into a per-warp shared slot.
+// folded pair (an L1/L2 hit: this thread just wrote it) and evaluates at
+// t = 0..m with running values in registers; each (product, t) value is added
+// to the thread's own slot sum in shared memory, and the block reduces the
+// slot sums once at the end (a warp shuffle reduction per value and pair
+// cost as much as the products themselves).
 constexpr int kRoundThreads = 128;
-constexpr int kMaxSlotsV2 = 64;
+constexpr int kMaxSlotsV2 = 48;  // slot sums in shared memory: 48 x 128 x 32 B = 192 KiB
 
 __device__ __forceinline__ Fr warp_sum(Fr v) {
 #pragma unroll
@@ -130,15 +133,13 @@ template <int MAXM>
 __global__ void __launch_bounds__(kRoundThreads) k_sumcheck_round_regs(SumcheckDesc desc, FrPtrList src,
                                                                        FrMutPtrList dst, FrPtrList rd, bool fold,
                                                                        Fr r, size_t pairs, Fr *partials) {
-    __shared__ Fr warp_slots[kRoundThreads / 32][kMaxSlotsV2];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // acc[s * kRoundThreads + t]: thread t's running sum of slot s over its pairs
+    extern __shared__ Fr acc[];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const int S = desc.slot_count, F = desc.factor_count;
-    for (int i = threadIdx.x; i < (kRoundThreads / 32) * S; i += blockDim.x) warp_slots[i / S][i % S] = Fr::zero();
-    __syncthreads();
-    for (size_t base = size_t(blockIdx.x) * kRoundThreads; base < pairs; base += size_t(gridDim.x) * kRoundThreads) {
-        const size_t b = base + threadIdx.x;
-        const bool active = b < pairs;
-        if (fold && active) {
+    for (int s = 0; s < S; s++) acc[s * kRoundThreads + t] = Fr::zero();
+    for (size_t b = size_t(blockIdx.x) * kRoundThreads + t; b < pairs; b += size_t(gridDim.x) * kRoundThreads) {
+        if (fold) {
             for (int f = 0; f < F; f++) {
                 const Fr *s = src.p[f] + 4 * b;
                 Fr a0 = load_fr(s), a1 = load_fr(s + 1), a2 = load_fr(s + 2), a3 = load_fr(s + 3);
@@ -150,51 +151,49 @@ __global__ void __launch_bounds__(kRoundThreads) k_sumcheck_round_regs(SumcheckD
         for (int p = 0; p < desc.product_count; p++) {
             const int begin = desc.offsets[p], m = desc.offsets[p + 1] - begin, slot = desc.slot_base[p];
             Fr e[MAXM], st[MAXM];
-            if (active) {
 #pragma unroll
-                for (int j = 0; j < MAXM; j++) {
-                    if (j < m) {
-                        const Fr *t = rd.p[desc.indices[begin + j]] + 2 * b;
-                        e[j] = load_fr(t);
-                        st[j] = load_fr(t + 1) - e[j];
-                    }
+            for (int j = 0; j < MAXM; j++) {
+                if (j < m) {
+                    const Fr *q = rd.p[desc.indices[begin + j]] + 2 * b;
+                    e[j] = load_fr(q);
+                    st[j] = load_fr(q + 1) - e[j];
                 }
             }
             for (int k = 0; k <= m; k++) {
-                Fr v = Fr::zero();
-                if (active) {
-                    if (k > 0) {
+                if (k > 0) {
 #pragma unroll
-                        for (int j = 0; j < MAXM; j++)
-                            if (j < m) e[j] = e[j] + st[j];
-                    }
-                    v = e[0];
-#pragma unroll
-                    for (int j = 1; j < MAXM; j++)
-                        if (j < m) v = v * e[j];
+                    for (int j = 0; j < MAXM; j++)
+                        if (j < m) e[j] = e[j] + st[j];
                 }
-                v = warp_sum(v);
-                if (lane == 0) warp_slots[warp][slot + k] = warp_slots[warp][slot + k] + v;
+                Fr v = e[0];
+#pragma unroll
+                for (int j = 1; j < MAXM; j++)
+                    if (j < m) v = v * e[j];
+                Fr &a = acc[(slot + k) * kRoundThreads + t];
+                a = a + v;
             }
         }
     }
     __syncthreads();
-    for (int s = threadIdx.x; s < S; s += blockDim.x) {
-        Fr a = warp_slots[0][s];
+    // warp w reduces slots w, w + 4, ...: 4 column values per lane, then shuffles
+    for (int s = warp; s < S; s += kRoundThreads / 32) {
+        Fr v = acc[s * kRoundThreads + lane];
 #pragma unroll
-        for (int w = 1; w < kRoundThreads / 32; w++) a = a + warp_slots[w][s];
-        partials[size_t(blockIdx.x) * S + s] = a;
+        for (int i = 1; i < kRoundThreads / 32; i++) v = v + acc[s * kRoundThreads + 32 * i + lane];
+        v = warp_sum(v);
+        if (lane == 0) partials[size_t(s) * gridDim.x + blockIdx.x] = v;  // slot-major
     }
 }
 
 // One block.  Warp w sums the block partials of slots w, w + warps, ... (lane
-// strided loads, then shuffles) into shared memory.  Then thread x evaluates
-// the round polynomial at t = x: product p of arity m contributes
-// coef_p * v_p(x), where v_p(x) is its slot sum at x <= m and otherwise the
-// Newton forward-difference extension sum_j C(x, j) Delta^j v_p(0) of the m+1
-// sums -- the unique polynomial of degree <= m through them, as the
-// reference's barycentric extrapolation (backend/src/cpu/sum_check.rs:183-217).
-// Writes the slot sums (Montgomery) and the d+1 canonical evaluations.
+// strided loads, then shuffles) into shared memory and slot_sums.  Thread p
+// then turns product p's m+1 sums v(0..m) into its forward differences
+// Delta^j v(0) in place, and thread x evaluates the round polynomial at t = x
+// as sum_p coef_p sum_{j <= min(x, m)} C(x, j) Delta^j v_p(0) -- Newton's
+// form of the unique polynomial of degree <= m through the sums, so equal to
+// the slot sum for x <= m and to the reference's barycentric extrapolation
+// (backend/src/cpu/sum_check.rs:183-217) beyond.  Writes the d+1 canonical
+// evaluations.
 __global__ void k_sumcheck_finalize(SumcheckDesc desc, const Fr *partials, int blocks,
                                     const Fr *coefs, int degree, Fr *slot_sums, Fr *out) {
     extern __shared__ Fr sums[];
@@ -202,7 +201,7 @@ __global__ void k_sumcheck_finalize(SumcheckDesc desc, const Fr *partials, int b
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
     for (int s = warp; s < S; s += warps) {
         Fr a = Fr::zero();
-        for (int b = lane; b < blocks; b += 32) a = a + partials[size_t(b) * S + s];
+        for (int b = lane; b < blocks; b += 32) a = a + partials[size_t(s) * blocks + b];
         a = warp_sum(a);
         if (lane == 0) {
             sums[s] = a;
@@ -210,32 +209,26 @@ __global__ void k_sumcheck_finalize(SumcheckDesc desc, const Fr *partials, int b
         }
     }
     __syncthreads();
+    for (int p = threadIdx.x; p < desc.product_count; p += blockDim.x) {
+        Fr *v = sums + desc.slot_base[p];
+        const int m = desc.offsets[p + 1] - desc.offsets[p];
+        for (int j = 1; j <= m; j++)
+            for (int i = m; i >= j; i--) v[i] = v[i] - v[i - 1];  // v[i] = Delta^j v(i - j)
+    }
+    __syncthreads();
     for (int x = threadIdx.x; x <= degree; x += blockDim.x) {
-        // C(x, j) for j <= x by Pascal's rule (x <= 64: every entry < 2^63)
-        uint64_t binom[kMaxDegree + 1];
-        binom[0] = 1;
-        for (int r = 1; r <= x; r++) {
-            binom[r] = 1;
-            for (int j = r - 1; j > 0; j--) binom[j] += binom[j - 1];
-        }
         Fr acc = Fr::zero();
         for (int p = 0; p < desc.product_count; p++) {
-            const int m = desc.offsets[p + 1] - desc.offsets[p];
             const Fr *v = sums + desc.slot_base[p];
-            Fr val;
-            if (x <= m) {
-                val = v[x];
-            } else {
-                Fr d[kMaxDegree + 1];
-                for (int i = 0; i <= m; i++) d[i] = v[i];
-                val = d[0];
-                for (int j = 1; j <= m; j++) {
-                    for (int i = 0; i + j <= m; i++) d[i] = d[i + 1] - d[i];  // d[0] = Delta^j v(0)
-                    Fr cj = Fr::zero();
-                    cj.v[0] = uint32_t(binom[j]);
-                    cj.v[1] = uint32_t(binom[j] >> 32);
-                    val = val + to_mont(cj) * d[0];
-                }
+            const int m = desc.offsets[p + 1] - desc.offsets[p];
+            Fr val = v[0];
+            uint64_t c = 1;  // C(x, j); C(64, j) < 2^61
+            for (int j = 1; j <= m && j <= x; j++) {
+                c = uint64_t((unsigned __int128)c * uint64_t(x - j + 1) / uint64_t(j));
+                Fr cj = Fr::zero();
+                cj.v[0] = uint32_t(c);
+                cj.v[1] = uint32_t(c >> 32);
+                val = val + to_mont(cj) * v[j];
             }
             acc = acc + coefs[p] * val;
         }
@@ -400,10 +393,13 @@ static void enqueue_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, cons
     Scratch partials, sums(ctx, d.slot_count * sizeof(Fr), st);
     int tok = ctx->prof_begin("sumcheck_round", st);
     if (regs) {
-        grid = grid_for(ctx, pairs, kRoundThreads, 8);
+        grid = grid_for(ctx, pairs, kRoundThreads, 4);
         partials = Scratch(ctx, size_t(grid) * d.slot_count * sizeof(Fr), st);
+        const size_t smem = size_t(d.slot_count) * kRoundThreads * sizeof(Fr);
         auto launch = [&](auto kernel) {
-            kernel<<<grid, kRoundThreads, 0, st>>>(d, src, dst, rd, fold, r, pairs, partials.as<Fr>());
+            if (smem > 48 * 1024)
+                check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+            kernel<<<grid, kRoundThreads, smem, st>>>(d, src, dst, rd, fold, r, pairs, partials.as<Fr>());
         };
         if (d.max_arity <= 2) launch(k_sumcheck_round_regs<2>);
         else if (d.max_arity <= 4) launch(k_sumcheck_round_regs<4>);
@@ -523,6 +519,44 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_final_evaluations(
         check_cuda(cudaMemcpyAsync(out_evaluations, outd.ptr, factor_count * sizeof(Fr),
                                    cudaMemcpyDeviceToHost, ctx->stream));
         ctx->sync();
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prove_rounds(HpCudaContext *ctx, HpCudaSumCheckProverState *s,
+                                                         HpMerlinTranscript *transcript, size_t rounds,
+                                                         uint8_t *out_messages, uint8_t *out_challenges) {
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(s != nullptr && transcript != nullptr && out_messages != nullptr && out_challenges != nullptr);
+        if (s->poisoned || s->round != 0) fail(HP_CUDA_STATUS_INVALID_STATE);
+        require(rounds == s->num_vars);
+        const size_t d1 = s->max_degree + 1;
+        hp::Scratch outd(ctx, d1 * sizeof(Fr));
+        // "prover msg" payload: u64 LE element count, then the canonical elements
+        std::vector<uint8_t> msg(8 + 32 * d1, 0);
+        for (int b = 0; b < 8; b++) msg[b] = uint8_t(uint64_t(d1) >> (8 * b));
+        Fr r = Fr::zero();
+        for (size_t k = 0; k < rounds; k++) {
+            try {
+                hp::enqueue_round(ctx, s, r, ctx->stream, outd.as<Fr>());
+                check_cuda(cudaMemcpyAsync(msg.data() + 8, outd.ptr, 32 * d1, cudaMemcpyDeviceToHost, ctx->stream));
+                ctx->sync();
+                hp::advance(s);
+            } catch (const hp::Failure &f) {
+                if (f.kind == HP_CUDA_STATUS_INVALID_STATE) s->poisoned = true;
+                throw;
+            }
+            std::memcpy(out_messages + 32 * d1 * k, msg.data() + 8, 32 * d1);
+            hp::merlin_append(transcript, "prover msg", msg.data(), msg.size());
+            // challenge: 64 transcript bytes reduced mod r, re-appended canonically
+            uint8_t wide[64], canon[32];
+            hp::merlin_challenge(transcript, "Internal round", wide, 64);
+            const hp::host::Fr64 c = hp::host::from_wide64(wide);
+            hp::host::to_canonical(c, canon);
+            hp::merlin_append(transcript, "Internal round", canon, 32);
+            std::memcpy(out_challenges + 32 * k, canon, 32);
+            std::memcpy(r.v, c.v, 32);
+        }
     });
 }
 

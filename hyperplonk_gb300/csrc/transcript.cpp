@@ -16,6 +16,7 @@
 #include <new>
 
 #include "../../include/hp_cuda.h"
+#include "transcript.h"
 
 namespace {
 
@@ -169,6 +170,15 @@ struct HpMerlinTranscript {
         strobe.prf(out, on, false);
     }
 };
+
+namespace hp {
+void merlin_append(HpMerlinTranscript *t, const char *label, const uint8_t *msg, size_t n) {
+    t->append(reinterpret_cast<const uint8_t *>(label), std::strlen(label), msg, n);
+}
+void merlin_challenge(HpMerlinTranscript *t, const char *label, uint8_t *out, size_t n) {
+    t->challenge(reinterpret_cast<const uint8_t *>(label), std::strlen(label), out, n);
+}
+}  // namespace hp
 
 extern "C" HpCudaStatus hp_host_v1_merlin_new(const uint8_t *label, size_t label_len, HpMerlinTranscript **out) {
     if (!out || (label_len && !label) || label_len > 0xffffffffu) return HpCudaStatus{HP_CUDA_STATUS_INVALID_PARAMETERS, 0};

@@ -73,6 +73,13 @@ def sumcheck_prove(backend, poly: VirtualPolynomial, transcript, final_evaluatio
         raise PolyIOPError("SumCheck requires positive variable count and degree.")
     transcript.append_serializable_element(b"aux info", ser.aux_info(d, nv))
     state = backend.prover_init(poly)
+    native = getattr(transcript, "native_merlin", lambda: None)()
+    if native is not None and hasattr(backend, "prove_rounds"):
+        # every round and its Fiat-Shamir step inside the library, one call
+        msgs, point = backend.prove_rounds(state, native, nv)
+        if final_evaluations is not None:
+            final_evaluations.extend(backend.final_evaluations(state, point[-1]))
+        return IOPProof(point, msgs)
     challenge = None
     msgs, point = [], []
     for _ in range(nv):

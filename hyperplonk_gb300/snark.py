@@ -77,13 +77,22 @@ class PcsAccumulator:
         self.polynomials, self.points, self.evals = [], [], []
 
     def insert_poly_and_points(self, backend, poly, point) -> None:
+        """The evaluation is due by multi_open (its only reader); backends with
+        evaluate_many compute all of them there in one call."""
         assert poly.num_vars == self.num_var
-        self.evals.append(backend.evaluate_mle(poly, point))
+        if not hasattr(backend, "evaluate_many"):
+            self.evals.append(backend.evaluate_mle(poly, point))
         self.polynomials.append(poly)
         self.points.append(list(point))
 
+    def evaluations(self, backend) -> list:
+        if len(self.evals) < len(self.polynomials):
+            self.evals = backend.evaluate_many(self.polynomials, self.points)
+        return self.evals
+
     def multi_open(self, backend, pcs_param, transcript, phases: dict | None = None) -> BatchProof:
-        return multi_open(backend, pcs_param, self.polynomials, self.points, self.evals, transcript, phases)
+        evals = self.evaluations(backend)
+        return multi_open(backend, pcs_param, self.polynomials, self.points, evals, transcript, phases)
 
 
 def prove(backend, pk: ProvingKey, pub_input: list, witnesses: list, transcript_cls=IOPTranscript,
@@ -131,6 +140,7 @@ def prove(backend, pk: ProvingKey, pub_input: list, witnesses: list, transcript_
         acc.insert_poly_and_points(backend, s, zc.point)
     r_pi = transcript.get_and_append_challenge_vectors(b"r_pi", ell)
     acc.insert_poly_and_points(backend, witness_mles[0], r_pi + [0] * (nv - ell))
+    acc.evaluations(backend)
     mark("evaluations")
     batch = acc.multi_open(backend, pk.pcs_param, transcript, phases)
     mark.restart()

@@ -62,6 +62,11 @@ class IOPTranscript:
         self._t.append_message(label, msg)
         self.is_empty = False
 
+    def native_merlin(self):
+        """The underlying native transcript when it is one (library calls may
+        then append and draw challenges on it directly), else None."""
+        return self._t if isinstance(self._t, MerlinTranscript) and not self.is_empty else None
+
     def append_field_element(self, label: bytes, x: int) -> None:
         self.append_message(label, (x % R_MODULUS).to_bytes(32, "little"))
 

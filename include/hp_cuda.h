@@ -207,6 +207,15 @@ HpCudaStatus hp_cuda_v1_batch_sumcheck_round(HpCudaContext *ctx, HpCudaSumCheckP
                                              uint8_t *const *out_evaluations, const size_t *evaluation_counts,
                                              size_t count);
 
+/* Evaluations of `count` resident MLEs, polynomial k at the point of
+ * num_vars[k] canonical Fr starting at points + 32 * (num_vars[0] + ... +
+ * num_vars[k-1]); writes count canonical Fr.  Each value equals
+ * hp_cuda_v1_mle_evaluate of the same arguments; all share one
+ * synchronisation.  No counterpart in the reference (its PcsAccumulator
+ * evaluates one polynomial per call, hyperplonk/src/utils.rs:58). */
+HpCudaStatus hp_cuda_v1_mle_evaluate_many(HpCudaContext *ctx, size_t count, const HpCudaDeviceAddress *polynomials,
+                                          const size_t *num_vars, const uint8_t *points,
+                                          uint8_t *out_evaluations);
 /* Evaluation of a resident MLE that allocates no device memory.  No
  * counterpart in the reference.  For callers that cannot call cudaMalloc:
  * hosts that own all device memory through their own pre-reserved arena, or
@@ -270,6 +279,21 @@ HpCudaStatus hp_host_v1_merlin_challenge(HpMerlinTranscript *t, const uint8_t *l
 HpCudaStatus hp_host_v1_merlin_clone(const HpMerlinTranscript *t, HpMerlinTranscript **out);
 HpCudaStatus hp_host_v1_merlin_free(HpMerlinTranscript *t);
 HpCudaStatus hp_host_v1_keccak_f1600(uint8_t *state200);
+/* All `rounds` (= num_vars) rounds of a fresh sumcheck state, with the
+ * Fiat-Shamir step of subroutines/src/poly_iop/sum_check/mod.rs:147-155 done
+ * here instead of by the caller: round k's message (max_degree+1 canonical
+ * Fr) is appended to `transcript` under "prover msg" as a serialized
+ * Vec<Fr> (u64 LE length, 32-byte LE elements), the challenge is 64 bytes
+ * under "Internal round" reduced mod r and appended back under the same
+ * label, and it folds the next round.  Writes the messages
+ * (rounds * (max_degree+1) * 32 bytes) and the challenges (rounds * 32).
+ * Afterwards the state is where the last per-round call would leave it
+ * (final_evaluations takes the last challenge).  InvalidState unless the
+ * state is at round 0.  No counterpart in the reference (its caller drives
+ * the rounds one at a time through the transcript). */
+HpCudaStatus hp_cuda_v1_sumcheck_prove_rounds(HpCudaContext *ctx, HpCudaSumCheckProverState *state,
+                                              HpMerlinTranscript *transcript, size_t rounds,
+                                              uint8_t *out_messages, uint8_t *out_challenges);
 HpCudaStatus hp_cuda_v1_srs_generate(HpCudaContext *ctx, size_t num_vars, uint64_t seed,
                                      uint8_t *out_packets, size_t point_count);
 
