@@ -363,7 +363,8 @@ __device__ __forceinline__ Field<P> operator*(const Field<P> &a, const Field<P> 
         return mont_mul_wide<P>(a, b);
 #endif
     }
-    return mont_mul_inline<P>(a, b);
+    // Fr (8 limbs) inlined: probe on GB300 63 G/s wide vs 45 G/s low/high CIOS
+    return mont_mul_wide<P>(a, b);
 }
 
 struct FqPair {

@@ -59,10 +59,17 @@ int msm_window_bits(size_t n) {
 MsmShape msm_shape(const MsmLayer &layer) {
     MsmShape s;
     s.buckets = size_t(1) << (layer.c - 1);
-    // 16-bucket segments once there are >= 2^16 buckets (thread count is not
-    // the limit there); shorter segments below, because a segment is a chain
-    // of 2 seg dependent additions and small MSMs are latency-bound
-    s.seg = std::min<size_t>(16, std::max<size_t>(1, s.buckets >> 12));
+    // 16-bucket segments from 2^17 buckets up; shorter below, because a
+    // segment is a chain of 2 seg dependent additions and smaller MSMs are
+    // latency-bound (measured: 2^15 buckets seg 4 1.29 ms vs seg 8 1.42 ms
+    // and seg 16 1.70 ms; 2^11 buckets seg 1 best; 2^19 seg 16 9.20 ms vs
+    // seg 8 9.56 ms and seg 32 9.47 ms)
+    s.seg = std::min<size_t>(16, std::max<size_t>(1, s.buckets >> 13));
+    // tuning override: HP_MSM_SEG=s (power of two, 1..64)
+    if (const char *env = std::getenv("HP_MSM_SEG")) {
+        const long v = std::atol(env);
+        if (v >= 1 && v <= 64 && (v & (v - 1)) == 0) s.seg = std::min<size_t>(s.buckets, size_t(v));
+    }
     s.segments = s.buckets / s.seg;
     s.seg_bits = 0;
     while ((size_t(1) << s.seg_bits) < s.segments) s.seg_bits++;
@@ -432,16 +439,16 @@ __global__ void k_msm_scatter(const Fr *scalars, const Fr *delta, size_t n, size
 // k_msm_bucket_fixup adds up.
 
 #ifndef HP_ACC_MINBLOCKS
-#define HP_ACC_MINBLOCKS 3  // measured best on GB300 at 2^20 (13.9 ms vs 14.2 ms at 1)
+#define HP_ACC_MINBLOCKS 4  // measured on GB300 at 2^20: 9.04 ms at 4, 9.20 at 3, 9.56 at 2
 #endif
 
 // Chunk length L = 32 records per thread, one block per 128 chunks, blocks
 // scheduled dynamically (measured at 2^20 points, c = 20: L = 32 9.56 ms per
 // MSM, 48 9.70, 64 9.60, 96 10.33; a grid of exactly the resident blocks with
-// L near 64 9.81).  A chunk is a chain of L dependent mixed additions, so an
-// MSM too small to give every SM eight blocks of 32-record chunks uses
-// shorter chunks (down to 2); when it also has few buckets (<= 8192), each
-// cut bucket's pieces are summed by a warp.
+// L near 64 9.81).  A chunk is a chain of L dependent mixed additions and a
+// bucket of k records cut into k/L pieces leaves a fix-up chain of k/L
+// additions, so an MSM of fewer than 2 M records (latency-bound: not enough
+// chunks to fill the GPU many times over) uses L ~ sqrt(k), 4 <= L <= 32.
 constexpr uint32_t kChunkRecords = 32;
 
 struct AccumulateGeometry {
@@ -450,9 +457,14 @@ struct AccumulateGeometry {
     unsigned grid;    // blocks of 128 threads
 };
 
-AccumulateGeometry accumulate_geometry(const HpCudaContext *ctx, size_t records) {
-    const size_t threads = size_t(ctx->sm_count > 0 ? ctx->sm_count : 152) * 8 * 128;
-    size_t L = std::min<size_t>(kChunkRecords, std::max<size_t>(2, (records + threads - 1) / threads));
+AccumulateGeometry accumulate_geometry(size_t records, size_t buckets) {
+    size_t L = kChunkRecords;
+    if (records < (size_t(1) << 21)) {
+        const size_t k = std::max<size_t>(1, records / std::max<size_t>(1, buckets));
+        size_t r = 1;
+        while ((r + 1) * (r + 1) <= k) r++;  // floor(sqrt(k))
+        L = std::min<size_t>(kChunkRecords, std::max<size_t>(4, r));
+    }
     // tuning override: HP_ACC_CHUNK=L (8 <= L <= 1024)
     if (const char *env = std::getenv("HP_ACC_CHUNK")) {
         const long v = std::atol(env);
@@ -522,43 +534,6 @@ __global__ void k_msm_bucket_fixup(const uint32_t *offsets, uint32_t buckets, ui
         Xyzz acc = load_xyzz(&pieces[2 * size_t(t0) + 1]);
         for (uint32_t t = t0 + 1; t <= t1; t++) acc = xyzz_add(acc, load_xyzz(&pieces[2 * size_t(t)]));
         store_xyzz(&bucket_sums[b], acc);
-    }
-}
-
-// The same with a warp per bucket (short chunks: many pieces per bucket):
-// lane i sums pieces i, i + 32, ..., then a shuffle tree of 5 additions.
-__device__ __forceinline__ Xyzz shfl_down_xyzz(const Xyzz &p, int off) {
-    Xyzz r;
-#pragma unroll
-    for (int i = 0; i < 12; i++) {
-        r.x.v[i] = __shfl_down_sync(0xffffffffu, p.x.v[i], off);
-        r.y.v[i] = __shfl_down_sync(0xffffffffu, p.y.v[i], off);
-        r.zz.v[i] = __shfl_down_sync(0xffffffffu, p.zz.v[i], off);
-        r.zzz.v[i] = __shfl_down_sync(0xffffffffu, p.zzz.v[i], off);
-    }
-    return r;
-}
-
-__global__ void __launch_bounds__(128) k_msm_bucket_fixup_warp(const uint32_t *offsets, uint32_t buckets,
-                                                               uint32_t chunk, const Xyzz *pieces,
-                                                               Xyzz *bucket_sums) {
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-    for (uint32_t b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); b < buckets; b += warps) {
-        const uint32_t begin = offsets[b], end = offsets[b + 1];
-        if (begin == end) {
-            if (lane == 0) store_xyzz(&bucket_sums[b], xyzz_inf());
-            continue;
-        }
-        const uint32_t t0 = begin / chunk, t1 = (end - 1) / chunk;
-        if (t0 == t1) continue;  // warp-uniform
-        // piece k = 0 is [2 t0 + 1], piece k >= 1 is [2 (t0 + k)]
-        Xyzz acc = xyzz_inf();
-        for (uint32_t k = lane; k <= t1 - t0; k += 32)
-            acc = xyzz_add(acc, load_xyzz(&pieces[k == 0 ? 2 * size_t(t0) + 1 : 2 * (size_t(t0) + k)]));
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) acc = xyzz_add(acc, shfl_down_xyzz(acc, off));
-        if (lane == 0) store_xyzz(&bucket_sums[b], acc);
     }
 }
 
@@ -660,20 +635,15 @@ void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz 
     k_msm_scatter<<<grid_for(ctx, n, 256), 256, 0, st>>>(scalars, layer.delta, n, layer.n, layer.c, layer.windows,
                                                         cursor.as<uint32_t>(), recs.as<uint32_t>());
     check_launch();
-    const AccumulateGeometry geo = accumulate_geometry(ctx, records);
+    const AccumulateGeometry geo = accumulate_geometry(records, B);
     Scratch pieces(ctx, std::max<size_t>(2 * geo.chunks, 1) * sizeof(Xyzz), st);
     int tok = ctx->prof_begin("msm_accumulate", st);
     k_msm_accumulate<<<geo.grid, 128, 0, st>>>(layer.bases, offsets.as<uint32_t>(), recs.as<uint32_t>(),
                                                uint32_t(B), geo.chunk, buckets.as<Xyzz>(), pieces.as<Xyzz>());
     check_launch();
     ctx->prof_end(tok, st);
-    // a warp per bucket only pays when buckets are few and cut into many pieces
-    if (geo.chunk == kChunkRecords || B > 8192)
-        k_msm_bucket_fixup<<<grid_for(ctx, B, 128, 8), 128, 0, st>>>(offsets.as<uint32_t>(), uint32_t(B), geo.chunk,
-                                                                    pieces.as<Xyzz>(), buckets.as<Xyzz>());
-    else
-        k_msm_bucket_fixup_warp<<<grid_for(ctx, 32 * B, 128, 8), 128, 0, st>>>(
-            offsets.as<uint32_t>(), uint32_t(B), geo.chunk, pieces.as<Xyzz>(), buckets.as<Xyzz>());
+    k_msm_bucket_fixup<<<grid_for(ctx, B, 128, 8), 128, 0, st>>>(offsets.as<uint32_t>(), uint32_t(B), geo.chunk,
+                                                                pieces.as<Xyzz>(), buckets.as<Xyzz>());
     check_launch();
     Scratch acc(ctx, sh.segments * sizeof(Xyzz), st), run(ctx, sh.segments * sizeof(Xyzz), st);
     k_msm_segments<<<grid_for(ctx, sh.segments, 128, 16), 128, 0, st>>>(buckets.as<Xyzz>(), sh.segments, sh.seg,

@@ -148,8 +148,9 @@ def prodcheck_prove(backend, pcs_param, fxs, gxs, transcript):
         raise PolyIOPError("fx and gx have different number of variables")
     frac = backend.compute_frac_poly(fxs, gxs)
     prod = backend.compute_product_poly(frac)
-    frac_comm = backend.commit(pcs_param, frac)
-    prod_comm = backend.commit(pcs_param, prod)
+    # prod_check/mod.rs commits frac then prod; one multi_commit gives the
+    # same two commitments and lets the two MSMs overlap
+    frac_comm, prod_comm = backend.multi_commit(pcs_param, [frac, prod])
     transcript.append_serializable_element(b"frac(x)", ser.g1_compressed(frac_comm))
     transcript.append_serializable_element(b"prod(x)", ser.g1_compressed(prod_comm))
     alpha = transcript.get_and_append_challenge(b"alpha")
