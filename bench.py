@@ -59,7 +59,8 @@ def parse():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=["prove", "commit", "sumcheck", "batch", "serve"], default="prove")
     ap.add_argument("--requests", type=int, default=28, help="serve workload: requests per offered load")
-    ap.add_argument("--lanes", type=int, default=2, help="serve workload: device contexts of the server")
+    ap.add_argument("--lanes", type=int, default=4, help="serve workload: device contexts of the server")
+    ap.add_argument("--slots", type=int, default=2, help="serve workload: proofs in flight per lane")
     ap.add_argument("--num-vars", type=int, default=None,
                     help="default 20 (prove, commit, sumcheck); the batch workload's SRS has 22")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -512,7 +513,9 @@ def run_serve(args, world, rank, local, pg):
     m = args.requests
     rng = random.Random(4)
     nvs = [rng.randint(lo, nv_max) for _ in range(m)]
-    wits = [snark.vanilla_witness(nv, 2, (4 << 32) | i) for i, nv in enumerate(nvs)]
+    # request witnesses arrive in pinned host buffers (uploaded by each proof)
+    pinned = [[s.pinned(t) for t in snark.vanilla_witness(nv, 2, (4 << 32) | i)] for i, nv in enumerate(nvs)]
+    wits = [[t.numpy() for t in w] for w in pinned]
     pubs = [[int.from_bytes(w[0][32 * j:32 * j + 32].tobytes(), "little") for j in range(min(16, 1 << nv))]
             for nv, w in zip(nvs, wits)]
     layers = s.be.generate_srs(nv_max, 0)
@@ -525,7 +528,7 @@ def run_serve(args, world, rank, local, pg):
         alone.append(snark.prove(s.be, plain.proving_key(nv, 2, 16), pub, w).to_bytes())
         service.append(time.perf_counter() - t0)
     mean_service = statistics.mean(service)
-    srv = serve.ProofServer(local, nv_max=nv_max, lanes=args.lanes, srs_layers=layers)
+    srv = serve.ProofServer(local, nv_max=nv_max, lanes=args.lanes, slots_per_lane=args.slots, srs_layers=layers)
     srv.prepare(sorted(set(nvs)))
     for i in range(min(4, m)):  # warm-up of the lanes
         srv.wait(srv.submit(nvs[i], wits[i], pubs[i]))
@@ -573,8 +576,8 @@ def run_serve(args, world, rank, local, pg):
         1.0 / top["served"]["proofs_per_s"],
         f"prove requests, vanilla-plonk circuits of 2^16..2^{nv_max} gates (num_vars uniform, seed 4), Poisson "
         f"arrivals at 0.5x..2x the plain path's capacity, {m} requests per load, SRS nv={nv_max} resident, "
-        f"{args.lanes} lanes",
-        {"num_vars": nvs, "requests": m, "lanes": args.lanes},
+        f"{args.lanes} lanes x {args.slots} slots",
+        {"num_vars": nvs, "requests": m, "lanes": args.lanes, "slots_per_lane": args.slots},
         {"value": top["served"]["proofs_per_s"], "unit": "proofs/s",
          "h2d_bytes_per_step": int(statistics.mean(3 * 32 * (1 << nv) for nv in nvs)),
          "d2h_bytes_per_step": int(statistics.mean(len(b) for b in alone))},

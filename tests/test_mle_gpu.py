@@ -148,3 +148,18 @@ def test_inputs_stay_immutable(gpu, oracle):
     gpu.compute_frac_poly([m], [gpu.mle_from_evaluations(nv, oracle.random_fr(901, 1 << nv))])
     gpu.evaluate_mle(m, list(range(nv)))
     assert gpu.download(m) == t
+
+
+def test_evaluate_many_matches_single_evaluations(gpu, oracle):
+    import random
+    rng = random.Random(21)
+    R = 0x73EDA753299D7D483339D80809A1D80553BDA402FFFE5BFEFFFFFFFF00000001
+    nvs = [0, 1, 5, 10, 11, 13, 21, 3]
+    mles = [gpu.mle_from_evaluations(nv, oracle.random_fr(500 + i, 1 << nv)) for i, nv in enumerate(nvs)]
+    points = [[rng.randrange(R) for _ in range(nv)] for nv in nvs]
+    many = gpu.evaluate_many(mles, points)
+    assert many == [gpu.evaluate_mle(m, p) for m, p in zip(mles, points)]
+    cpu = oracle.CpuBackend()
+    for i, (nv, p) in enumerate(zip(nvs[:6], points[:6])):
+        assert many[i] == cpu.evaluate_mle(cpu.mle_from_evaluations(nv, oracle.random_fr(500 + i, 1 << nv)), p)
+    assert gpu.evaluate_many([], []) == []
