@@ -11,6 +11,8 @@
 //    quotients stay on the device as MSM scalars, only the partial sums and
 //    the final scalar come back.
 #include <algorithm>
+#include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <vector>
@@ -54,6 +56,33 @@ static const MsmLayer &ready_layer(const HpCudaMultilinearKzgPreparedProverParam
 }
 
 // Download `total` XYZZ partials and finish each MSM into a packet.
+// Independent MSMs, task i writing its partial rows at the running offset.
+// MSMs of >= 4 M (point, window) records fill the GPU alone: one msm_run
+// each, overlapped on worker streams; all smaller ones share one launch per
+// phase (msm_run_many) on another worker stream.  HP_MSM_MANY=0 runs every
+// MSM alone on the worker streams, HP_MSM_MANY=1 all of them together.
+static void run_msms(HpCudaContext *ctx, std::vector<MsmTask> tasks, Xyzz *parts) {
+    if (tasks.empty()) return;
+    size_t o = 0;
+    for (auto &t : tasks) {
+        t.out_row = o;
+        o += size_t(msm_shape(*t.layer).partials);
+    }
+    const char *env = std::getenv("HP_MSM_MANY");
+    const size_t big_records = env && env[0] == '0' ? 0 : env && env[0] == '1' ? SIZE_MAX : (size_t(1) << 22);
+    std::vector<MsmTask> big, small;
+    for (const auto &t : tasks)
+        (size_t(t.layer->windows) * t.n >= big_records ? big : small).push_back(t);
+    std::stable_sort(big.begin(), big.end(), [](const MsmTask &a, const MsmTask &b) { return a.n > b.n; });
+    const size_t lanes = big.size() + (small.empty() ? 0 : 1);
+    const int k = int(std::min<size_t>(lanes, HpCudaContext::kWorkers));
+    ctx->fork(k);
+    size_t w = 0;
+    if (!small.empty()) msm_run_many(ctx, small.data(), small.size(), parts, ctx->workers[w++ % size_t(k)]);
+    for (const auto &t : big) msm_run(ctx, *t.layer, t.scalars, parts + t.out_row, ctx->workers[w++ % size_t(k)], t.n);
+    ctx->join(k);
+}
+
 static void finish_msms(HpCudaContext *ctx, const Xyzz *dev, const std::vector<const MsmLayer *> &layers,
                         uint8_t *out97) {
     std::vector<MsmShape> shapes;
@@ -162,15 +191,9 @@ extern "C" HpCudaStatus hp_cuda_v1_multilinear_kzg_multi_commit(
             total += size_t(shapes[i].partials);
         }
         hp::Scratch parts(ctx, total * sizeof(hp::Xyzz));
-        size_t off = 0;
-        // independent MSMs overlap on the context's worker streams
-        const int k = int(std::min<size_t>(count, HpCudaContext::kWorkers));
-        ctx->fork(k);
-        for (size_t i = 0; i < count; i++) {
-            hp::msm_run(ctx, *layers[i], scalars[i], parts.as<hp::Xyzz>() + off, ctx->workers[i % size_t(k)]);
-            off += size_t(shapes[i].partials);
-        }
-        ctx->join(k);
+        std::vector<hp::MsmTask> tasks(count);
+        for (size_t i = 0; i < count; i++) tasks[i] = hp::MsmTask{layers[i], scalars[i], layers[i]->n, 0};
+        hp::run_msms(ctx, tasks, parts.as<hp::Xyzz>());
         hp::finish_msms(ctx, parts.as<hp::Xyzz>(), layers, out_commitments);
     });
 }
@@ -220,15 +243,9 @@ extern "C" HpCudaStatus hp_cuda_v1_multilinear_kzg_open(
             qo += half;
             cur = next;
         }
-        const int k = int(std::min<size_t>(nv, HpCudaContext::kWorkers));
-        ctx->fork(k);
-        size_t off = 0;
-        for (size_t i = 0; i < nv; i++) {
-            hp::msm_run(ctx, *layers[i], q.as<Fr>() + q_off[i], parts.as<hp::Xyzz>() + off,
-                        ctx->workers[i % size_t(k)]);
-            off += size_t(shapes[i].partials);
-        }
-        ctx->join(k);
+        std::vector<hp::MsmTask> tasks(nv);
+        for (size_t i = 0; i < nv; i++) tasks[i] = hp::MsmTask{layers[i], q.as<Fr>() + q_off[i], layers[i]->n, 0};
+        hp::run_msms(ctx, tasks, parts.as<hp::Xyzz>());
         hp::download_canonical(ctx, cur, 1, out_evaluation);
         hp::finish_msms(ctx, parts.as<hp::Xyzz>(), layers, out_quotients);
     });
@@ -300,23 +317,9 @@ extern "C" HpCudaStatus hp_cuda_v1_batch_msm(HpCudaContext *ctx, HpCudaMultiline
             total += size_t(hp::msm_shape(*layers[i]).partials);
         }
         hp::Scratch parts(ctx, total * sizeof(hp::Xyzz));
-        // largest first, round-robin over the worker streams
-        std::vector<size_t> order(count);
-        for (size_t i = 0; i < count; i++) order[i] = i;
-        std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return num_vars[a] > num_vars[b]; });
-        std::vector<size_t> part_off(count);
-        size_t off = 0;
-        for (size_t i = 0; i < count; i++) {
-            part_off[i] = off;
-            off += size_t(hp::msm_shape(*layers[i]).partials);
-        }
-        const int k = int(std::min<size_t>(count, HpCudaContext::kWorkers));
-        ctx->fork(k);
-        for (size_t j = 0; j < count; j++) {
-            const size_t i = order[j];
-            hp::msm_run(ctx, *layers[i], sc[i], parts.as<hp::Xyzz>() + part_off[i], ctx->workers[j % size_t(k)]);
-        }
-        ctx->join(k);
+        std::vector<hp::MsmTask> tasks(count);
+        for (size_t i = 0; i < count; i++) tasks[i] = hp::MsmTask{layers[i], sc[i], layers[i]->n, 0};
+        hp::run_msms(ctx, tasks, parts.as<hp::Xyzz>());
         hp::finish_msms(ctx, parts.as<hp::Xyzz>(), layers, out_points);
     });
 }

@@ -448,8 +448,11 @@ __global__ void k_msm_scatter(const Fr *scalars, const Fr *delta, size_t n, size
 // L near 64 9.81).  A chunk is a chain of L dependent mixed additions and a
 // bucket of k records cut into k/L pieces leaves a fix-up chain of k/L
 // additions, so an MSM of fewer than 2 M records (latency-bound: not enough
-// chunks to fill the GPU many times over) uses L ~ sqrt(k), 4 <= L <= 32.
+// chunks to fill the GPU many times over) uses L = 8 (measured: 2^12 points
+// L = 8 0.54 ms, 4 0.63, 16 0.60, 32 0.82; 2^16 L = 8 1.33 ms, 5 1.38,
+// 16 1.35, 32 1.38; 2^18 L = 32 3.07 ms, 16 3.12, 8 3.18).
 constexpr uint32_t kChunkRecords = 32;
+constexpr uint32_t kSmallChunkRecords = 8;
 
 struct AccumulateGeometry {
     uint32_t chunk;   // records per chunk (L)
@@ -457,18 +460,12 @@ struct AccumulateGeometry {
     unsigned grid;    // blocks of 128 threads
 };
 
-AccumulateGeometry accumulate_geometry(size_t records, size_t buckets) {
-    size_t L = kChunkRecords;
-    if (records < (size_t(1) << 21)) {
-        const size_t k = std::max<size_t>(1, records / std::max<size_t>(1, buckets));
-        size_t r = 1;
-        while ((r + 1) * (r + 1) <= k) r++;  // floor(sqrt(k))
-        L = std::min<size_t>(kChunkRecords, std::max<size_t>(4, r));
-    }
-    // tuning override: HP_ACC_CHUNK=L (8 <= L <= 1024)
+AccumulateGeometry accumulate_geometry(size_t records) {
+    size_t L = records < (size_t(1) << 21) ? kSmallChunkRecords : kChunkRecords;
+    // tuning override: HP_ACC_CHUNK=L (2 <= L <= 1024)
     if (const char *env = std::getenv("HP_ACC_CHUNK")) {
         const long v = std::atol(env);
-        if (v >= 8 && v <= 1024) L = size_t(v);
+        if (v >= 2 && v <= 1024) L = size_t(v);
     }
     AccumulateGeometry g;
     g.chunk = uint32_t(L);
@@ -487,16 +484,56 @@ __device__ __forceinline__ uint32_t bucket_of(const uint32_t *offsets, uint32_t 
     return lo;
 }
 
-__global__ void __launch_bounds__(128, HP_ACC_MINBLOCKS) k_msm_accumulate(const Affine *bases, const uint32_t *offsets,
+// Base table of a bucket: one layer (a single MSM) ...
+struct OneTable {
+    const Affine *bases;
+    __device__ __forceinline__ void prepare() const {}
+    __device__ __forceinline__ const Affine *of(uint32_t) const { return bases; }
+};
+
+// ... or the layer of the instance owning the bucket (many MSMs in one
+// launch, instance bucket ranges ascending; the table sits in shared memory).
+constexpr int kMaxInstances = 64;
+struct ManyTables {
+    const uint32_t *bucket_base;  // [count]
+    const Affine *const *bases;   // [count]
+    int count;
+    __device__ __forceinline__ void prepare() const {
+        __shared__ uint32_t s_base[kMaxInstances];
+        __shared__ const Affine *s_tab[kMaxInstances];
+        for (int i = threadIdx.x; i < count; i += blockDim.x) {
+            s_base[i] = bucket_base[i];
+            s_tab[i] = bases[i];
+        }
+        __syncthreads();
+        sb = s_base;
+        st = s_tab;
+    }
+    __device__ __forceinline__ const Affine *of(uint32_t b) const {
+        int lo = 0, hi = count;  // sb[lo] <= b < sb[hi]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (sb[mid] <= b) lo = mid; else hi = mid;
+        }
+        return st[lo];
+    }
+    mutable const uint32_t *sb = nullptr;
+    mutable const Affine *const *st = nullptr;
+};
+
+template <class Tables>
+__global__ void __launch_bounds__(128, HP_ACC_MINBLOCKS) k_msm_accumulate(Tables tables, const uint32_t *offsets,
                                                                           const uint32_t *records, uint32_t buckets,
                                                                           uint32_t chunk, Xyzz *bucket_sums,
                                                                           Xyzz *pieces) {
+    tables.prepare();
     const uint32_t total = offsets[buckets];
     const uint32_t chunks = (total + chunk - 1) / chunk;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < chunks; t += gridDim.x * blockDim.x) {
         const uint32_t lo = t * chunk, hi = min(lo + chunk, total);
         uint32_t b = bucket_of(offsets, buckets, lo);
         uint32_t b_end = offsets[b + 1];
+        const Affine *bases = tables.of(b);
         Xyzz acc = xyzz_inf();
         for (uint32_t k = lo;; k++) {
             if (k == hi || k == b_end) {
@@ -509,6 +546,7 @@ __global__ void __launch_bounds__(128, HP_ACC_MINBLOCKS) k_msm_accumulate(const 
                 if (k == hi) break;
                 // next non-empty bucket containing record k
                 do { b++; b_end = offsets[b + 1]; } while (b_end <= k);
+                bases = tables.of(b);
                 acc = xyzz_inf();
             }
             uint32_t rec = records[k];
@@ -635,10 +673,10 @@ void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz 
     k_msm_scatter<<<grid_for(ctx, n, 256), 256, 0, st>>>(scalars, layer.delta, n, layer.n, layer.c, layer.windows,
                                                         cursor.as<uint32_t>(), recs.as<uint32_t>());
     check_launch();
-    const AccumulateGeometry geo = accumulate_geometry(records, B);
+    const AccumulateGeometry geo = accumulate_geometry(records);
     Scratch pieces(ctx, std::max<size_t>(2 * geo.chunks, 1) * sizeof(Xyzz), st);
     int tok = ctx->prof_begin("msm_accumulate", st);
-    k_msm_accumulate<<<geo.grid, 128, 0, st>>>(layer.bases, offsets.as<uint32_t>(), recs.as<uint32_t>(),
+    k_msm_accumulate<<<geo.grid, 128, 0, st>>>(OneTable{layer.bases}, offsets.as<uint32_t>(), recs.as<uint32_t>(),
                                                uint32_t(B), geo.chunk, buckets.as<Xyzz>(), pieces.as<Xyzz>());
     check_launch();
     ctx->prof_end(tok, st);
@@ -667,6 +705,227 @@ void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz 
         check_launch();
         k_msm_rows<<<sh.partials, 64, 0, st>>>(partial.as<Xyzz>(), chunks, out_partials);
         check_launch();
+    }
+    ctx->prof_end(whole, st);
+}
+
+// ---------------------------------------------------------------------------
+// Many MSMs in one launch sequence
+// ---------------------------------------------------------------------------
+//
+// Instances keep their own layer (window width, window table, randomisation)
+// and get disjoint ranges of one global bucket array, record array, segment
+// array and subset-block range; every phase above is one launch over all
+// instances' items, a thread finding its instance by a binary search over
+// the (ascending) range starts.  Results are the same per instance as
+// msm_run's: the per-bucket, per-segment and per-subset arithmetic is.
+
+struct MsmInst {
+    const Fr *scalars;
+    const Fr *delta;
+    uint32_t n, stride;        // points; the layer's point count (window stride)
+    int c, windows;
+    uint32_t point_base;       // first global point
+    uint32_t bucket_base;      // first global bucket
+    uint32_t seg, segments, seg_base;
+    int seg_bits, per, chunks;
+    uint32_t block_base;       // first subset block: (seg_bits + 1) * chunks blocks
+    uint32_t row_base;         // first staged row: seg_bits + 1 rows
+    uint32_t out_row;          // first output row
+};
+
+template <class Key>
+__device__ __forceinline__ int inst_of(const MsmInst *in, int count, uint32_t key, Key k) {
+    int lo = 0, hi = count;  // k(in[lo]) <= key < k(in[hi])
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (k(in[mid]) <= key) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_msmm_histogram(const MsmInst *in, int count, uint32_t points, uint32_t *counts) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < points; g += gridDim.x * blockDim.x) {
+        const MsmInst &m = in[inst_of(in, count, g, [](const MsmInst &x) { return x.point_base; })];
+        const Fr s = msm_scalar(m.scalars, m.delta, g - m.point_base);
+        uint32_t *cnt = counts + m.bucket_base;
+        for_each_digit(s, m.c, m.windows, [&](int, uint32_t mag, bool) { atomicAdd(&cnt[mag - 1], 1u); });
+    }
+}
+
+__global__ void k_msmm_scatter(const MsmInst *in, int count, uint32_t points, uint32_t *cursor, uint32_t *records) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < points; g += gridDim.x * blockDim.x) {
+        const MsmInst &m = in[inst_of(in, count, g, [](const MsmInst &x) { return x.point_base; })];
+        const uint32_t i = g - m.point_base;
+        const Fr s = msm_scalar(m.scalars, m.delta, i);
+        uint32_t *cur = cursor + m.bucket_base;
+        for_each_digit(s, m.c, m.windows, [&](int w, uint32_t mag, bool neg) {
+            const uint32_t pos = atomicAdd(&cur[mag - 1], 1u);
+            records[pos] = uint32_t(size_t(w) * m.stride + i) | (neg ? 0x80000000u : 0u);
+        });
+    }
+}
+
+__global__ void __launch_bounds__(128) k_msmm_segments(const MsmInst *in, int count, uint32_t segments,
+                                                       const Xyzz *buckets, Xyzz *acc_out, Xyzz *run_out) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < segments; g += gridDim.x * blockDim.x) {
+        const MsmInst &m = in[inst_of(in, count, g, [](const MsmInst &x) { return x.seg_base; })];
+        const Xyzz *bk = buckets + m.bucket_base + size_t(g - m.seg_base) * m.seg;
+        Xyzz run = xyzz_inf(), acc = xyzz_inf();
+        for (uint32_t l = m.seg; l-- > 0;) {
+            run = xyzz_add(run, load_xyzz(&bk[l]));
+            acc = xyzz_add(acc, run);
+        }
+        store_xyzz(&acc_out[g], acc);
+        store_xyzz(&run_out[g], run);
+    }
+}
+
+// Block -> (instance, subset y, chunk); writes stage[(row_base + y) * 64 + chunk].
+__global__ void __launch_bounds__(kSubsetThreads) k_msmm_subsets(const MsmInst *in, int count, const Xyzz *run,
+                                                                 const Xyzz *acc, Xyzz *stage) {
+    __shared__ Xyzz sm[kSubsetThreads];
+    const MsmInst &m = in[inst_of(in, count, blockIdx.x, [](const MsmInst &x) { return x.block_base; })];
+    const uint32_t local = blockIdx.x - m.block_base;
+    const int y = int(local / uint32_t(m.chunks)), chunk = int(local % uint32_t(m.chunks));
+    const int t = threadIdx.x, T = blockDim.x;
+    const size_t count_y = y < m.seg_bits ? m.segments / 2 : m.segments;
+    const size_t first = size_t(chunk) * size_t(T) * m.per;
+    const Xyzz *r = run + m.seg_base, *a = acc + m.seg_base;
+    Xyzz s = xyzz_inf();
+    for (int k = 0; k < m.per; k++) {
+        const size_t e = first + size_t(k) * T + t;
+        if (e >= count_y) break;
+        Xyzz v;
+        if (y < m.seg_bits) {
+            const size_t j = ((e >> y) << (y + 1)) | (size_t(1) << y) | (e & ((size_t(1) << y) - 1));
+            v = load_xyzz(&r[j]);
+        } else {
+            v = load_xyzz(&a[e]);
+        }
+        s = xyzz_add(s, v);
+    }
+    sm[t] = s;
+    __syncthreads();
+    for (int half = T / 2; half > 0; half >>= 1) {
+        if (t < half) sm[t] = xyzz_add(sm[t], sm[t + half]);
+        __syncthreads();
+    }
+    if (t == 0) store_xyzz(&stage[(size_t(m.row_base) + y) * 64 + chunk], sm[0]);
+}
+
+// Row r (of all instances' rows) = sum of its instance's chunks of stage.
+__global__ void k_msmm_rows(const MsmInst *in, int count, const Xyzz *stage, Xyzz *out) {
+    __shared__ Xyzz sm[64];
+    const uint32_t r = blockIdx.x;
+    const MsmInst &m = in[inst_of(in, count, r, [](const MsmInst &x) { return x.row_base; })];
+    const int t = threadIdx.x;
+    sm[t] = t < m.chunks ? load_xyzz(&stage[size_t(r) * 64 + t]) : xyzz_inf();
+    __syncthreads();
+    for (int half = 32; half > 0; half >>= 1) {
+        if (t < half) sm[t] = xyzz_add(sm[t], sm[t + half]);
+        __syncthreads();
+    }
+    if (t == 0) store_xyzz(&out[m.out_row + (r - m.row_base)], sm[0]);
+}
+
+// One group: at most kMaxInstances instances, all of it resident at once.
+static void msm_run_group(HpCudaContext *ctx, const MsmTask *tasks, size_t count, Xyzz *out_rows, cudaStream_t st) {
+    std::vector<MsmInst> in(count);
+    std::vector<uint32_t> bucket_base(count);
+    std::vector<const Affine *> tables(count);
+    size_t points = 0, B = 0, segs = 0, blocks = 0, rows = 0, records = 0;
+    for (size_t i = 0; i < count; i++) {
+        const MsmLayer &L = *tasks[i].layer;
+        const MsmShape sh = msm_shape(L);
+        MsmInst &m = in[i];
+        m.scalars = tasks[i].scalars;
+        m.delta = L.delta;
+        m.n = uint32_t(tasks[i].n);
+        m.stride = uint32_t(L.n);
+        m.c = L.c;
+        m.windows = L.windows;
+        m.point_base = uint32_t(points);
+        m.bucket_base = uint32_t(B);
+        m.seg = uint32_t(sh.seg);
+        m.segments = uint32_t(sh.segments);
+        m.seg_base = uint32_t(segs);
+        m.seg_bits = sh.seg_bits;
+        m.per = kSubsetPerThread;
+        m.chunks = int((sh.segments + kSubsetPerBlock - 1) / kSubsetPerBlock);
+        if (m.chunks > 64) fail(HP_CUDA_STATUS_NOT_IMPLEMENTED);
+        m.block_base = uint32_t(blocks);
+        m.row_base = uint32_t(rows);
+        m.out_row = uint32_t(tasks[i].out_row);
+        bucket_base[i] = m.bucket_base;
+        tables[i] = L.bases;
+        points += tasks[i].n;
+        B += sh.buckets;
+        segs += sh.segments;
+        blocks += size_t(sh.partials) * m.chunks;
+        rows += size_t(sh.partials);
+        records += size_t(L.windows) * tasks[i].n;
+    }
+    require(records < (size_t(1) << 31) && B < (size_t(1) << 31));
+    Scratch din(ctx, count * sizeof(MsmInst), st), dbase(ctx, count * 4, st), dtab(ctx, count * sizeof(void *), st);
+    check_cuda(cudaMemcpyAsync(din.ptr, in.data(), count * sizeof(MsmInst), cudaMemcpyHostToDevice, st));
+    check_cuda(cudaMemcpyAsync(dbase.ptr, bucket_base.data(), count * 4, cudaMemcpyHostToDevice, st));
+    check_cuda(cudaMemcpyAsync(dtab.ptr, tables.data(), count * sizeof(void *), cudaMemcpyHostToDevice, st));
+    const MsmInst *inst = din.as<MsmInst>();
+    const int cnt = int(count);
+    Scratch counts(ctx, (B + 1) * 4, st), offsets(ctx, (B + 1) * 4, st), cursor(ctx, B * 4, st);
+    Scratch recs(ctx, std::max<size_t>(records, 1) * 4, st), buckets(ctx, B * sizeof(Xyzz), st);
+    check_cuda(cudaMemsetAsync(counts.ptr, 0, (B + 1) * 4, st));
+    k_msmm_histogram<<<grid_for(ctx, points, 256), 256, 0, st>>>(inst, cnt, uint32_t(points), counts.as<uint32_t>());
+    check_launch();
+    const unsigned tiles = unsigned((B + kScanTile - 1) / kScanTile);
+    Scratch tile_sums(ctx, size_t(tiles) * 4, st);
+    if (tiles > 1) {
+        k_msm_scan_sums<<<tiles, kScanThreads, 0, st>>>(counts.as<uint32_t>(), B, tile_sums.as<uint32_t>());
+        check_launch();
+    }
+    k_msm_scan<<<tiles, kScanThreads, 0, st>>>(counts.as<uint32_t>(), B, tile_sums.as<uint32_t>(),
+                                              offsets.as<uint32_t>(), cursor.as<uint32_t>());
+    check_launch();
+    k_msmm_scatter<<<grid_for(ctx, points, 256), 256, 0, st>>>(inst, cnt, uint32_t(points), cursor.as<uint32_t>(),
+                                                              recs.as<uint32_t>());
+    check_launch();
+    const AccumulateGeometry geo = accumulate_geometry(records);
+    Scratch pieces(ctx, std::max<size_t>(2 * geo.chunks, 1) * sizeof(Xyzz), st);
+    k_msm_accumulate<<<geo.grid, 128, 0, st>>>(ManyTables{dbase.as<uint32_t>(), dtab.as<const Affine *>(), cnt},
+                                               offsets.as<uint32_t>(), recs.as<uint32_t>(), uint32_t(B), geo.chunk,
+                                               buckets.as<Xyzz>(), pieces.as<Xyzz>());
+    check_launch();
+    k_msm_bucket_fixup<<<grid_for(ctx, B, 128, 8), 128, 0, st>>>(offsets.as<uint32_t>(), uint32_t(B), geo.chunk,
+                                                                pieces.as<Xyzz>(), buckets.as<Xyzz>());
+    check_launch();
+    Scratch acc(ctx, segs * sizeof(Xyzz), st), run(ctx, segs * sizeof(Xyzz), st);
+    k_msmm_segments<<<grid_for(ctx, segs, 128, 16), 128, 0, st>>>(inst, cnt, uint32_t(segs), buckets.as<Xyzz>(),
+                                                                  acc.as<Xyzz>(), run.as<Xyzz>());
+    check_launch();
+    Scratch stage(ctx, rows * 64 * sizeof(Xyzz), st);
+    k_msmm_subsets<<<unsigned(blocks), kSubsetThreads, 0, st>>>(inst, cnt, run.as<Xyzz>(), acc.as<Xyzz>(),
+                                                               stage.as<Xyzz>());
+    check_launch();
+    k_msmm_rows<<<unsigned(rows), 64, 0, st>>>(inst, cnt, stage.as<Xyzz>(), out_rows);
+    check_launch();
+}
+
+void msm_run_many(HpCudaContext *ctx, const MsmTask *tasks, size_t count, Xyzz *out_rows, cudaStream_t stream) {
+    const cudaStream_t st = stream ? stream : ctx->stream;
+    // groups of <= kMaxInstances instances and <= 2^27 records (bounded scratch)
+    size_t i = 0;
+    int whole = ctx->prof_begin("msm_many", st);
+    while (i < count) {
+        size_t j = i, records = 0;
+        while (j < count && j - i < size_t(kMaxInstances)) {
+            const size_t r = size_t(tasks[j].layer->windows) * tasks[j].n;
+            if (j > i && records + r > (size_t(1) << 27)) break;
+            records += r;
+            j++;
+        }
+        msm_run_group(ctx, tasks + i, j - i, out_rows, st);
+        i = j;
     }
     ctx->prof_end(whole, st);
 }

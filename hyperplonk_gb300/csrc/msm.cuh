@@ -63,6 +63,18 @@ void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz 
 // Batch XYZZ -> affine (one field inversion per 512 points); pre: n Fq scratch.
 void xyzz_to_affine(HpCudaContext *ctx, const Xyzz *in, Affine *out, Fq *pre, size_t n);
 
+// Many MSMs in one launch per phase: task i = the first n points of layer
+// `layer` with `scalars`; writes its msm_shape(layer).partials rows (what
+// msm_run writes for it alone) to out_rows + out_row.
+struct MsmTask {
+    const MsmLayer *layer;
+    const Fr *scalars;
+    size_t n;
+    size_t out_row;
+};
+void msm_run_many(HpCudaContext *ctx, const MsmTask *tasks, size_t count, Xyzz *out_rows,
+                  cudaStream_t stream = nullptr);
+
 // Host: combine the partials of one MSM into a point.
 host::Xyzz64 msm_combine_host(const MsmShape &shape, const host::Xyzz64 *partials);
 // Host: combine the partials of one MSM over `layer` (removing its
