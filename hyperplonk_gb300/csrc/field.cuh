@@ -33,18 +33,6 @@ __device__ __forceinline__ uint32_t subc_cc(uint32_t a, uint32_t b) {
 __device__ __forceinline__ uint32_t subc(uint32_t a, uint32_t b) {
     uint32_t r; asm volatile("subc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b)); return r;
 }
-__device__ __forceinline__ uint32_t mad_lo_cc(uint32_t a, uint32_t b, uint32_t c) {
-    uint32_t r; asm volatile("mad.lo.cc.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c)); return r;
-}
-__device__ __forceinline__ uint32_t madc_lo_cc(uint32_t a, uint32_t b, uint32_t c) {
-    uint32_t r; asm volatile("madc.lo.cc.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c)); return r;
-}
-__device__ __forceinline__ uint32_t mad_hi_cc(uint32_t a, uint32_t b, uint32_t c) {
-    uint32_t r; asm volatile("mad.hi.cc.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c)); return r;
-}
-__device__ __forceinline__ uint32_t madc_hi_cc(uint32_t a, uint32_t b, uint32_t c) {
-    uint32_t r; asm volatile("madc.hi.cc.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c)); return r;
-}
 
 // ---------------------------------------------------------------------------
 // Moduli.  P: modulus limbs, INV: -P^-1 mod 2^32, ONE: R mod P, R2: R^2 mod P.
@@ -180,59 +168,13 @@ __device__ __forceinline__ Field<P> dbl(const Field<P> &a) {
     return a + a;
 }
 
-// CIOS Montgomery multiplication, 32-bit limbs: per row one carry chain for
-// the low halves and one for the high halves of a*b_i, then the same for
-// m*p.  4N^2 + N multiply-adds per product.
-template <class P>
-__device__ __forceinline__ Field<P> mont_mul_inline(const Field<P> &a, const Field<P> &b) {
-    constexpr int N = P::N;
-    uint32_t t[N + 2];
-#pragma unroll
-    for (int i = 0; i < N + 2; i++) t[i] = 0;
-#pragma unroll
-    for (int i = 0; i < N; i++) {
-        const uint32_t bi = b.v[i];
-        // t += lo(a * bi)
-        t[0] = mad_lo_cc(a.v[0], bi, t[0]);
-#pragma unroll
-        for (int j = 1; j < N; j++) t[j] = madc_lo_cc(a.v[j], bi, t[j]);
-        t[N] = addc_cc(t[N], 0);
-        t[N + 1] = addc(t[N + 1], 0);
-        // t += hi(a * bi) << 32
-        t[1] = mad_hi_cc(a.v[0], bi, t[1]);
-#pragma unroll
-        for (int j = 1; j < N; j++) t[j + 1] = madc_hi_cc(a.v[j], bi, t[j + 1]);
-        t[N + 1] = addc(t[N + 1], 0);
-        // reduction: t += m * p, t[0] becomes 0
-        const uint32_t m = t[0] * P::INV;
-        t[0] = mad_lo_cc(m, P::p(0), t[0]);
-#pragma unroll
-        for (int j = 1; j < N; j++) t[j] = madc_lo_cc(m, P::p(j), t[j]);
-        t[N] = addc_cc(t[N], 0);
-        t[N + 1] = addc(t[N + 1], 0);
-        t[1] = mad_hi_cc(m, P::p(0), t[1]);
-#pragma unroll
-        for (int j = 1; j < N; j++) t[j + 1] = madc_hi_cc(m, P::p(j), t[j + 1]);
-        t[N + 1] = addc(t[N + 1], 0);
-        // shift one limb down
-#pragma unroll
-        for (int j = 0; j < N + 1; j++) t[j] = t[j + 1];
-        t[N + 1] = 0;
-    }
-    Field<P> r;
-#pragma unroll
-    for (int i = 0; i < N; i++) r.v[i] = t[i];
-    reduce_once<P>(r, t[N]);
-    return r;
-}
-
 // CIOS Montgomery multiplication with 32x32 -> 64-bit multiply-adds: each
 // partial product a_j * b_i + t_j + carry fits 64 bits, so one wide multiply
-// and one 64-bit add replace the separate low-half and high-half multiplies
-// of mont_mul_inline; the high half of a 32x32 product costs two multiply
-// issues on this GPU, the wide form fewer (probe on GB300, 12 limbs:
-// 20.7 G/s vs 19.9 G/s out of line, 25.3 G/s inlined with two products
-// interleaved).
+// and one 64-bit add replace separate low-half and high-half multiply-add
+// chains (mad.lo.cc / madc.hi.cc); the high half of a 32x32 product costs
+// two multiply issues on this GPU, the wide form fewer (probe on GB300, 12
+// limbs: 20.7 G/s vs 19.9 G/s for the low/high form out of line, 25.3 G/s
+// inlined with two products interleaved; 8 limbs: 63 vs 45 G/s).
 template <class P>
 __device__ __forceinline__ Field<P> mont_mul_wide(const Field<P> &a, const Field<P> &b) {
     constexpr int N = P::N;

@@ -486,6 +486,50 @@ extern "C" HpCudaStatus hp_cuda_v1_mle_evaluate(HpCudaContext *ctx, HpCudaDevice
     });
 }
 
+namespace hp {
+
+// sum_i a[i] * b[i]: block partials (thread sums, shuffle and shared-memory
+// reduction), then one block sums the partials into out.
+__device__ __forceinline__ Fr fr_warp_sum(Fr v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        Fr o;
+#pragma unroll
+        for (int i = 0; i < 8; i++) o.v[i] = __shfl_down_sync(0xffffffffu, v.v[i], off);
+        v = v + o;
+    }
+    return v;
+}
+
+__device__ __forceinline__ Fr block_sum(Fr v) {  // blockDim.x = 256; result in thread 0
+    __shared__ Fr warp_part[8];
+    v = fr_warp_sum(v);
+    if ((threadIdx.x & 31) == 0) warp_part[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        v = threadIdx.x < 8 ? warp_part[threadIdx.x] : Fr::zero();
+        v = fr_warp_sum(v);
+    }
+    return v;
+}
+
+__global__ void __launch_bounds__(256) k_dot_partials(const Fr *a, const Fr *b, size_t n, Fr *partials) {
+    Fr acc = Fr::zero();
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+        acc = acc + load_fr(&a[i]) * load_fr(&b[i]);
+    acc = block_sum(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+}
+
+__global__ void __launch_bounds__(256) k_sum_partials(const Fr *partials, int count, Fr *out) {
+    Fr acc = Fr::zero();
+    for (int i = threadIdx.x; i < count; i += blockDim.x) acc = acc + partials[i];
+    acc = block_sum(acc);
+    if (threadIdx.x == 0) *out = acc;
+}
+
+}  // namespace hp
+
 extern "C" HpCudaStatus hp_cuda_v1_mle_evaluate_many(HpCudaContext *ctx, size_t count,
                                                      const HpCudaDeviceAddress *polynomials,
                                                      const size_t *num_vars, const uint8_t *points,
@@ -505,8 +549,41 @@ extern "C" HpCudaStatus hp_cuda_v1_mle_evaluate_many(HpCudaContext *ctx, size_t 
             off += num_vars[k];
         }
         Scratch res(ctx, count * sizeof(Fr));
+        // Polynomials of >= 2^12 entries sharing a point: f(point) = sum_x f[x]
+        // eq(x, point), one eq table per distinct point (a streaming dot
+        // product per polynomial instead of a fold chain each); the others fold.
+        constexpr size_t kDotMinVars = 12;
+        std::vector<bool> done(count, false);
+        off = 0;
+        std::vector<size_t> first(count);
+        for (size_t k = 0; k < count; k++) {
+            first[k] = off;
+            off += num_vars[k];
+        }
+        for (size_t k = 0; k < count; k++) {
+            if (done[k] || num_vars[k] < kDotMinVars) continue;
+            std::vector<size_t> group{k};
+            for (size_t j = k + 1; j < count; j++)
+                if (!done[j] && num_vars[j] == num_vars[k] &&
+                    std::memcmp(points + 32 * first[j], points + 32 * first[k], 32 * num_vars[k]) == 0)
+                    group.push_back(j);
+            if (group.size() < 2) continue;
+            const size_t nv = num_vars[k], n = hp::table_len(nv);
+            Scratch rd(ctx, nv * sizeof(Fr)), eq(ctx, n * sizeof(Fr));
+            check_cuda(cudaMemcpyAsync(rd.ptr, pts[k].data(), nv * sizeof(Fr), cudaMemcpyHostToDevice, ctx->stream));
+            hp::build_eq(ctx, rd.as<Fr>(), nv, eq.as<Fr>());
+            const unsigned grid = hp::grid_for(ctx, n, 256, 8);
+            Scratch part(ctx, size_t(grid) * sizeof(Fr));
+            for (size_t j : group) {
+                hp::k_dot_partials<<<grid, 256, 0, ctx->stream>>>(tables[j], eq.as<Fr>(), n, part.as<Fr>());
+                check_launch();
+                hp::k_sum_partials<<<1, 256, 0, ctx->stream>>>(part.as<Fr>(), int(grid), res.as<Fr>() + j);
+                check_launch();
+                done[j] = true;
+            }
+        }
         for (size_t k = 0; k < count; k++)
-            hp::fold_to_scalar(ctx, tables[k], num_vars[k], pts[k].data(), res.as<Fr>() + k);
+            if (!done[k]) hp::fold_to_scalar(ctx, tables[k], num_vars[k], pts[k].data(), res.as<Fr>() + k);
         hp::download_canonical(ctx, res.as<Fr>(), count, out_evaluations);
     });
 }

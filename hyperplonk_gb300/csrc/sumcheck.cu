@@ -115,7 +115,13 @@ __global__ void k_sumcheck_round(SumcheckDesc desc, FrPtrList src, FrMutPtrList 
 // to the thread's own slot sum in shared memory, and the block reduces the
 // slot sums once at the end (a warp shuffle reduction per value and pair
 // cost as much as the products themselves).
-constexpr int kRoundThreads = 128;
+#ifndef HP_ROUND_THREADS
+#define HP_ROUND_THREADS 128
+#endif
+#ifndef HP_ROUND_BLOCKS_PER_SM
+#define HP_ROUND_BLOCKS_PER_SM 4
+#endif
+constexpr int kRoundThreads = HP_ROUND_THREADS;
 constexpr int kMaxSlotsV2 = 48;  // slot sums in shared memory: 48 x 128 x 32 B = 192 KiB
 
 __device__ __forceinline__ Fr warp_sum(Fr v) {
@@ -393,7 +399,7 @@ static void enqueue_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, cons
     Scratch partials, sums(ctx, d.slot_count * sizeof(Fr), st);
     int tok = ctx->prof_begin("sumcheck_round", st);
     if (regs) {
-        grid = grid_for(ctx, pairs, kRoundThreads, 4);
+        grid = grid_for(ctx, pairs, kRoundThreads, HP_ROUND_BLOCKS_PER_SM);
         partials = Scratch(ctx, size_t(grid) * d.slot_count * sizeof(Fr), st);
         const size_t smem = size_t(d.slot_count) * kRoundThreads * sizeof(Fr);
         auto launch = [&](auto kernel) {

@@ -163,3 +163,22 @@ def test_evaluate_many_matches_single_evaluations(gpu, oracle):
     for i, (nv, p) in enumerate(zip(nvs[:6], points[:6])):
         assert many[i] == cpu.evaluate_mle(cpu.mle_from_evaluations(nv, oracle.random_fr(500 + i, 1 << nv)), p)
     assert gpu.evaluate_many([], []) == []
+
+
+def test_evaluate_many_shared_points_use_eq_dot_products(gpu, oracle):
+    """Polynomials of >= 2^12 entries sharing a point are evaluated as dot
+    products with one eq table; values equal the single evaluations and the
+    oracle's."""
+    import random
+    rng = random.Random(22)
+    R = 0x73EDA753299D7D483339D80809A1D80553BDA402FFFE5BFEFFFFFFFF00000001
+    nv = 13
+    p1 = [rng.randrange(R) for _ in range(nv)]
+    p2 = [rng.randrange(R) for _ in range(nv)]
+    tables = [oracle.random_fr(600 + i, 1 << nv) for i in range(5)]
+    mles = [gpu.mle_from_evaluations(nv, t) for t in tables]
+    points = [p1, p2, p1, p1, p2]
+    many = gpu.evaluate_many(mles, points)
+    assert many == [gpu.evaluate_mle(m, p) for m, p in zip(mles, points)]
+    cpu = oracle.CpuBackend()
+    assert many == [cpu.evaluate_mle(cpu.mle_from_evaluations(nv, t), p) for t, p in zip(tables, points)]
