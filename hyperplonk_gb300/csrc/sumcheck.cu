@@ -200,21 +200,11 @@ __global__ void __launch_bounds__(kRoundThreads) k_sumcheck_round_regs(SumcheckD
 // the slot sum for x <= m and to the reference's barycentric extrapolation
 // (backend/src/cpu/sum_check.rs:183-217) beyond.  Writes the d+1 canonical
 // evaluations.
-__global__ void k_sumcheck_finalize(SumcheckDesc desc, const Fr *partials, int blocks,
-                                    const Fr *coefs, int degree, Fr *slot_sums, Fr *out) {
-    extern __shared__ Fr sums[];
-    const int S = desc.slot_count;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
-    for (int s = warp; s < S; s += warps) {
-        Fr a = Fr::zero();
-        for (int b = lane; b < blocks; b += 32) a = a + partials[size_t(s) * blocks + b];
-        a = warp_sum(a);
-        if (lane == 0) {
-            sums[s] = a;
-            slot_sums[s] = a;
-        }
-    }
-    __syncthreads();
+// Given the slot sums in shared memory (all threads of the block): turn each
+// product's m+1 sums into forward differences in place, then thread x writes
+// the canonical round evaluation at t = x.
+__device__ __forceinline__ void finalize_from_sums(const SumcheckDesc &desc, Fr *sums, const Fr *coefs, int degree,
+                                                   Fr *out) {
     for (int p = threadIdx.x; p < desc.product_count; p += blockDim.x) {
         Fr *v = sums + desc.slot_base[p];
         const int m = desc.offsets[p + 1] - desc.offsets[p];
@@ -240,6 +230,86 @@ __global__ void k_sumcheck_finalize(SumcheckDesc desc, const Fr *partials, int b
         }
         out[x] = from_mont(acc);
     }
+}
+
+__global__ void k_sumcheck_finalize(SumcheckDesc desc, const Fr *partials, int blocks,
+                                    const Fr *coefs, int degree, Fr *slot_sums, Fr *out) {
+    extern __shared__ Fr sums[];
+    const int S = desc.slot_count;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+    for (int s = warp; s < S; s += warps) {
+        Fr a = Fr::zero();
+        for (int b = lane; b < blocks; b += 32) a = a + partials[size_t(s) * blocks + b];
+        a = warp_sum(a);
+        if (lane == 0) {
+            sums[s] = a;
+            slot_sums[s] = a;
+        }
+    }
+    __syncthreads();
+    finalize_from_sums(desc, sums, coefs, degree, out);
+}
+
+// A round of at most kSmallPairs pairs in one block, finalize included (the
+// last rounds of every sumcheck: latency-bound, so the work is spread over
+// (factor, pair) and (product, pair) items instead of one pair per thread).
+constexpr int kSmallPairs = 64;
+constexpr int kSmallThreads = 256;
+
+template <int MAXM>
+__global__ void __launch_bounds__(kSmallThreads) k_sumcheck_round_small(SumcheckDesc desc, FrPtrList src,
+                                                                        FrMutPtrList dst, FrPtrList rd, bool fold,
+                                                                        Fr r, int pairs, const Fr *coefs, int degree,
+                                                                        Fr *out) {
+    extern __shared__ Fr sm[];  // vals[S][kSmallPairs], then sums[S]
+    const int S = desc.slot_count, F = desc.factor_count;
+    Fr *vals = sm, *sums = sm + size_t(S) * kSmallPairs;
+    if (fold) {
+        for (int idx = threadIdx.x; idx < F * pairs; idx += blockDim.x) {
+            const int f = idx / pairs, b = idx % pairs;
+            const Fr *q = src.p[f] + 4 * b;
+            Fr a0 = load_fr(q), a1 = load_fr(q + 1), a2 = load_fr(q + 2), a3 = load_fr(q + 3);
+            Fr *d = dst.p[f] + 2 * b;
+            store_fr(d, a0 + r * (a1 - a0));
+            store_fr(d + 1, a2 + r * (a3 - a2));
+        }
+        __syncthreads();  // the folded tables are read below by other threads
+    }
+    for (int idx = threadIdx.x; idx < desc.product_count * pairs; idx += blockDim.x) {
+        const int p = idx / pairs, b = idx % pairs;
+        const int begin = desc.offsets[p], m = desc.offsets[p + 1] - begin, slot = desc.slot_base[p];
+        Fr e[MAXM], st[MAXM];
+#pragma unroll
+        for (int j = 0; j < MAXM; j++) {
+            if (j < m) {
+                const Fr *q = rd.p[desc.indices[begin + j]] + 2 * b;
+                e[j] = load_fr(q);
+                st[j] = load_fr(q + 1) - e[j];
+            }
+        }
+        for (int k = 0; k <= m; k++) {
+            if (k > 0) {
+#pragma unroll
+                for (int j = 0; j < MAXM; j++)
+                    if (j < m) e[j] = e[j] + st[j];
+            }
+            Fr v = e[0];
+#pragma unroll
+            for (int j = 1; j < MAXM; j++)
+                if (j < m) v = v * e[j];
+            vals[(slot + k) * kSmallPairs + b] = v;
+        }
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int s = warp; s < S; s += kSmallThreads / 32) {
+        Fr v = lane < pairs ? vals[s * kSmallPairs + lane] : Fr::zero();
+        if (lane + 32 < pairs) v = v + vals[s * kSmallPairs + lane + 32];
+        v = warp_sum(v);
+        if (lane == 0) sums[s] = v;
+    }
+    __syncthreads();
+    finalize_from_sums(desc, sums, coefs, degree, out);
 }
 
 __global__ void k_sumcheck_final_fold(FrPtrList tables, int count, Fr r, Fr *out) {
@@ -395,6 +465,23 @@ static void enqueue_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, cons
         rd.p[f] = fold ? dst.p[f] : src.p[f];
     }
     const bool regs = d.max_arity <= 8 && d.slot_count <= kMaxSlotsV2;
+    if (regs && pairs <= size_t(kSmallPairs)) {
+        int tok = ctx->prof_begin("sumcheck_round", st);
+        const size_t smem = size_t(d.slot_count) * (kSmallPairs + 1) * sizeof(Fr);
+        auto launch = [&](auto kernel) {
+            if (smem > 48 * 1024)
+                check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+            kernel<<<1, kSmallThreads, smem, st>>>(d, src, dst, rd, fold, r, int(pairs),
+                                                   static_cast<const Fr *>(s->coefs), int(s->max_degree), out_dev);
+        };
+        if (d.max_arity <= 2) launch(k_sumcheck_round_small<2>);
+        else if (d.max_arity <= 4) launch(k_sumcheck_round_small<4>);
+        else if (d.max_arity <= 6) launch(k_sumcheck_round_small<6>);
+        else launch(k_sumcheck_round_small<8>);
+        check_launch();
+        ctx->prof_end(tok, st);
+        return;
+    }
     unsigned grid;
     Scratch partials, sums(ctx, d.slot_count * sizeof(Fr), st);
     int tok = ctx->prof_begin("sumcheck_round", st);
