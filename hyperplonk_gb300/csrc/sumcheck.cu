@@ -135,10 +135,48 @@ __device__ __forceinline__ Fr warp_sum(Fr v) {
     return v;
 }
 
+__device__ void finalize_from_sums(const SumcheckDesc &desc, Fr *sums, const Fr *coefs, int degree, Fr *out);
+
+__device__ __forceinline__ Fr load_fr_cg(const Fr *p) {  // L2 load: written by other blocks of this launch
+    const uint4 *q = reinterpret_cast<const uint4 *>(p);
+    const uint4 a = __ldcg(q), b = __ldcg(q + 1);
+    Fr r;
+    r.v[0] = a.x; r.v[1] = a.y; r.v[2] = a.z; r.v[3] = a.w;
+    r.v[4] = b.x; r.v[5] = b.y; r.v[6] = b.z; r.v[7] = b.w;
+    return r;
+}
+
+// After the block partials (slot-major) are written: the last block of the
+// launch to finish (a counter per prover state, reset by that block) sums
+// them and writes the round message -- no separate finalize launch.
+__device__ __forceinline__ void finish_round_in_last_block(const SumcheckDesc &desc, const Fr *partials,
+                                                           unsigned *counter, const Fr *coefs, int degree,
+                                                           Fr *out, Fr *sums) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    const int S = desc.slot_count, blocks = gridDim.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+    for (int s = warp; s < S; s += warps) {
+        Fr a = Fr::zero();
+        for (int b = lane; b < blocks; b += 32) a = a + load_fr_cg(&partials[size_t(s) * blocks + b]);
+        a = warp_sum(a);
+        if (lane == 0) sums[s] = a;
+    }
+    __syncthreads();
+    finalize_from_sums(desc, sums, coefs, degree, out);
+    if (threadIdx.x == 0) *counter = 0u;
+}
+
 template <int MAXM>
 __global__ void __launch_bounds__(kRoundThreads) k_sumcheck_round_regs(SumcheckDesc desc, FrPtrList src,
                                                                        FrMutPtrList dst, FrPtrList rd, bool fold,
-                                                                       Fr r, size_t pairs, Fr *partials) {
+                                                                       Fr r, size_t pairs, Fr *partials,
+                                                                       unsigned *counter, const Fr *coefs,
+                                                                       int degree, Fr *out) {
     // acc[s * kRoundThreads + t]: thread t's running sum of slot s over its pairs
     extern __shared__ Fr acc[];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -189,6 +227,8 @@ __global__ void __launch_bounds__(kRoundThreads) k_sumcheck_round_regs(SumcheckD
         v = warp_sum(v);
         if (lane == 0) partials[size_t(s) * gridDim.x + blockIdx.x] = v;  // slot-major
     }
+    __syncthreads();  // acc is reused below as the last block's slot sums
+    finish_round_in_last_block(desc, partials, counter, coefs, degree, out, acc);
 }
 
 // One block.  Warp w sums the block partials of slots w, w + warps, ... (lane
@@ -203,8 +243,7 @@ __global__ void __launch_bounds__(kRoundThreads) k_sumcheck_round_regs(SumcheckD
 // Given the slot sums in shared memory (all threads of the block): turn each
 // product's m+1 sums into forward differences in place, then thread x writes
 // the canonical round evaluation at t = x.
-__device__ __forceinline__ void finalize_from_sums(const SumcheckDesc &desc, Fr *sums, const Fr *coefs, int degree,
-                                                   Fr *out) {
+__device__ void finalize_from_sums(const SumcheckDesc &desc, Fr *sums, const Fr *coefs, int degree, Fr *out) {
     for (int p = threadIdx.x; p < desc.product_count; p += blockDim.x) {
         Fr *v = sums + desc.slot_base[p];
         const int m = desc.offsets[p + 1] - desc.offsets[p];
@@ -346,6 +385,11 @@ static const Fr *state_table(HpCudaSumCheckProverState *s, int which, int f) {
     return static_cast<const Fr *>(s->fold_b) + f * b_stride;
 }
 
+static unsigned *round_counter(HpCudaSumCheckProverState *s) {
+    const size_t p = std::max(size_t(s->desc.product_count), size_t(1));
+    return reinterpret_cast<unsigned *>(static_cast<Fr *>(s->coefs) + p);
+}
+
 static void release_state(HpCudaContext *ctx, HpCudaSumCheckProverState *s) {
     for (void *p : s->inputs) {
         try { ctx->unref(p); } catch (...) {}
@@ -415,8 +459,12 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_create(
                 ctx->ref(factors[f]);
                 s->inputs.push_back(factors[f]);
             }
-            s->coefs = ctx->scratch(std::max(product_count, size_t(1)) * sizeof(Fr));
+            // coefficients, then one zeroed Fr slot whose first word is the
+            // round kernels' last-block counter
+            s->coefs = ctx->scratch((std::max(product_count, size_t(1)) + 1) * sizeof(Fr));
             hp::host_scalars_to_device(ctx, coefficients, product_count, static_cast<Fr *>(s->coefs));
+            check_cuda(cudaMemsetAsync(static_cast<Fr *>(s->coefs) + std::max(product_count, size_t(1)), 0,
+                                       sizeof(Fr), ctx->stream));
             size_t a_len = hp::table_len(num_vars - 1);
             size_t b_len = num_vars >= 2 ? hp::table_len(num_vars - 2) : 1;
             size_t fcount = std::max(factor_count, size_t(1));
@@ -469,7 +517,7 @@ static void enqueue_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, cons
         int tok = ctx->prof_begin("sumcheck_round", st);
         const size_t smem = size_t(d.slot_count) * (kSmallPairs + 1) * sizeof(Fr);
         auto launch = [&](auto kernel) {
-            if (smem > 48 * 1024)
+            if (smem > 32 * 1024)
                 check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
             kernel<<<1, kSmallThreads, smem, st>>>(d, src, dst, rd, fold, r, int(pairs),
                                                    static_cast<const Fr *>(s->coefs), int(s->max_degree), out_dev);
@@ -490,15 +538,21 @@ static void enqueue_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, cons
         partials = Scratch(ctx, size_t(grid) * d.slot_count * sizeof(Fr), st);
         const size_t smem = size_t(d.slot_count) * kRoundThreads * sizeof(Fr);
         auto launch = [&](auto kernel) {
-            if (smem > 48 * 1024)
+            // the kernel's own static shared memory counts against the same
+            // 48 KiB default, so opt in well before the dynamic size reaches it
+            if (smem > 32 * 1024)
                 check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-            kernel<<<grid, kRoundThreads, smem, st>>>(d, src, dst, rd, fold, r, pairs, partials.as<Fr>());
+            kernel<<<grid, kRoundThreads, smem, st>>>(d, src, dst, rd, fold, r, pairs, partials.as<Fr>(),
+                                                      round_counter(s), static_cast<const Fr *>(s->coefs),
+                                                      int(s->max_degree), out_dev);
         };
         if (d.max_arity <= 2) launch(k_sumcheck_round_regs<2>);
         else if (d.max_arity <= 4) launch(k_sumcheck_round_regs<4>);
         else if (d.max_arity <= 6) launch(k_sumcheck_round_regs<6>);
         else launch(k_sumcheck_round_regs<8>);
         check_launch();
+        ctx->prof_end(tok, st);
+        return;
     } else {
         size_t smem;
         int T = round_block_size(d, &smem);
