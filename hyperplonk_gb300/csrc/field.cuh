@@ -40,7 +40,8 @@ __device__ __forceinline__ uint32_t subc(uint32_t a, uint32_t b) {
 struct FrParams {
     static constexpr int N = 8;
     static constexpr uint32_t INV = 0xffffffffu;
-    __device__ __forceinline__ static uint32_t p(int i) {
+    static constexpr bool LAZY = false;  // 4r > 2^256: values kept in [0, r)
+    __host__ __device__ __forceinline__ static uint32_t p(int i) {
         constexpr uint32_t P[8] = {0x00000001u, 0xffffffffu, 0xfffe5bfeu, 0x53bda402u,
                                    0x09a1d805u, 0x3339d808u, 0x299d7d48u, 0x73eda753u};
         return P[i];
@@ -57,10 +58,21 @@ struct FrParams {
     }
 };
 
+// Fq values are kept in [0, 2p) between operations ("lazy" reduction): as
+// 4p < 2^384 = R, a Montgomery product of two such values is already < 2p
+// without its final subtraction; sums and differences reduce against 2p; a
+// value is zero when it is 0 or p; from_mont returns the canonical value.
 struct FqParams {
     static constexpr int N = 12;
     static constexpr uint32_t INV = 0xfffcfffdu;
-    __device__ __forceinline__ static uint32_t p(int i) {
+    static constexpr bool LAZY = true;
+    __device__ __forceinline__ static uint32_t p2(int i) {
+        constexpr uint32_t P2[12] = {0xffff5556u, 0x73fdffffu, 0x62a7ffffu, 0x3d57fffdu,
+                                     0xed61ec48u, 0xce61a541u, 0xe70a257eu, 0xc8ee9709u,
+                                     0x869759aeu, 0x96374f6cu, 0x72ffcd34u, 0x340223d4u};
+        return P2[i];
+    }
+    __host__ __device__ __forceinline__ static uint32_t p(int i) {
         constexpr uint32_t P[12] = {0xffffaaabu, 0xb9feffffu, 0xb153ffffu, 0x1eabfffeu,
                                     0xf6b0f624u, 0x6730d2a0u, 0xf38512bfu, 0x64774b84u,
                                     0x434bacd7u, 0x4b1ba7b6u, 0x397fe69au, 0x1a0111eau};
@@ -98,17 +110,15 @@ struct Field {
         return r;
     }
     __host__ __device__ __forceinline__ bool is_zero() const {
-        uint32_t acc = 0;
+        uint32_t acc = 0, accp = 0;
 #pragma unroll
-        for (int i = 0; i < N; i++) acc |= v[i];
-        return acc == 0;
+        for (int i = 0; i < N; i++) {
+            acc |= v[i];
+            accp |= v[i] ^ P::p(i);
+        }
+        return acc == 0 || (P::LAZY && accp == 0);
     }
-    __device__ __forceinline__ bool operator==(const Field &o) const {
-        uint32_t acc = 0;
-#pragma unroll
-        for (int i = 0; i < N; i++) acc |= v[i] ^ o.v[i];
-        return acc == 0;
-    }
+    __device__ __forceinline__ bool operator==(const Field &o) const;
     __device__ __forceinline__ bool operator!=(const Field &o) const { return !(*this == o); }
 };
 
@@ -128,6 +138,19 @@ __device__ __forceinline__ void reduce_once(Field<P> &r, uint32_t hi) {
     for (int i = 0; i < N; i++) r.v[i] = borrow ? r.v[i] : t[i];
 }
 
+// r = a - 2p if a >= 2p (lazy Fq: a < 4p < 2^384, no carry-out limb)
+template <class P>
+__device__ __forceinline__ void reduce_2p(Field<P> &r) {
+    constexpr int N = P::N;
+    uint32_t t[N];
+    t[0] = sub_cc(r.v[0], P::p2(0));
+#pragma unroll
+    for (int i = 1; i < N; i++) t[i] = subc_cc(r.v[i], P::p2(i));
+    uint32_t borrow = subc(0, 0);
+#pragma unroll
+    for (int i = 0; i < N; i++) r.v[i] = borrow ? r.v[i] : t[i];
+}
+
 template <class P>
 __device__ __forceinline__ Field<P> operator+(const Field<P> &a, const Field<P> &b) {
     constexpr int N = P::N;
@@ -136,7 +159,12 @@ __device__ __forceinline__ Field<P> operator+(const Field<P> &a, const Field<P> 
 #pragma unroll
     for (int i = 1; i < N; i++) r.v[i] = addc_cc(a.v[i], b.v[i]);
     uint32_t hi = addc(0, 0);
-    reduce_once<P>(r, hi);
+    if constexpr (P::LAZY) {
+        (void)hi;
+        reduce_2p<P>(r);
+    } else {
+        reduce_once<P>(r, hi);
+    }
     return r;
 }
 
@@ -148,11 +176,16 @@ __device__ __forceinline__ Field<P> operator-(const Field<P> &a, const Field<P> 
 #pragma unroll
     for (int i = 1; i < N; i++) r.v[i] = subc_cc(a.v[i], b.v[i]);
     uint32_t borrow = subc(0, 0);  // 0xffffffff on borrow
-    uint32_t t[N];
-    t[0] = add_cc(r.v[0], P::p(0) & borrow);
+    uint32_t t[N], m[N];
 #pragma unroll
-    for (int i = 1; i < N - 1; i++) t[i] = addc_cc(r.v[i], P::p(i) & borrow);
-    t[N - 1] = addc(r.v[N - 1], P::p(N - 1) & borrow);
+    for (int i = 0; i < N; i++) {
+        if constexpr (P::LAZY) m[i] = P::p2(i) & borrow;
+        else m[i] = P::p(i) & borrow;
+    }
+    t[0] = add_cc(r.v[0], m[0]);
+#pragma unroll
+    for (int i = 1; i < N - 1; i++) t[i] = addc_cc(r.v[i], m[i]);
+    t[N - 1] = addc(r.v[N - 1], m[N - 1]);
 #pragma unroll
     for (int i = 0; i < N; i++) r.v[i] = t[i];
     return r;
@@ -212,7 +245,7 @@ __device__ __forceinline__ Field<P> mont_mul_wide(const Field<P> &a, const Field
     Field<P> r;
 #pragma unroll
     for (int i = 0; i < N; i++) r.v[i] = t[i];
-    reduce_once<P>(r, t[N]);
+    if constexpr (!P::LAZY) reduce_once<P>(r, t[N]);  // lazy: already < 2p
     return r;
 }
 
@@ -275,7 +308,7 @@ __device__ __forceinline__ Field<P> mont_sqr_wide(const Field<P> &a) {
     Field<P> r;
 #pragma unroll
     for (int i = 0; i < N; i++) r.v[i] = T[N + i];
-    reduce_once<P>(r, c2);
+    if constexpr (!P::LAZY) reduce_once<P>(r, c2);  // lazy: already < 2p
     return r;
 }
 
@@ -376,7 +409,7 @@ __device__ __forceinline__ Field<FqParams> fq_mul_karatsuba(const Field<FqParams
     Field<FqParams> r;
 #pragma unroll
     for (int i = 0; i < 12; i++) r.v[i] = T[12 + i];
-    reduce_once<FqParams>(r, c2);
+    (void)c2;  // lazy Fq: the result is < 2p < 2^382, c2 = 0
     return r;
 }
 
@@ -480,7 +513,26 @@ template <class P>
 __device__ __forceinline__ Field<P> from_mont(const Field<P> &a) {
     Field<P> one = Field<P>::zero();
     one.v[0] = 1;
-    return a * one;
+    Field<P> r = a * one;
+    if constexpr (P::LAZY) reduce_once<P>(r, 0u);  // [0, 2p) -> canonical
+    return r;
+}
+
+// The value in [0, p) (lazy Fq values may hold v + p).
+template <class P>
+__device__ __forceinline__ Field<P> canonical(const Field<P> &a) {
+    Field<P> r = a;
+    if constexpr (P::LAZY) reduce_once<P>(r, 0u);
+    return r;
+}
+
+template <class P>
+__device__ __forceinline__ bool Field<P>::operator==(const Field<P> &o) const {
+    const Field<P> a = canonical(*this), b = canonical(o);
+    uint32_t acc = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++) acc |= a.v[i] ^ b.v[i];
+    return acc == 0;
 }
 
 // True if the integer held in a is < p (canonical).

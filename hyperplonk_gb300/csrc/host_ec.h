@@ -39,6 +39,12 @@ inline void fq_sub_p(uint64_t *a) {
         borrow = (d >> 64) & 1;
     }
 }
+// [0, 2p) -> [0, p): device Fq values are kept below 2p between operations.
+inline Fq64 fq_canonical(Fq64 a) {
+    if (fq_geq_p(a.v)) fq_sub_p(a.v);
+    return a;
+}
+
 inline Fq64 fq_add(const Fq64 &a, const Fq64 &b) {
     Fq64 r;
     unsigned __int128 c = 0;

@@ -930,15 +930,23 @@ void msm_run_many(HpCudaContext *ctx, const MsmTask *tasks, size_t count, Xyzz *
     ctx->prof_end(whole, st);
 }
 
-host::Xyzz64 msm_combine_host(const MsmShape &shape, const host::Xyzz64 *partials) {
+host::Xyzz64 msm_combine_host(const MsmShape &shape, const host::Xyzz64 *device_partials) {
+    // device coordinates are in [0, 2p): canonical first
+    std::vector<host::Xyzz64> partials(device_partials, device_partials + shape.partials);
+    for (auto &q : partials) {
+        q.x = host::fq_canonical(q.x);
+        q.y = host::fq_canonical(q.y);
+        q.zz = host::fq_canonical(q.zz);
+        q.zzz = host::fq_canonical(q.zzz);
+    }
     // result = A + seg * sum_k 2^k T_k, A = partials[bits], T_k = partials[k]
     host::Xyzz64 h = host::xyzz_inf();
     for (int k = shape.seg_bits - 1; k >= 0; k--) {
         h = host::xyzz_double(h);
-        h = host::xyzz_add(h, partials[k]);
+        h = host::xyzz_add(h, partials[size_t(k)]);
     }
     for (size_t s = shape.seg; s > 1; s >>= 1) h = host::xyzz_double(h);
-    return host::xyzz_add(partials[shape.seg_bits], h);
+    return host::xyzz_add(partials[size_t(shape.seg_bits)], h);
 }
 
 host::Xyzz64 msm_result_host(const MsmLayer &layer, const host::Xyzz64 *partials) {
