@@ -226,8 +226,8 @@ extern "C" HpCudaStatus hp_cuda_v1_multilinear_kzg_open(
         hp::Scratch fa(ctx, hp::table_len(nv - 1) * sizeof(Fr));
         hp::Scratch fb(ctx, hp::table_len(nv >= 2 ? nv - 2 : 0) * sizeof(Fr));
         // all quotients first (q_i at offset 2^nv - 2^(nv-i)), then their MSMs
-        // overlap on the worker streams: the late rounds' MSMs are tiny and
-        // latency bound one at a time
+        // together (run_msms): the late rounds' MSMs are tiny and latency
+        // bound one at a time
         hp::Scratch q(ctx, hp::table_len(nv) * sizeof(Fr));
         const Fr *cur = f;
         Fr *bufs[2] = {fa.as<Fr>(), fb.as<Fr>()};

@@ -8,14 +8,17 @@
 //     s(t) = sum_b prod_j (f_j[2b] + t*(f_j[2b+1] - f_j[2b]))   for t = 0..m,
 // scales by the product coefficient and extends the degree-m polynomial to
 // t = 0..max_degree.  The reference extends with barycentric weights; this
-// backend extends with forward differences over the integer nodes, which
-// yields the same field elements (the degree-m interpolant is unique).
+// backend evaluates Newton's forward-difference form over the integer nodes,
+// which yields the same field elements (the degree-m interpolant is unique).
 //
 // GB300 shape: one launch per round fuses the fold of round k-1's challenge
 // with the message of round k, so each factor table is read once and its
-// folded half written once per round.  Per-thread partial sums stay in shared
-// memory, are tree-reduced per block, and a one-block finalize kernel sums
-// the block partials, extrapolates, scales and converts to canonical bytes.
+// folded half written once per round.  Per-thread slot sums stay in shared
+// memory and are reduced once per block; the last block of the launch sums
+// the block partials, extrapolates, scales and writes canonical bytes.
+// Rounds of <= 64 pairs run in one block (fold, products and finalize in one
+// launch); products of arity > 8 or more than 48 slots use a shared-memory
+// kernel and a separate one-block finalize.
 #include <algorithm>
 #include <cstring>
 #include <vector>
