@@ -25,8 +25,8 @@ overlap one lane's host work (transcript, serialisation) and latency-bound
 phases with another's device work; a lane's proofs wait for each other at
 every coalesced step, so few slots per lane and several lanes serve a
 mixed-size stream best (measured on GB300, nv 16..22 at 1.5x the plain
-capacity: 4 lanes x 2 slots or 6 x 1 about 1.3x the plain throughput,
-2 lanes x 6 slots 1.07x).
+capacity with pinned request witnesses: 4 lanes x 2 slots 1.09x the plain
+throughput; with 2 lanes x 6 slots about the same as plain).
 
 Each proof is byte-identical to the same request proven alone: the device
 work of a proof does not depend on what it is batched with (tests check it).
