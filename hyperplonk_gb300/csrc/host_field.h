@@ -121,5 +121,36 @@ inline Fr64 one() {
     return r;
 }
 
+inline Fr64 neg(const Fr64 &a) {
+    if (is_zero(a)) return a;
+    Fr64 r;
+    unsigned __int128 borrow = 0;
+    for (int i = 0; i < 4; i++) {
+        unsigned __int128 d = (unsigned __int128)kFrP[i] - a.v[i] - borrow;
+        r.v[i] = (uint64_t)d;
+        borrow = (d >> 64) & 1;
+    }
+    return r;
+}
+
+// Montgomery form of the integer k (k < 2^64, so k < r).
+inline Fr64 from_u64(uint64_t k) {
+    Fr64 raw = {{k, 0, 0, 0}}, r2;
+    std::memcpy(r2.v, kFrR2, 32);
+    return mont_mul(raw, r2);
+}
+
+// a^(r-2) = a^-1 for a != 0 (Fermat), Montgomery in and out.
+inline Fr64 inverse(const Fr64 &a) {
+    uint64_t e[4] = {kFrP[0] - 2, kFrP[1], kFrP[2], kFrP[3]};
+    Fr64 acc = one();
+    for (int i = 3; i >= 0; i--)
+        for (int b = 63; b >= 0; b--) {
+            acc = mont_mul(acc, acc);
+            if ((e[i] >> b) & 1) acc = mont_mul(acc, a);
+        }
+    return acc;
+}
+
 }  // namespace host
 }  // namespace hp

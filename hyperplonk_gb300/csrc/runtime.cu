@@ -1,6 +1,7 @@
 // runtime.cu -- context lifetime, buffer registry, retirement.
 // ABI: hp_cuda_v1_context_create / _destroy / _buffer_retire / _context_stream
 // (reference bridge.h:43-45, bridge_runtime.cpp).
+#include <algorithm>
 #include <atomic>
 #include <cstring>
 
@@ -27,6 +28,32 @@ void *HpCudaContext::scratch(size_t bytes, cudaStream_t s) {
     void *p = nullptr;
     check_cuda(cudaMallocFromPoolAsync(&p, bytes ? bytes : 16, pool, s ? s : stream));
     return p;
+}
+
+uint8_t *HpCudaContext::mailbox(size_t bytes, void **dev) {
+    if (bytes > mailbox_bytes) {
+        if (h_mailbox) {
+            check_cuda(cudaStreamSynchronize(stream));
+            check_cuda(cudaFreeHost(h_mailbox));
+            h_mailbox = nullptr;
+            d_mailbox = nullptr;
+            mailbox_bytes = 0;
+        }
+        const size_t n = std::max<size_t>(bytes, 4096);
+        void *h = nullptr;
+        check_cuda(cudaHostAlloc(&h, n, cudaHostAllocMapped));
+        void *d = nullptr;
+        cudaError_t e = cudaHostGetDevicePointer(&d, h, 0);
+        if (e != cudaSuccess) {
+            cudaFreeHost(h);
+            check_cuda(e);
+        }
+        h_mailbox = static_cast<uint8_t *>(h);
+        d_mailbox = d;
+        mailbox_bytes = n;
+    }
+    *dev = d_mailbox;
+    return h_mailbox;
 }
 
 void HpCudaContext::scratch_free(void *p, cudaStream_t s) {
@@ -197,6 +224,7 @@ extern "C" HpCudaStatus hp_cuda_v1_context_destroy(HpCudaContext *ctx) {
         if (ctx->fork_event) cudaEventDestroy(ctx->fork_event);
         cudaFree(ctx->d_flags);
         cudaFreeHost(ctx->h_flags);
+        if (ctx->h_mailbox) cudaFreeHost(ctx->h_mailbox);
         cudaStreamDestroy(ctx->stream);
         cudaMemPoolDestroy(ctx->pool);
         delete ctx;

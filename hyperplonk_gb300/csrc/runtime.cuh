@@ -128,6 +128,14 @@ struct HpCudaContext {
     int prof_begin(const char *name, cudaStream_t s = nullptr);
     void prof_end(int token, cudaStream_t s = nullptr);
     void prof_resolve();
+    // Pinned, device-mapped host memory for small per-round results that a
+    // kernel writes straight into host memory (no copy launch, no staging);
+    // grown on demand.  Calls on one context are not concurrent.
+    uint8_t *h_mailbox = nullptr;
+    void *d_mailbox = nullptr;
+    size_t mailbox_bytes = 0;
+    // Host pointer to >= `bytes` of the mailbox; *dev gets its device alias.
+    uint8_t *mailbox(size_t bytes, void **dev);
     // Clear the device status word (stream ordered).
     void clear_flags();
     // Synchronize and return the status word.

@@ -1,5 +1,5 @@
 // sumcheck.cu -- SumCheck prover state and the fused fold + round-message
-// kernel.
+// kernels.
 //
 // Reference semantics: backend/src/cpu/sum_check.rs:35-217.  Round k (1-based)
 // first fixes the lowest variable of every distinct factor with the previous
@@ -8,18 +8,21 @@
 //     s(t) = sum_b prod_j (f_j[2b] + t*(f_j[2b+1] - f_j[2b]))   for t = 0..m,
 // scales by the product coefficient and extends the degree-m polynomial to
 // t = 0..max_degree.  The reference extends with barycentric weights; this
-// backend evaluates Newton's forward-difference form over the integer nodes,
-// which yields the same field elements (the degree-m interpolant is unique).
+// backend applies a per-state matrix of coefficient-scaled Lagrange weights
+// over the integer nodes to the slot sums, which yields the same field
+// elements (the degree-m interpolant is unique).
 //
 // GB300 shape: one launch per round fuses the fold of round k-1's challenge
 // with the message of round k, so each factor table is read once and its
-// folded half written once per round.  Per-thread slot sums stay in shared
-// memory and are reduced once per block; the last block of the launch sums
+// folded half written once per round, and the last block of the launch sums
 // the block partials, extrapolates, scales and writes canonical bytes.
-// Rounds of <= 64 pairs run in one block (fold, products and finalize in one
-// launch); products of arity > 8 or more than 48 slots use a shared-memory
-// kernel and a separate one-block finalize.
+// Large rounds: one pair per thread, per-thread slot sums in shared memory.
+// Rounds of up to a few thousand pairs: one (slot, pair) item per thread,
+// so the latency chain per thread is one product, not the whole polynomial.
+// Products of arity > 8 or more than 48 slots use a shared-memory kernel and
+// a separate one-block finalize.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -138,7 +141,8 @@ __device__ __forceinline__ Fr warp_sum(Fr v) {
     return v;
 }
 
-__device__ void finalize_from_sums(const SumcheckDesc &desc, Fr *sums, const Fr *coefs, int degree, Fr *out);
+__device__ void finalize_from_sums(const SumcheckDesc &desc, const Fr *sums, const Fr *weights, int degree,
+                                   Fr *out);
 
 __device__ __forceinline__ Fr load_fr_cg(const Fr *p) {  // L2 load: written by other blocks of this launch
     const uint4 *q = reinterpret_cast<const uint4 *>(p);
@@ -153,24 +157,24 @@ __device__ __forceinline__ Fr load_fr_cg(const Fr *p) {  // L2 load: written by 
 // launch to finish (a counter per prover state, reset by that block) sums
 // them and writes the round message -- no separate finalize launch.
 __device__ __forceinline__ void finish_round_in_last_block(const SumcheckDesc &desc, const Fr *partials,
-                                                           unsigned *counter, const Fr *coefs, int degree,
-                                                           Fr *out, Fr *sums) {
+                                                           int per_slot, unsigned *counter, const Fr *weights,
+                                                           int degree, Fr *out, Fr *sums) {
     __shared__ bool last;
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
     __syncthreads();
     if (!last) return;
-    const int S = desc.slot_count, blocks = gridDim.x;
+    const int S = desc.slot_count;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
     for (int s = warp; s < S; s += warps) {
         Fr a = Fr::zero();
-        for (int b = lane; b < blocks; b += 32) a = a + load_fr_cg(&partials[size_t(s) * blocks + b]);
+        for (int b = lane; b < per_slot; b += 32) a = a + load_fr_cg(&partials[size_t(s) * per_slot + b]);
         a = warp_sum(a);
         if (lane == 0) sums[s] = a;
     }
     __syncthreads();
-    finalize_from_sums(desc, sums, coefs, degree, out);
+    finalize_from_sums(desc, sums, weights, degree, out);
     if (threadIdx.x == 0) *counter = 0u;
 }
 
@@ -178,7 +182,7 @@ template <int MAXM>
 __global__ void __launch_bounds__(kRoundThreads) k_sumcheck_round_regs(SumcheckDesc desc, FrPtrList src,
                                                                        FrMutPtrList dst, FrPtrList rd, bool fold,
                                                                        Fr r, size_t pairs, Fr *partials,
-                                                                       unsigned *counter, const Fr *coefs,
+                                                                       unsigned *counter, const Fr *weights,
                                                                        int degree, Fr *out) {
     // acc[s * kRoundThreads + t]: thread t's running sum of slot s over its pairs
     extern __shared__ Fr acc[];
@@ -231,51 +235,222 @@ __global__ void __launch_bounds__(kRoundThreads) k_sumcheck_round_regs(SumcheckD
         if (lane == 0) partials[size_t(s) * gridDim.x + blockIdx.x] = v;  // slot-major
     }
     __syncthreads();  // acc is reused below as the last block's slot sums
-    finish_round_in_last_block(desc, partials, counter, coefs, degree, out, acc);
+    finish_round_in_last_block(desc, partials, int(gridDim.x), counter, weights, degree, out, acc);
 }
 
-// One block.  Warp w sums the block partials of slots w, w + warps, ... (lane
-// strided loads, then shuffles) into shared memory and slot_sums.  Thread p
-// then turns product p's m+1 sums v(0..m) into its forward differences
-// Delta^j v(0) in place, and thread x evaluates the round polynomial at t = x
-// as sum_p coef_p sum_{j <= min(x, m)} C(x, j) Delta^j v_p(0) -- Newton's
-// form of the unique polynomial of degree <= m through the sums, so equal to
-// the slot sum for x <= m and to the reference's barycentric extrapolation
-// (backend/src/cpu/sum_check.rs:183-217) beyond.  Writes the d+1 canonical
-// evaluations.
-// Given the slot sums in shared memory (all threads of the block): turn each
-// product's m+1 sums into forward differences in place, then thread x writes
-// the canonical round evaluation at t = x.
-__device__ void finalize_from_sums(const SumcheckDesc &desc, Fr *sums, const Fr *coefs, int degree, Fr *out) {
-    for (int p = threadIdx.x; p < desc.product_count; p += blockDim.x) {
-        Fr *v = sums + desc.slot_base[p];
-        const int m = desc.offsets[p + 1] - desc.offsets[p];
-        for (int j = 1; j <= m; j++)
-            for (int i = m; i >= j; i--) v[i] = v[i] - v[i - 1];  // v[i] = Delta^j v(i - j)
-    }
-    __syncthreads();
-    for (int x = threadIdx.x; x <= degree; x += blockDim.x) {
-        Fr acc = Fr::zero();
-        for (int p = 0; p < desc.product_count; p++) {
-            const Fr *v = sums + desc.slot_base[p];
-            const int m = desc.offsets[p + 1] - desc.offsets[p];
-            Fr val = v[0];
-            uint64_t c = 1;  // C(x, j); C(64, j) < 2^61
-            for (int j = 1; j <= m && j <= x; j++) {
-                c = uint64_t((unsigned __int128)c * uint64_t(x - j + 1) / uint64_t(j));
-                Fr cj = Fr::zero();
-                cj.v[0] = uint32_t(c);
-                cj.v[1] = uint32_t(c >> 32);
-                val = val + to_mont(cj) * v[j];
-            }
-            acc = acc + coefs[p] * val;
+// Unreduced sums of Montgomery products.  The last factor product of a slot
+// value is not reduced per pair: the 512-bit a*b goes into a 17-limb
+// accumulator (no overflow below 2^32 products of values < r), reduced once
+// per thread at the end, as REDC(sum a_i b_i) = sum REDC(a_i b_i) mod r.
+// This halves the multiply work of that product and replaces the per-pair
+// modular add by a carry chain.
+struct FrAcc {
+    uint32_t w[17];
+};
+
+__device__ __forceinline__ void acc_zero(FrAcc &X) {
+#pragma unroll
+    for (int i = 0; i < 17; i++) X.w[i] = 0;
+}
+
+__device__ __forceinline__ void acc_mul_add(FrAcc &X, const Fr &a, const Fr &b) {
+    uint32_t z[16];
+    school_wide<8>(a.v, b.v, z);
+    X.w[0] = add_cc(X.w[0], z[0]);
+#pragma unroll
+    for (int i = 1; i < 16; i++) X.w[i] = addc_cc(X.w[i], z[i]);
+    X.w[16] = addc(X.w[16], 0);
+}
+
+// X += a * 2^256, whose REDC is a (products of arity 1)
+__device__ __forceinline__ void acc_add_shifted(FrAcc &X, const Fr &a) {
+    X.w[8] = add_cc(X.w[8], a.v[0]);
+#pragma unroll
+    for (int i = 1; i < 8; i++) X.w[8 + i] = addc_cc(X.w[8 + i], a.v[i]);
+    X.w[16] = addc(X.w[16], 0);
+}
+
+// REDC(X) = X 2^-256 mod r, in [0, r): 8 Montgomery rows over the low 16
+// limbs (result < 2^256 + r < 4r, so at most 3 subtractions of r), plus the
+// share of limb 16, w 2^512 2^-256 = w 2^256 = to_mont(w).
+__device__ Fr acc_reduce(const FrAcc &X) {
+    uint32_t t[17];
+#pragma unroll
+    for (int i = 0; i < 16; i++) t[i] = X.w[i];
+    t[16] = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const uint32_t m = t[i] * FrParams::INV;
+        uint32_t carry = 0;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const uint64_t d = uint64_t(m) * FrParams::p(j) + (uint64_t(t[i + j]) + carry);
+            t[i + j] = uint32_t(d);
+            carry = uint32_t(d >> 32);
         }
-        out[x] = from_mont(acc);
+#pragma unroll
+        for (int j = i + 8; j < 17; j++) {
+            const uint64_t d = uint64_t(t[j]) + carry;
+            t[j] = uint32_t(d);
+            carry = uint32_t(d >> 32);
+        }
+    }
+    Fr r;
+#pragma unroll
+    for (int i = 0; i < 8; i++) r.v[i] = t[8 + i];
+    uint32_t hi = t[16];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        uint32_t u[8];
+        u[0] = sub_cc(r.v[0], FrParams::p(0));
+#pragma unroll
+        for (int i = 1; i < 8; i++) u[i] = subc_cc(r.v[i], FrParams::p(i));
+        const uint32_t h2 = subc(hi, 0);
+        const bool keep = h2 == 0xffffffffu;  // (hi, r) < p
+#pragma unroll
+        for (int i = 0; i < 8; i++) r.v[i] = keep ? r.v[i] : u[i];
+        hi = keep ? hi : h2;
+    }
+    Fr w = Fr::zero();
+    w.v[0] = X.w[16];
+    return r + to_mont(w);
+}
+
+// dst_f[i] = src_f[2i] + r (src_f[2i+1] - src_f[2i]) for the `count` factor
+// tables, i < 2^log_half: the fold of a large round, ahead of the (slot, pair)
+// kernel below (elementwise, so every pass is coalesced and HBM-bound).
+__global__ void __launch_bounds__(256) k_sumcheck_fold(FrPtrList src, FrMutPtrList dst, int count, int log_half,
+                                                       Fr r) {
+    const size_t half = size_t(1) << log_half, total = size_t(count) << log_half;
+    for (size_t idx = size_t(blockIdx.x) * blockDim.x + threadIdx.x; idx < total;
+         idx += size_t(gridDim.x) * blockDim.x) {
+        const int f = int(idx >> log_half);
+        const size_t i = idx & (half - 1);
+        const Fr *q = src.p[f] + 2 * i;
+        const Fr a0 = load_fr(q), a1 = load_fr(q + 1);
+        store_fr(dst.p[f] + i, a0 + r * (a1 - a0));
     }
 }
 
-__global__ void k_sumcheck_finalize(SumcheckDesc desc, const Fr *partials, int blocks,
-                                    const Fr *coefs, int degree, Fr *slot_sums, Fr *out) {
+// One thread per (slot, pair) item, slot = (product p, node t): the thread
+// steps the m factors of p to t at its pair and multiplies them, a chain of
+// m - 1 products with the last one accumulated unreduced -- no per-thread
+// slot table, so occupancy is set by registers alone.  Block = kWideThreads
+// pairs of one slot; blocks interleave slots (block b: slot b % S) so that
+// resident blocks share their pairs' factor rows in L2.  Each block covers
+// pairs blk*T + t + i*bps*T (bps = blocks per slot); one partial per block,
+// slot-major; the last block finishes the round.
+//   fold = true (rounds of up to a few thousand pairs): the thread folds its
+// factors from `src` with r itself (a factor is re-folded once per slot
+// that reads it: cheap at these sizes, and it saves a launch); the item at a
+// factor's first occurrence (desc.writer) and t = 0 stores the folded pair,
+// so every folded table is written exactly once.
+//   fold = false: `src` holds this round's tables (the inputs in round 1,
+// else the k_sumcheck_fold output).
+constexpr int kWideThreads = 128;
+static_assert(kMaxFactors == kMaxList, "one writer entry per factor pointer");
+
+// (HP_WIDE_MINBLOCKS: a minimum-blocks-per-SM bound, a tuning hook; none by
+// default, ~80 registers, 6 blocks per SM)
+#ifdef HP_WIDE_MINBLOCKS
+#define HP_WIDE_BOUNDS __launch_bounds__(kWideThreads, HP_WIDE_MINBLOCKS)
+#else
+#define HP_WIDE_BOUNDS __launch_bounds__(kWideThreads)
+#endif
+
+// e = lo + k (hi - lo) = hi + (k - 1)(hi - lo), then the slot value's
+// running product v (factor j of m), the last factor into the accumulator
+__device__ __forceinline__ void slot_step(FrAcc &X, Fr &v, const Fr &lo, const Fr &hi, int j, int m, int k) {
+    Fr e = k == 0 ? lo : hi;
+    if (k >= 2) {
+        const Fr step = hi - lo;
+        for (int i = 1; i < k; i++) e = e + step;
+    }
+    if (j == m - 1) {
+        if (m == 1) acc_add_shifted(X, e);
+        else acc_mul_add(X, v, e);
+    } else {
+        v = j == 0 ? e : v * e;
+    }
+}
+
+template <int MAXM>
+__global__ void HP_WIDE_BOUNDS k_sumcheck_round_wide(SumcheckDesc desc, FrPtrList src, FrMutPtrList dst, bool fold,
+                                                     Fr r, size_t pairs, int blocks_per_slot, Fr *partials,
+                                                     unsigned *counter, const Fr *weights, int degree, Fr *out) {
+    extern __shared__ Fr sums[];  // S slot sums, used by the last block
+    __shared__ Fr wsum[kWideThreads / 32];
+    const int S = desc.slot_count;
+    const int s = int(blockIdx.x % unsigned(S)), blk = int(blockIdx.x / unsigned(S));
+    int p = 0;
+    while (p + 1 < desc.product_count && desc.slot_base[p + 1] <= s) p++;
+    const int begin = desc.offsets[p], m = desc.offsets[p + 1] - begin, k = s - desc.slot_base[p];
+    FrAcc X;
+    acc_zero(X);
+    const size_t stride = size_t(blocks_per_slot) * kWideThreads;
+    for (size_t b = size_t(blk) * kWideThreads + threadIdx.x; b < pairs; b += stride) {
+        Fr v;
+#pragma unroll
+        for (int j = 0; j < MAXM; j++) {
+            if (j < m) {
+                const int f = desc.indices[begin + j];
+                Fr lo, hi;
+                if (fold) {
+                    const Fr *q = src.p[f] + 4 * b;
+                    const Fr a0 = load_fr(q), a1 = load_fr(q + 1), a2 = load_fr(q + 2), a3 = load_fr(q + 3);
+                    lo = a0 + r * (a1 - a0);
+                    hi = a2 + r * (a3 - a2);
+                    if (k == 0 && desc.writer[f] == begin + j) {
+                        Fr *d = dst.p[f] + 2 * b;
+                        store_fr(d, lo);
+                        store_fr(d + 1, hi);
+                    }
+                } else {
+                    const Fr *q = src.p[f] + 2 * b;
+                    lo = load_fr(q);
+                    hi = load_fr(q + 1);
+                }
+                slot_step(X, v, lo, hi, j, m, k);
+            }
+        }
+    }
+    Fr a = acc_reduce(X);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    a = warp_sum(a);
+    if (lane == 0) wsum[warp] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        Fr t = wsum[0];
+#pragma unroll
+        for (int w = 1; w < kWideThreads / 32; w++) t = t + wsum[w];
+        partials[size_t(s) * blocks_per_slot + blk] = t;
+    }
+    finish_round_in_last_block(desc, partials, blocks_per_slot, counter, weights, degree, out, sums);
+}
+
+// Given the slot sums (Montgomery, shared memory) of a round, writes the d+1
+// canonical round evaluations out[x] = sum_s W[x][s] * sums[s], one warp per
+// x.  W (per prover state, built on the host) holds for slot
+// s = slot_base[p] + i the product coefficient times the Lagrange basis
+// polynomial l_i of the nodes 0..m (m = arity of p) at x: the slot sums are
+// the product's values at t = 0..m, so the row is the unique polynomial of
+// degree <= m through them -- equal to the slot sum for x <= m and to the
+// reference's barycentric extrapolation (backend/src/cpu/sum_check.rs:183-217)
+// beyond -- scaled and summed over products.
+__device__ void finalize_from_sums(const SumcheckDesc &desc, const Fr *sums, const Fr *weights, int degree,
+                                   Fr *out) {
+    const int S = desc.slot_count;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+    for (int x = warp; x <= degree; x += warps) {
+        Fr a = Fr::zero();
+        for (int s = lane; s < S; s += 32) a = a + weights[size_t(x) * S + s] * sums[s];
+        a = warp_sum(a);
+        if (lane == 0) out[x] = from_mont(a);
+    }
+}
+
+__global__ void k_sumcheck_finalize(SumcheckDesc desc, const Fr *partials, int blocks, const Fr *weights,
+                                    int degree, Fr *out) {
     extern __shared__ Fr sums[];
     const int S = desc.slot_count;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
@@ -283,13 +458,10 @@ __global__ void k_sumcheck_finalize(SumcheckDesc desc, const Fr *partials, int b
         Fr a = Fr::zero();
         for (int b = lane; b < blocks; b += 32) a = a + partials[size_t(s) * blocks + b];
         a = warp_sum(a);
-        if (lane == 0) {
-            sums[s] = a;
-            slot_sums[s] = a;
-        }
+        if (lane == 0) sums[s] = a;
     }
     __syncthreads();
-    finalize_from_sums(desc, sums, coefs, degree, out);
+    finalize_from_sums(desc, sums, weights, degree, out);
 }
 
 // A round of at most kSmallPairs pairs in one block, finalize included (the
@@ -301,8 +473,8 @@ constexpr int kSmallThreads = 256;
 template <int MAXM>
 __global__ void __launch_bounds__(kSmallThreads) k_sumcheck_round_small(SumcheckDesc desc, FrPtrList src,
                                                                         FrMutPtrList dst, FrPtrList rd, bool fold,
-                                                                        Fr r, int pairs, const Fr *coefs, int degree,
-                                                                        Fr *out) {
+                                                                        Fr r, int pairs, const Fr *weights,
+                                                                        int degree, Fr *out) {
     extern __shared__ Fr sm[];  // vals[S][kSmallPairs], then sums[S]
     const int S = desc.slot_count, F = desc.factor_count;
     Fr *vals = sm, *sums = sm + size_t(S) * kSmallPairs;
@@ -351,7 +523,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_sumcheck_round_small(Sumcheck
         if (lane == 0) sums[s] = v;
     }
     __syncthreads();
-    finalize_from_sums(desc, sums, coefs, degree, out);
+    finalize_from_sums(desc, sums, weights, degree, out);
 }
 
 __global__ void k_sumcheck_final_fold(FrPtrList tables, int count, Fr r, Fr *out) {
@@ -374,7 +546,12 @@ struct HpCudaSumCheckProverState {
     std::vector<void *> inputs;  // referenced input factor buffers
     void *fold_a = nullptr;      // F x 2^(nv-1) Fr
     void *fold_b = nullptr;      // F x 2^(nv-2) Fr
-    void *coefs = nullptr;       // P Montgomery coefficients (device)
+    // device: one zeroed Fr slot whose first word is the round kernels'
+    // last-block counter, then the (max_degree + 1) x slot_count extrapolation
+    // weights (Montgomery) of finalize_from_sums
+    void *weights = nullptr;
+    void *partials = nullptr;  // block partials of a round, reused every round
+    size_t partials_bytes = 0;
     int current = 0;             // 0: inputs, 1: fold_a, 2: fold_b
 };
 
@@ -390,7 +567,71 @@ static const Fr *state_table(HpCudaSumCheckProverState *s, int which, int f) {
 
 static unsigned *round_counter(HpCudaSumCheckProverState *s) {
     const size_t p = std::max(size_t(s->desc.product_count), size_t(1));
-    return reinterpret_cast<unsigned *>(static_cast<Fr *>(s->coefs) + p);
+    return reinterpret_cast<unsigned *>(s->weights);
+}
+
+static const Fr *state_weights(HpCudaSumCheckProverState *s) { return static_cast<const Fr *>(s->weights) + 1; }
+
+static size_t big_blocks_per_sm();
+
+// Block partials of any round of the state: the largest grid x slots of the
+// round kernels (per-pair grid kernel, (slot, pair) kernel, shared-memory
+// kernel).
+static size_t partials_capacity(const SumcheckDesc &d, int sm_count) {
+    const size_t sms = size_t(sm_count > 0 ? sm_count : 152), S = size_t(d.slot_count);
+    size_t n = sms * HP_ROUND_BLOCKS_PER_SM * S;
+    n = std::max(n, sms * 2 * S);
+    n = std::max(n, size_t(64) * S);
+    n = std::max(n, sms * big_blocks_per_sm() + S);
+    return n * sizeof(Fr);
+}
+
+// The state's partials buffer when it holds `bytes`, else `fallback`.
+static Fr *round_partials(HpCudaContext *ctx, HpCudaSumCheckProverState *s, size_t bytes, Scratch &fallback,
+                          cudaStream_t st) {
+    if (bytes <= s->partials_bytes) return static_cast<Fr *>(s->partials);
+    fallback = Scratch(ctx, bytes, st);
+    return fallback.as<Fr>();
+}
+
+// The (degree + 1) x slot_count matrix W of finalize_from_sums, Montgomery
+// form: W[x][slot_base[p] + i] = c_p * l_{m,i}(x), where l_{m,i} is the
+// Lagrange basis polynomial of the nodes 0..m (m = arity of product p):
+// l_{m,i}(x) = [x == i] for x <= m, else
+// prod_{k != i} (x - k) / ((-1)^(m-i) i! (m-i)!).
+static std::vector<host::Fr64> extrapolation_weights(const SumcheckDesc &d, const uint8_t *coefficients,
+                                                     size_t degree) {
+    using host::Fr64;
+    const int S = d.slot_count, D = int(degree);
+    std::vector<Fr64> w(size_t(D + 1) * S, Fr64{{0, 0, 0, 0}});
+    // inverse factorials 0..kMaxDegree
+    std::vector<Fr64> fact(kMaxDegree + 1), inv_fact(kMaxDegree + 1);
+    fact[0] = host::one();
+    for (int k = 1; k <= kMaxDegree; k++) fact[k] = host::mont_mul(fact[k - 1], host::from_u64(uint64_t(k)));
+    inv_fact[kMaxDegree] = host::inverse(fact[kMaxDegree]);
+    for (int k = kMaxDegree; k >= 1; k--) inv_fact[k - 1] = host::mont_mul(inv_fact[k], host::from_u64(uint64_t(k)));
+    for (int p = 0; p < d.product_count; p++) {
+        const int m = d.offsets[p + 1] - d.offsets[p], base = d.slot_base[p];
+        Fr64 c;
+        if (!host::from_canonical(coefficients + 32 * size_t(p), c)) fail(HP_CUDA_STATUS_INVALID_PARAMETERS);
+        for (int i = 0; i <= m; i++) {
+            Fr64 den = host::mont_mul(inv_fact[i], inv_fact[m - i]);
+            if ((m - i) & 1) den = host::neg(den);
+            const Fr64 ci = host::mont_mul(c, den);
+            for (int x = 0; x <= D; x++) {
+                Fr64 v;
+                if (x <= m) {
+                    v = x == i ? c : Fr64{{0, 0, 0, 0}};
+                } else {
+                    v = ci;
+                    for (int k = 0; k <= m; k++)
+                        if (k != i) v = host::mont_mul(v, host::from_u64(uint64_t(x - k)));
+                }
+                w[size_t(x) * S + base + i] = v;
+            }
+        }
+    }
+    return w;
 }
 
 static void release_state(HpCudaContext *ctx, HpCudaSumCheckProverState *s) {
@@ -400,8 +641,9 @@ static void release_state(HpCudaContext *ctx, HpCudaSumCheckProverState *s) {
     s->inputs.clear();
     if (s->fold_a) ctx->scratch_free(s->fold_a);
     if (s->fold_b) ctx->scratch_free(s->fold_b);
-    if (s->coefs) ctx->scratch_free(s->coefs);
-    s->fold_a = s->fold_b = s->coefs = nullptr;
+    if (s->weights) ctx->scratch_free(s->weights);
+    if (s->partials) ctx->scratch_free(s->partials);
+    s->fold_a = s->fold_b = s->weights = s->partials = nullptr;
 }
 
 static int round_block_size(const SumcheckDesc &d, size_t *smem_out) {
@@ -454,7 +696,11 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_create(
                 max_arity = std::max(max_arity, m);
             }
             d.offsets[product_count] = uint16_t(index_count);
-            for (size_t i = 0; i < index_count; i++) d.indices[i] = uint8_t(factor_indices[i]);
+            for (int f = 0; f < hp::kMaxFactors; f++) d.writer[f] = hp::kNoWriter;
+            for (size_t i = 0; i < index_count; i++) {
+                d.indices[i] = uint8_t(factor_indices[i]);
+                if (d.writer[factor_indices[i]] == hp::kNoWriter) d.writer[factor_indices[i]] = uint16_t(i);
+            }
             d.slot_count = std::max(slots, 1);
             d.max_arity = max_arity;
             for (size_t f = 0; f < factor_count; f++) {
@@ -462,12 +708,14 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_create(
                 ctx->ref(factors[f]);
                 s->inputs.push_back(factors[f]);
             }
-            // coefficients, then one zeroed Fr slot whose first word is the
-            // round kernels' last-block counter
-            s->coefs = ctx->scratch((std::max(product_count, size_t(1)) + 1) * sizeof(Fr));
-            hp::host_scalars_to_device(ctx, coefficients, product_count, static_cast<Fr *>(s->coefs));
-            check_cuda(cudaMemsetAsync(static_cast<Fr *>(s->coefs) + std::max(product_count, size_t(1)), 0,
-                                       sizeof(Fr), ctx->stream));
+            std::vector<hp::host::Fr64> w = hp::extrapolation_weights(d, coefficients, max_degree);
+            s->weights = ctx->scratch((w.size() + 1) * sizeof(Fr));
+            check_cuda(cudaMemsetAsync(s->weights, 0, sizeof(Fr), ctx->stream));
+            check_cuda(cudaMemcpyAsync(static_cast<Fr *>(s->weights) + 1, w.data(), w.size() * sizeof(Fr),
+                                       cudaMemcpyHostToDevice, ctx->stream));
+            s->partials_bytes = hp::partials_capacity(d, ctx->sm_count);
+            s->partials = ctx->scratch(s->partials_bytes);
+            ctx->sync();  // w is a pageable host vector
             size_t a_len = hp::table_len(num_vars - 1);
             size_t b_len = num_vars >= 2 ? hp::table_len(num_vars - 2) : 1;
             size_t fcount = std::max(factor_count, size_t(1));
@@ -498,6 +746,11 @@ static void check_round(HpCudaSumCheckProverState *s, const uint8_t *challenge_o
     if (s->round > 0 && challenge_or_null == nullptr) fail(HP_CUDA_STATUS_INVALID_STATE);
 }
 
+static size_t wide_max_pairs();
+static size_t wide_min_pairs();
+static bool big_slot_rounds();
+static size_t big_blocks_per_sm();
+
 // Enqueues one round of state s on stream st: fold with r (rounds > 1) and
 // message into out_dev (degree + 1 canonical Fr, device).  Scratch is ordered
 // on st.  Does not advance the state.
@@ -516,6 +769,53 @@ static void enqueue_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, cons
         rd.p[f] = fold ? dst.p[f] : src.p[f];
     }
     const bool regs = d.max_arity <= 8 && d.slot_count <= kMaxSlotsV2;
+    bool all_written = true;
+    for (int f = 0; f < d.factor_count; f++) all_written = all_written && d.writer[f] != kNoWriter;
+    const bool slots_ok = d.max_arity <= 8 && d.product_count > 0;
+    const bool wide = slots_ok && (all_written || !fold) && pairs >= wide_min_pairs() && pairs <= wide_max_pairs();
+    const bool big = slots_ok && pairs > wide_max_pairs() && big_slot_rounds();
+    if (wide || big) {
+        int tok = ctx->prof_begin("sumcheck_round", st);
+        const size_t tiles = (pairs + kWideThreads - 1) / kWideThreads;
+        int bps = int(std::min(tiles, size_t(1) << 20));
+        FrPtrList tables = src;
+        bool fused_fold = fold;
+        if (big) {
+            // fold every table first, then one pass over the folded tables;
+            // about two waves of blocks over the GPU in all
+            if (fold) {
+                int log_half = 0;
+                while ((size_t(1) << log_half) < 2 * pairs) log_half++;
+                const size_t total = size_t(d.factor_count) << log_half;
+                const size_t sms = size_t(ctx->sm_count > 0 ? ctx->sm_count : 152);
+                const unsigned fgrid = unsigned(std::min<size_t>((total + 255) / 256, sms * 8));
+                k_sumcheck_fold<<<fgrid, 256, 0, st>>>(src, dst, d.factor_count, log_half, r);
+                check_launch();
+                tables = rd;
+                fused_fold = false;
+            }
+            const size_t target = size_t(ctx->sm_count > 0 ? ctx->sm_count : 152) * big_blocks_per_sm();
+            bps = int(std::max<size_t>(1, std::min(tiles, (target + d.slot_count - 1) / d.slot_count)));
+        }
+        const unsigned grid = unsigned(d.slot_count) * unsigned(bps);
+        Scratch spill;
+        Fr *partials = round_partials(ctx, s, size_t(grid) * sizeof(Fr), spill, st);
+        const size_t smem = size_t(d.slot_count) * sizeof(Fr);
+        auto launch = [&](auto kernel) {
+            if (smem > 32 * 1024)
+                check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+            kernel<<<grid, kWideThreads, smem, st>>>(d, tables, dst, fused_fold, r, pairs, bps, partials,
+                                                     round_counter(s), state_weights(s), int(s->max_degree),
+                                                     out_dev);
+        };
+        if (d.max_arity <= 2) launch(k_sumcheck_round_wide<2>);
+        else if (d.max_arity <= 4) launch(k_sumcheck_round_wide<4>);
+        else if (d.max_arity <= 6) launch(k_sumcheck_round_wide<6>);
+        else launch(k_sumcheck_round_wide<8>);
+        check_launch();
+        ctx->prof_end(tok, st);
+        return;
+    }
     if (regs && pairs <= size_t(kSmallPairs)) {
         int tok = ctx->prof_begin("sumcheck_round", st);
         const size_t smem = size_t(d.slot_count) * (kSmallPairs + 1) * sizeof(Fr);
@@ -523,7 +823,7 @@ static void enqueue_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, cons
             if (smem > 32 * 1024)
                 check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
             kernel<<<1, kSmallThreads, smem, st>>>(d, src, dst, rd, fold, r, int(pairs),
-                                                   static_cast<const Fr *>(s->coefs), int(s->max_degree), out_dev);
+                                                   state_weights(s), int(s->max_degree), out_dev);
         };
         if (d.max_arity <= 2) launch(k_sumcheck_round_small<2>);
         else if (d.max_arity <= 4) launch(k_sumcheck_round_small<4>);
@@ -534,19 +834,20 @@ static void enqueue_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, cons
         return;
     }
     unsigned grid;
-    Scratch partials, sums(ctx, d.slot_count * sizeof(Fr), st);
+    Scratch spill;
+    Fr *partials = nullptr;
     int tok = ctx->prof_begin("sumcheck_round", st);
     if (regs) {
         grid = grid_for(ctx, pairs, kRoundThreads, HP_ROUND_BLOCKS_PER_SM);
-        partials = Scratch(ctx, size_t(grid) * d.slot_count * sizeof(Fr), st);
+        partials = round_partials(ctx, s, size_t(grid) * d.slot_count * sizeof(Fr), spill, st);
         const size_t smem = size_t(d.slot_count) * kRoundThreads * sizeof(Fr);
         auto launch = [&](auto kernel) {
             // the kernel's own static shared memory counts against the same
             // 48 KiB default, so opt in well before the dynamic size reaches it
             if (smem > 32 * 1024)
                 check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-            kernel<<<grid, kRoundThreads, smem, st>>>(d, src, dst, rd, fold, r, pairs, partials.as<Fr>(),
-                                                      round_counter(s), static_cast<const Fr *>(s->coefs),
+            kernel<<<grid, kRoundThreads, smem, st>>>(d, src, dst, rd, fold, r, pairs, partials,
+                                                      round_counter(s), state_weights(s),
                                                       int(s->max_degree), out_dev);
         };
         if (d.max_arity <= 2) launch(k_sumcheck_round_regs<2>);
@@ -563,15 +864,42 @@ static void enqueue_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, cons
             check_cuda(cudaFuncSetAttribute(k_sumcheck_round, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             int(smem)));
         grid = grid_for(ctx, pairs, unsigned(T), 2);
-        partials = Scratch(ctx, size_t(grid) * d.slot_count * sizeof(Fr), st);
-        k_sumcheck_round<<<grid, T, smem, st>>>(d, src, dst, fold, r, pairs, partials.as<Fr>());
+        partials = round_partials(ctx, s, size_t(grid) * d.slot_count * sizeof(Fr), spill, st);
+        k_sumcheck_round<<<grid, T, smem, st>>>(d, src, dst, fold, r, pairs, partials);
         check_launch();
     }
     ctx->prof_end(tok, st);
-    k_sumcheck_finalize<<<1, 256, size_t(d.slot_count) * sizeof(Fr), st>>>(d, partials.as<Fr>(), int(grid),
-                                                           static_cast<const Fr *>(s->coefs), int(s->max_degree),
-                                                           sums.as<Fr>(), out_dev);
+    k_sumcheck_finalize<<<1, 256, size_t(d.slot_count) * sizeof(Fr), st>>>(d, partials, int(grid),
+                                                           state_weights(s), int(s->max_degree), out_dev);
     check_launch();
+}
+
+// Rounds of wide_min_pairs() .. wide_max_pairs() pairs use the (slot, pair)
+// kernel with the fold fused; HP_WIDE_MAX_PAIRS / HP_WIDE_MIN_PAIRS override
+// the range (a maximum of 0 turns it off).
+static size_t env_size(const char *name, size_t dflt) {
+    const char *env = std::getenv(name);
+    if (env == nullptr || *env == '\0') return dflt;
+    return size_t(std::strtoull(env, nullptr, 10));
+}
+static size_t wide_max_pairs() {
+    static const size_t v = env_size("HP_WIDE_MAX_PAIRS", size_t(1) << 13);
+    return v;
+}
+static size_t wide_min_pairs() {
+    static const size_t v = env_size("HP_WIDE_MIN_PAIRS", size_t(kSmallPairs) + 1);
+    return v;
+}
+// Rounds above wide_max_pairs(): k_sumcheck_fold + the (slot, pair) kernel
+// (HP_BIG_SLOTS=0: the per-pair shared-memory kernel instead), with about
+// big_blocks_per_sm() blocks per SM in all (HP_BIG_BLOCKS_PER_SM).
+static bool big_slot_rounds() {
+    static const bool v = env_size("HP_BIG_SLOTS", 1) != 0;
+    return v;
+}
+static size_t big_blocks_per_sm() {
+    static const size_t v = std::max<size_t>(1, env_size("HP_BIG_BLOCKS_PER_SM", 16));
+    return v;
 }
 
 static void advance(HpCudaSumCheckProverState *s) {
@@ -592,11 +920,11 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_round(HpCudaContext *ct
         Fr r = Fr::zero();
         if (challenge_or_null) r = hp::host_scalar(challenge_or_null);
         try {
-            hp::Scratch outd(ctx, evaluation_count * sizeof(Fr));
-            hp::enqueue_round(ctx, s, r, ctx->stream, outd.as<Fr>());
-            check_cuda(cudaMemcpyAsync(out_evaluations, outd.ptr, evaluation_count * sizeof(Fr),
-                                       cudaMemcpyDeviceToHost, ctx->stream));
+            void *box_dev = nullptr;
+            const uint8_t *box = ctx->mailbox(evaluation_count * sizeof(Fr), &box_dev);
+            hp::enqueue_round(ctx, s, r, ctx->stream, static_cast<Fr *>(box_dev));
             ctx->sync();
+            std::memcpy(out_evaluations, box, evaluation_count * sizeof(Fr));
             hp::advance(s);
         } catch (const hp::Failure &f) {
             if (f.kind == HP_CUDA_STATUS_INVALID_STATE) s->poisoned = true;
@@ -623,22 +951,22 @@ extern "C" HpCudaStatus hp_cuda_v1_batch_sumcheck_round(HpCudaContext *ctx, HpCu
             total += evaluation_counts[i];
         }
         try {
-            hp::Scratch outd(ctx, total * sizeof(Fr));
-            std::vector<Fr> host_out(total);
+            // the round kernels write their messages into the mapped mailbox
+            void *box_dev = nullptr;
+            const uint8_t *box = ctx->mailbox(total * sizeof(Fr), &box_dev);
             const int k = int(std::min<size_t>(count, HpCudaContext::kWorkers));
             ctx->fork(k);
             size_t off = 0;
             for (size_t i = 0; i < count; i++) {
-                hp::enqueue_round(ctx, states[i], rs[i], ctx->workers[i % size_t(k)], outd.as<Fr>() + off);
+                hp::enqueue_round(ctx, states[i], rs[i], ctx->workers[i % size_t(k)],
+                                  static_cast<Fr *>(box_dev) + off);
                 off += evaluation_counts[i];
             }
             ctx->join(k);
-            check_cuda(cudaMemcpyAsync(host_out.data(), outd.ptr, total * sizeof(Fr), cudaMemcpyDeviceToHost,
-                                       ctx->stream));
             ctx->sync();
             off = 0;
             for (size_t i = 0; i < count; i++) {
-                std::memcpy(out_evaluations[i], host_out.data() + off, evaluation_counts[i] * sizeof(Fr));
+                std::memcpy(out_evaluations[i], box + off * sizeof(Fr), evaluation_counts[i] * sizeof(Fr));
                 off += evaluation_counts[i];
                 hp::advance(states[i]);
             }
@@ -681,21 +1009,23 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prove_rounds(HpCudaContext *ctx, HpC
         if (s->poisoned || s->round != 0) fail(HP_CUDA_STATUS_INVALID_STATE);
         require(rounds == s->num_vars);
         const size_t d1 = s->max_degree + 1;
-        hp::Scratch outd(ctx, d1 * sizeof(Fr));
+        // each round's kernel writes its message into the mapped mailbox
+        void *box_dev = nullptr;
+        const uint8_t *box = ctx->mailbox(32 * d1, &box_dev);
         // "prover msg" payload: u64 LE element count, then the canonical elements
         std::vector<uint8_t> msg(8 + 32 * d1, 0);
         for (int b = 0; b < 8; b++) msg[b] = uint8_t(uint64_t(d1) >> (8 * b));
         Fr r = Fr::zero();
         for (size_t k = 0; k < rounds; k++) {
             try {
-                hp::enqueue_round(ctx, s, r, ctx->stream, outd.as<Fr>());
-                check_cuda(cudaMemcpyAsync(msg.data() + 8, outd.ptr, 32 * d1, cudaMemcpyDeviceToHost, ctx->stream));
+                hp::enqueue_round(ctx, s, r, ctx->stream, static_cast<Fr *>(box_dev));
                 ctx->sync();
                 hp::advance(s);
             } catch (const hp::Failure &f) {
                 if (f.kind == HP_CUDA_STATUS_INVALID_STATE) s->poisoned = true;
                 throw;
             }
+            std::memcpy(msg.data() + 8, box, 32 * d1);
             std::memcpy(out_messages + 32 * d1 * k, msg.data() + 8, 32 * d1);
             hp::merlin_append(transcript, "prover msg", msg.data(), msg.size());
             // challenge: 64 transcript bytes reduced mod r, re-appended canonically

@@ -12,6 +12,7 @@ namespace hp {
 constexpr int kMaxProducts = 64;
 constexpr int kMaxIndices = 256;
 constexpr int kMaxDegree = 64;
+constexpr int kMaxFactors = 32;  // distinct factor tables of one state
 
 struct SumcheckDesc {
     int factor_count;
@@ -21,6 +22,12 @@ struct SumcheckDesc {
     uint16_t offsets[kMaxProducts + 1];
     uint16_t slot_base[kMaxProducts];
     uint8_t indices[kMaxIndices];
+    // writer[f]: the position in `indices` of factor f's first occurrence
+    // (kNoWriter if f is in no product); the wide round kernel's item at that
+    // position and t = 0 stores f's folded pair
+    uint16_t writer[kMaxFactors];
 };
+
+constexpr uint16_t kNoWriter = 0xffff;
 
 }  // namespace hp

@@ -57,7 +57,10 @@ def test_round_kat_and_ordering(gpu):
     assert gpu.download(mle) == b"".join(v.to_bytes(32, "little") for v in (2, 3, 5, 7))
 
 
-@pytest.mark.parametrize("nv", [1, 2, 3, 10, 14])
+# nv <= 14: every round in the wide (slot, pair) kernel, from unfolded inputs
+# on; nv = 16: the first two rounds in the grid kernel, whose folded tables
+# the wide kernel then reads
+@pytest.mark.parametrize("nv", [1, 2, 3, 10, 14, 16])
 def test_degree2_four_products_over_six_mles(gpu, cpu, oracle, nv):
     rng = random.Random(nv)
     prods = [(rng.randrange(R), [0, 1]), (rng.randrange(R), [2, 3]), (rng.randrange(R), [4, 5]),
@@ -81,9 +84,9 @@ def test_repeated_factors_max_degree_34(gpu, cpu, oracle):
     run_both(gpu, cpu, vg, vc, 34)
 
 
-def test_zerocheck_shape_degree4(gpu, cpu, oracle):
+@pytest.mark.parametrize("nv", [11, 15])
+def test_zerocheck_shape_degree4(gpu, cpu, oracle, nv):
     """Gate polynomial times eq: q_L w1 + q_R w2 + q_O w3 + q_M w1 w2 + q_C, x eq."""
-    nv = 11
     # 0..4 selectors, 5..7 witnesses, 8 eq
     prods = [(1, [0, 5, 8]), (1, [1, 6, 8]), (1, [2, 7, 8]), (1, [3, 5, 6, 8]), (1, [4, 8])]
     vg, vc, _, _ = build_pair(gpu, cpu, oracle, nv, 9, prods, 4)
