@@ -433,7 +433,9 @@ def run_sumcheck(args, world, rank, local, pg):
         {"value": world / e2e_s, "unit": "proofs/s", "h2d_bytes_per_step": 6 * 32 * (1 << nv),
          "d2h_bytes_per_step": 32 * (3 * nv + 6)}, nl, clk)
     result["roofline"] = {
-        "bound": "imad", "kernel": "k_sumcheck_round_regs (fold + round message)",
+        "bound": "imad",
+        "kernel": "sumcheck rounds: k_sumcheck_fold + k_sumcheck_round_wide (large and middle rounds), "
+                  "k_sumcheck_round_small (<= 64 pairs)",
         "achieved": imad_work / kernel_s / 1e12, "peak": imad / 1e12, "unit": "TIMAD/s",
         "frac": imad_work / kernel_s / imad, "traffic": None,
         "peak_source": "measured live: mad.lo.u32 issue rate on this GPU (libhp_probe)",
