@@ -241,7 +241,7 @@ class CpuProveSample:
         self.cpu = orc.CpuBackend()
         self.nv = nv
         sel, self.wit, perm, self.pub = snark.vanilla_fixture(nv, PROVE_SEED)
-        self.pk = snark.preprocess(self.cpu, nv, min(16, 1 << nv), sel, perm, orc.srs_layers(nv, 0))
+        self.pk = snark.preprocess(self.cpu, nv, min(16, 1 << nv), sel, perm, orc.srs_layers(nv, 0), commit=False)
 
     def step(self) -> float:
         t0 = time.perf_counter()
@@ -645,7 +645,7 @@ def run_gb300(args, world, rank, local, pg):
     else:
         from hyperplonk_gb300 import snark
         sel, wit, perm, pub = snark.vanilla_fixture(nv, PROVE_SEED)
-        pk = snark.preprocess(be, nv, min(16, n), sel, perm, layers)
+        pk = snark.preprocess(be, nv, min(16, n), sel, perm, layers, commit=False)
         del layers, sel, perm
         pinned = [s.pinned(w) for w in wit]
         wit_host = [p.numpy() for p in pinned]

@@ -9,7 +9,7 @@ with selectors ordered [q_L, q_R, q_O, q_M, q_C] and witnesses [w1, w2, w3].
 from __future__ import annotations
 
 import ctypes
-from dataclasses import dataclass
+from dataclasses import dataclass, field
 
 import numpy as np
 
@@ -28,12 +28,33 @@ VANILLA_GATE = [(1, 0, [0]), (1, 1, [1]), (1, 2, [2]), (1, 3, [0, 1]), (1, 4, []
 
 @dataclass
 class ProvingKey:
+    """structs.rs:126-146."""
     num_vars: int
     num_pub_input: int
     gate: list
     pcs_param: object
     selector_oracles: list
     permutation_oracles: list
+    selector_commitments: list = field(default_factory=list)
+    permutation_commitments: list = field(default_factory=list)
+
+    def verifying_key(self, pcs_verifier_param) -> "VerifyingKey":
+        """The matching verifying key; `pcs_verifier_param` is the SRS's
+        verifier half (g, h, h_mask), which the prover never needs."""
+        return VerifyingKey(self.num_vars, self.num_pub_input, self.gate, pcs_verifier_param,
+                            list(self.selector_commitments), list(self.permutation_commitments))
+
+
+@dataclass
+class VerifyingKey:
+    """structs.rs:150-159: instance parameters, the PCS verifier parameter and
+    the preprocessed commitments."""
+    num_vars: int
+    num_pub_input: int
+    gate: list
+    pcs_param: object
+    selector_commitments: list
+    perm_commitments: list
 
 
 @dataclass
@@ -50,14 +71,21 @@ class HyperPlonkProof:
 
 
 def preprocess(backend, num_vars: int, num_pub_input: int, selectors: list, permutation: list,
-               srs_layers: list, gate=VANILLA_GATE) -> ProvingKey:
-    """snark.rs:56-105 (prover half): prepare the trimmed SRS, upload selector
-    and permutation oracles.  `srs_layers` are the num_vars + 1 layers of the
-    trimmed prover parameters; selectors / permutation are table packets."""
+               srs_layers: list, gate=VANILLA_GATE, commit: bool = True) -> ProvingKey:
+    """snark.rs:56-105: prepare the trimmed SRS, upload the permutation and
+    selector oracles and commit to them (permutations first, then selectors,
+    one multi_commit each, as the reference does).  `srs_layers` are the
+    num_vars + 1 layers of the trimmed prover parameters; selectors /
+    permutation are table packets.  commit=False skips the commitments (a
+    prover that never hands out a verifying key)."""
     pcs = backend.prepare_prover_param(num_vars, srs_layers)
     perms = [backend.mle_from_evaluations(num_vars, p) for p in permutation]
     sels = [backend.mle_from_evaluations(num_vars, s) for s in selectors]
-    return ProvingKey(num_vars, num_pub_input, gate, pcs, sels, perms)
+    pk = ProvingKey(num_vars, num_pub_input, gate, pcs, sels, perms)
+    if commit:
+        pk.permutation_commitments = list(backend.multi_commit(pcs, perms))
+        pk.selector_commitments = list(backend.multi_commit(pcs, sels))
+    return pk
 
 
 def build_f(gate, num_vars: int, selector_mles, witness_mles) -> VirtualPolynomial:

@@ -1321,3 +1321,493 @@ int or_srs_gen(size_t nv, uint64_t seed, uint8_t *out) {
     free(t);
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* BLS12-381 pairing -- for the verifier only (multilinear_kzg/mod.rs:169-221,
+ * hyperplonk/src/snark.rs verify).  Textbook forms, written for clarity:
+ *   Fq2  = Fq[u]/(u^2 + 1)
+ *   Fq6  = Fq2[v]/(v^3 - xi), xi = 1 + u
+ *   Fq12 = Fq6[w]/(w^2 - v)
+ *   G2   = r-torsion of E': y^2 = x^3 + 4 xi over Fq2, mapped into E(Fq12)
+ *          by (x, y) -> (x w^-2, y w^-3) (w^6 = xi)
+ *   e(P, Q) = f_{|z|, Q}(P)^((p^12 - 1) / r), conjugated as z < 0, with the
+ *   optimal-ate loop parameter |z| = 0xd201000000010000 and affine line
+ *   functions in Fq12 (vertical lines dropped: they vanish under the final
+ *   exponentiation).
+ * The final exponent and the G2 cofactor are large integers computed by the
+ * caller from p, r and z and passed in as little-endian 64-bit limbs.       */
+/* ------------------------------------------------------------------------ */
+
+typedef struct { fq_t c0, c1; } fq2_t;
+typedef struct { fq2_t c0, c1, c2; } fq6_t;
+typedef struct { fq6_t c0, c1; } fq12_t;
+
+static void fq2_add(fq2_t *r, const fq2_t *a, const fq2_t *b) {
+    fq_add(&r->c0, &a->c0, &b->c0);
+    fq_add(&r->c1, &a->c1, &b->c1);
+}
+static void fq2_sub(fq2_t *r, const fq2_t *a, const fq2_t *b) {
+    fq_sub(&r->c0, &a->c0, &b->c0);
+    fq_sub(&r->c1, &a->c1, &b->c1);
+}
+static void fq2_neg(fq2_t *r, const fq2_t *a) {
+    fq_neg(&r->c0, &a->c0);
+    fq_neg(&r->c1, &a->c1);
+}
+static void fq2_mul(fq2_t *r, const fq2_t *a, const fq2_t *b) {
+    fq_t t0, t1, t2, t3;
+    fq_mul(&t0, &a->c0, &b->c0);
+    fq_mul(&t1, &a->c1, &b->c1);
+    fq_mul(&t2, &a->c0, &b->c1);
+    fq_mul(&t3, &a->c1, &b->c0);
+    fq_sub(&r->c0, &t0, &t1);
+    fq_add(&r->c1, &t2, &t3);
+}
+static void fq2_mul_xi(fq2_t *r, const fq2_t *a) { /* (c0 + c1 u)(1 + u) */
+    fq_t t0, t1;
+    fq_sub(&t0, &a->c0, &a->c1);
+    fq_add(&t1, &a->c0, &a->c1);
+    r->c0 = t0;
+    r->c1 = t1;
+}
+static void fq2_inv(fq2_t *r, const fq2_t *a) { /* (c0 - c1 u) / (c0^2 + c1^2) */
+    fq_t n, t, ninv;
+    fq_mul(&n, &a->c0, &a->c0);
+    fq_mul(&t, &a->c1, &a->c1);
+    fq_add(&n, &n, &t);
+    fq_inv(&ninv, &n);
+    fq_mul(&r->c0, &a->c0, &ninv);
+    fq_mul(&t, &a->c1, &ninv);
+    fq_neg(&r->c1, &t);
+}
+static int fq2_is_zero(const fq2_t *a) { return fq_is_zero(&a->c0) && fq_is_zero(&a->c1); }
+static int fq2_eq(const fq2_t *a, const fq2_t *b) { return fq_eq(&a->c0, &b->c0) && fq_eq(&a->c1, &b->c1); }
+static void fq2_zero(fq2_t *r) { fq_zero(&r->c0); fq_zero(&r->c1); }
+static void fq2_one(fq2_t *r) { fq_one(&r->c0); fq_zero(&r->c1); }
+
+static void fq6_add(fq6_t *r, const fq6_t *a, const fq6_t *b) {
+    fq2_add(&r->c0, &a->c0, &b->c0);
+    fq2_add(&r->c1, &a->c1, &b->c1);
+    fq2_add(&r->c2, &a->c2, &b->c2);
+}
+static void fq6_sub(fq6_t *r, const fq6_t *a, const fq6_t *b) {
+    fq2_sub(&r->c0, &a->c0, &b->c0);
+    fq2_sub(&r->c1, &a->c1, &b->c1);
+    fq2_sub(&r->c2, &a->c2, &b->c2);
+}
+static void fq6_neg(fq6_t *r, const fq6_t *a) {
+    fq2_neg(&r->c0, &a->c0);
+    fq2_neg(&r->c1, &a->c1);
+    fq2_neg(&r->c2, &a->c2);
+}
+static void fq6_mul(fq6_t *r, const fq6_t *a, const fq6_t *b) {
+    fq2_t a0b0, a1b1, a2b2, a0b1, a1b0, a0b2, a2b0, a1b2, a2b1, t;
+    fq2_mul(&a0b0, &a->c0, &b->c0);
+    fq2_mul(&a1b1, &a->c1, &b->c1);
+    fq2_mul(&a2b2, &a->c2, &b->c2);
+    fq2_mul(&a0b1, &a->c0, &b->c1);
+    fq2_mul(&a1b0, &a->c1, &b->c0);
+    fq2_mul(&a0b2, &a->c0, &b->c2);
+    fq2_mul(&a2b0, &a->c2, &b->c0);
+    fq2_mul(&a1b2, &a->c1, &b->c2);
+    fq2_mul(&a2b1, &a->c2, &b->c1);
+    fq6_t o;
+    fq2_add(&t, &a1b2, &a2b1); /* c0 = a0b0 + xi (a1b2 + a2b1) */
+    fq2_mul_xi(&t, &t);
+    fq2_add(&o.c0, &a0b0, &t);
+    fq2_mul_xi(&t, &a2b2); /* c1 = a0b1 + a1b0 + xi a2b2 */
+    fq2_add(&o.c1, &a0b1, &a1b0);
+    fq2_add(&o.c1, &o.c1, &t);
+    fq2_add(&o.c2, &a0b2, &a1b1); /* c2 = a0b2 + a1b1 + a2b0 */
+    fq2_add(&o.c2, &o.c2, &a2b0);
+    *r = o;
+}
+static void fq6_mul_v(fq6_t *r, const fq6_t *a) { /* (c0, c1, c2) v = (xi c2, c0, c1) */
+    fq6_t o;
+    fq2_mul_xi(&o.c0, &a->c2);
+    o.c1 = a->c0;
+    o.c2 = a->c1;
+    *r = o;
+}
+static void fq6_inv(fq6_t *r, const fq6_t *a) {
+    /* (A + B v + C v^2) / N, A = a0^2 - xi a1 a2, B = xi a2^2 - a0 a1,
+     * C = a1^2 - a0 a2, N = a0 A + xi (a2 B + a1 C) */
+    fq2_t A, B, C, t, n, ninv;
+    fq2_mul(&A, &a->c0, &a->c0);
+    fq2_mul(&t, &a->c1, &a->c2);
+    fq2_mul_xi(&t, &t);
+    fq2_sub(&A, &A, &t);
+    fq2_mul(&B, &a->c2, &a->c2);
+    fq2_mul_xi(&B, &B);
+    fq2_mul(&t, &a->c0, &a->c1);
+    fq2_sub(&B, &B, &t);
+    fq2_mul(&C, &a->c1, &a->c1);
+    fq2_mul(&t, &a->c0, &a->c2);
+    fq2_sub(&C, &C, &t);
+    fq2_mul(&n, &a->c2, &B);
+    fq2_mul(&t, &a->c1, &C);
+    fq2_add(&n, &n, &t);
+    fq2_mul_xi(&n, &n);
+    fq2_mul(&t, &a->c0, &A);
+    fq2_add(&n, &n, &t);
+    fq2_inv(&ninv, &n);
+    fq2_mul(&r->c0, &A, &ninv);
+    fq2_mul(&r->c1, &B, &ninv);
+    fq2_mul(&r->c2, &C, &ninv);
+}
+static void fq6_zero(fq6_t *r) { fq2_zero(&r->c0); fq2_zero(&r->c1); fq2_zero(&r->c2); }
+static void fq6_one(fq6_t *r) { fq2_one(&r->c0); fq2_zero(&r->c1); fq2_zero(&r->c2); }
+static int fq6_eq(const fq6_t *a, const fq6_t *b) {
+    return fq2_eq(&a->c0, &b->c0) && fq2_eq(&a->c1, &b->c1) && fq2_eq(&a->c2, &b->c2);
+}
+
+static void fq12_add(fq12_t *r, const fq12_t *a, const fq12_t *b) {
+    fq6_add(&r->c0, &a->c0, &b->c0);
+    fq6_add(&r->c1, &a->c1, &b->c1);
+}
+static void fq12_sub(fq12_t *r, const fq12_t *a, const fq12_t *b) {
+    fq6_sub(&r->c0, &a->c0, &b->c0);
+    fq6_sub(&r->c1, &a->c1, &b->c1);
+}
+static void fq12_mul(fq12_t *r, const fq12_t *a, const fq12_t *b) {
+    /* (a0 + a1 w)(b0 + b1 w) = a0 b0 + v a1 b1 + (a0 b1 + a1 b0) w */
+    fq6_t t0, t1, t2, t3;
+    fq6_mul(&t0, &a->c0, &b->c0);
+    fq6_mul(&t1, &a->c1, &b->c1);
+    fq6_mul(&t2, &a->c0, &b->c1);
+    fq6_mul(&t3, &a->c1, &b->c0);
+    fq6_mul_v(&t1, &t1);
+    fq6_add(&r->c0, &t0, &t1);
+    fq6_add(&r->c1, &t2, &t3);
+}
+static void fq12_inv(fq12_t *r, const fq12_t *a) { /* (a0 - a1 w) / (a0^2 - v a1^2) */
+    fq6_t n, t, ninv;
+    fq6_mul(&n, &a->c0, &a->c0);
+    fq6_mul(&t, &a->c1, &a->c1);
+    fq6_mul_v(&t, &t);
+    fq6_sub(&n, &n, &t);
+    fq6_inv(&ninv, &n);
+    fq6_mul(&r->c0, &a->c0, &ninv);
+    fq6_mul(&t, &a->c1, &ninv);
+    fq6_neg(&r->c1, &t);
+}
+static void fq12_conj(fq12_t *r, const fq12_t *a) { r->c0 = a->c0; fq6_neg(&r->c1, &a->c1); }
+static void fq12_one(fq12_t *r) { fq6_one(&r->c0); fq6_zero(&r->c1); }
+static int fq12_eq(const fq12_t *a, const fq12_t *b) { return fq6_eq(&a->c0, &b->c0) && fq6_eq(&a->c1, &b->c1); }
+static void fq12_from_fq2(fq12_t *r, const fq2_t *a) {
+    fq6_zero(&r->c0);
+    fq6_zero(&r->c1);
+    r->c0.c0 = *a;
+}
+static void fq12_from_fq(fq12_t *r, const fq_t *a) {
+    fq2_t t;
+    t.c0 = *a;
+    fq_zero(&t.c1);
+    fq12_from_fq2(r, &t);
+}
+static void fq12_pow(fq12_t *r, const fq12_t *a, const uint64_t *e, size_t limbs) {
+    fq12_t acc;
+    fq12_one(&acc);
+    int started = 0;
+    for (size_t i = limbs; i-- > 0;)
+        for (int bit = 63; bit >= 0; bit--) {
+            if (started) fq12_mul(&acc, &acc, &acc);
+            if ((e[i] >> bit) & 1) {
+                fq12_mul(&acc, &acc, a);
+                started = 1;
+            }
+        }
+    *r = acc;
+}
+
+/* sqrt in Fq (p = 3 mod 4): a^((p+1)/4); returns 1 iff a is a square */
+static int fq_sqrt(fq_t *r, const fq_t *a) {
+    uint64_t e[6];
+    memcpy(e, FQ_P, sizeof e);
+    e[0] += 1; /* p + 1: p's low limb ends in ...aaab, no carry */
+    for (int i = 0; i < 6; i++) e[i] = (e[i] >> 2) | (i < 5 ? e[i + 1] << 62 : 0);
+    fq_t s, chk;
+    fq_pow(&s, a, e);
+    fq_mul(&chk, &s, &s);
+    if (!fq_eq(&chk, a)) return 0;
+    *r = s;
+    return 1;
+}
+
+/* sqrt in Fq2 by the norm method; returns 1 iff a is a square */
+static int fq2_sqrt(fq2_t *r, const fq2_t *a) {
+    if (fq2_is_zero(a)) {
+        fq2_zero(r);
+        return 1;
+    }
+    fq_t two, half;
+    fq_from_u64(&two, 2);
+    fq_inv(&half, &two);
+    fq2_t cand;
+    if (fq_is_zero(&a->c1)) {
+        fq_t s, n;
+        if (fq_sqrt(&s, &a->c0)) {
+            cand.c0 = s;
+            fq_zero(&cand.c1);
+        } else {
+            fq_neg(&n, &a->c0);
+            if (!fq_sqrt(&s, &n)) return 0;
+            fq_zero(&cand.c0);
+            cand.c1 = s; /* (s u)^2 = -s^2 */
+        }
+    } else {
+        fq_t alpha, t, gamma, delta, x0, x1, d;
+        fq_mul(&alpha, &a->c0, &a->c0);
+        fq_mul(&t, &a->c1, &a->c1);
+        fq_add(&alpha, &alpha, &t);
+        if (!fq_sqrt(&gamma, &alpha)) return 0;
+        fq_add(&delta, &a->c0, &gamma);
+        fq_mul(&delta, &delta, &half);
+        if (!fq_sqrt(&x0, &delta)) {
+            fq_sub(&delta, &a->c0, &gamma);
+            fq_mul(&delta, &delta, &half);
+            if (!fq_sqrt(&x0, &delta)) return 0;
+        }
+        fq_add(&d, &x0, &x0);
+        fq_inv(&d, &d);
+        fq_mul(&x1, &a->c1, &d);
+        cand.c0 = x0;
+        cand.c1 = x1;
+    }
+    fq2_t chk;
+    fq2_mul(&chk, &cand, &cand);
+    if (!fq2_eq(&chk, a)) return 0;
+    *r = cand;
+    return 1;
+}
+
+typedef struct { fq2_t x, y; int inf; } g2a_t;
+
+static void g2_b(fq2_t *b) { /* 4 xi = 4 + 4u */
+    fq_from_u64(&b->c0, 4);
+    fq_from_u64(&b->c1, 4);
+}
+static int g2_on_curve(const g2a_t *p) {
+    if (p->inf) return 1;
+    fq2_t l, r, b;
+    fq2_mul(&l, &p->y, &p->y);
+    fq2_mul(&r, &p->x, &p->x);
+    fq2_mul(&r, &r, &p->x);
+    g2_b(&b);
+    fq2_add(&r, &r, &b);
+    return fq2_eq(&l, &r);
+}
+static void g2_double(g2a_t *r, const g2a_t *p) {
+    if (p->inf || fq2_is_zero(&p->y)) {
+        memset(r, 0, sizeof *r);
+        r->inf = 1;
+        return;
+    }
+    fq2_t lam, t, d, x3, y3;
+    fq2_mul(&t, &p->x, &p->x);
+    fq2_add(&lam, &t, &t);
+    fq2_add(&lam, &lam, &t);
+    fq2_add(&d, &p->y, &p->y);
+    fq2_inv(&d, &d);
+    fq2_mul(&lam, &lam, &d);
+    fq2_mul(&x3, &lam, &lam);
+    fq2_sub(&x3, &x3, &p->x);
+    fq2_sub(&x3, &x3, &p->x);
+    fq2_sub(&t, &p->x, &x3);
+    fq2_mul(&y3, &lam, &t);
+    fq2_sub(&y3, &y3, &p->y);
+    r->x = x3;
+    r->y = y3;
+    r->inf = 0;
+}
+static void g2_add(g2a_t *r, const g2a_t *p, const g2a_t *q) {
+    if (p->inf) { *r = *q; return; }
+    if (q->inf) { *r = *p; return; }
+    if (fq2_eq(&p->x, &q->x)) {
+        if (fq2_eq(&p->y, &q->y)) g2_double(r, p);
+        else { memset(r, 0, sizeof *r); r->inf = 1; }
+        return;
+    }
+    fq2_t lam, t, d, x3, y3;
+    fq2_sub(&lam, &q->y, &p->y);
+    fq2_sub(&d, &q->x, &p->x);
+    fq2_inv(&d, &d);
+    fq2_mul(&lam, &lam, &d);
+    fq2_mul(&x3, &lam, &lam);
+    fq2_sub(&x3, &x3, &p->x);
+    fq2_sub(&x3, &x3, &q->x);
+    fq2_sub(&t, &p->x, &x3);
+    fq2_mul(&y3, &lam, &t);
+    fq2_sub(&y3, &y3, &p->y);
+    r->x = x3;
+    r->y = y3;
+    r->inf = 0;
+}
+static void g2_mul(g2a_t *r, const g2a_t *p, const uint64_t *k, size_t limbs) {
+    g2a_t acc;
+    memset(&acc, 0, sizeof acc);
+    acc.inf = 1;
+    for (size_t i = limbs; i-- > 0;)
+        for (int bit = 63; bit >= 0; bit--) {
+            g2_double(&acc, &acc);
+            if ((k[i] >> bit) & 1) g2_add(&acc, &acc, p);
+        }
+    *r = acc;
+}
+static int g2_from_bytes(g2a_t *r, const uint8_t *b) {
+    int zero = 1;
+    for (int i = 0; i < 192; i++) zero &= b[i] == 0;
+    memset(r, 0, sizeof *r);
+    if (zero) {
+        r->inf = 1;
+        return 1;
+    }
+    return fq_from_bytes(&r->x.c0, b) && fq_from_bytes(&r->x.c1, b + 48) && fq_from_bytes(&r->y.c0, b + 96) &&
+           fq_from_bytes(&r->y.c1, b + 144) && g2_on_curve(r);
+}
+static void g2_to_bytes(uint8_t *b, const g2a_t *p) {
+    if (p->inf) {
+        memset(b, 0, 192);
+        return;
+    }
+    fq_to_bytes(b, &p->x.c0);
+    fq_to_bytes(b + 48, &p->x.c1);
+    fq_to_bytes(b + 96, &p->y.c0);
+    fq_to_bytes(b + 144, &p->y.c1);
+}
+
+/* f_{|z|, Q}(P) with Q untwisted into E(Fq12), conjugated for z < 0 */
+static void miller_loop(fq12_t *out, const g1a_t *P, const g2a_t *Q) {
+    const uint64_t z = 0xd201000000010000ULL;
+    fq12_t w, wi, wi2, wi3, qx, qy, px, py, tx, ty, f;
+    fq6_zero(&w.c0);
+    fq6_one(&w.c1);
+    fq12_inv(&wi, &w);
+    fq12_mul(&wi2, &wi, &wi);
+    fq12_mul(&wi3, &wi2, &wi);
+    fq12_from_fq2(&qx, &Q->x);
+    fq12_mul(&qx, &qx, &wi2);
+    fq12_from_fq2(&qy, &Q->y);
+    fq12_mul(&qy, &qy, &wi3);
+    fq12_from_fq(&px, &P->x);
+    fq12_from_fq(&py, &P->y);
+    tx = qx;
+    ty = qy;
+    fq12_one(&f);
+    for (int bit = 62; bit >= 0; bit--) {
+        fq12_t lam, num, den, l, t, nx, ny;
+        /* tangent at T */
+        fq12_mul(&t, &tx, &tx);
+        fq12_add(&num, &t, &t);
+        fq12_add(&num, &num, &t);
+        fq12_add(&den, &ty, &ty);
+        fq12_inv(&den, &den);
+        fq12_mul(&lam, &num, &den);
+        fq12_sub(&t, &px, &tx);
+        fq12_mul(&t, &lam, &t);
+        fq12_sub(&l, &py, &ty);
+        fq12_sub(&l, &l, &t);
+        fq12_mul(&f, &f, &f);
+        fq12_mul(&f, &f, &l);
+        fq12_mul(&nx, &lam, &lam);
+        fq12_sub(&nx, &nx, &tx);
+        fq12_sub(&nx, &nx, &tx);
+        fq12_sub(&t, &tx, &nx);
+        fq12_mul(&ny, &lam, &t);
+        fq12_sub(&ny, &ny, &ty);
+        tx = nx;
+        ty = ny;
+        if ((z >> bit) & 1) {
+            /* chord through T and Q */
+            fq12_sub(&num, &qy, &ty);
+            fq12_sub(&den, &qx, &tx);
+            fq12_inv(&den, &den);
+            fq12_mul(&lam, &num, &den);
+            fq12_sub(&t, &px, &tx);
+            fq12_mul(&t, &lam, &t);
+            fq12_sub(&l, &py, &ty);
+            fq12_sub(&l, &l, &t);
+            fq12_mul(&f, &f, &l);
+            fq12_mul(&nx, &lam, &lam);
+            fq12_sub(&nx, &nx, &tx);
+            fq12_sub(&nx, &nx, &qx);
+            fq12_sub(&t, &tx, &nx);
+            fq12_mul(&ny, &lam, &t);
+            fq12_sub(&ny, &ny, &ty);
+            tx = nx;
+            ty = ny;
+        }
+    }
+    fq12_conj(out, &f);
+}
+
+/* The fixed G2 point: the first x = (k, 1), k = 1, 2, ..., with x^3 + 4 xi a
+ * square, times the cofactor (#E'(Fq2) / r, given as limbs). */
+int or_g2_derive(const uint64_t *cofactor, size_t limbs, uint8_t *out192) {
+    for (uint64_t k = 1; k < 1000; k++) {
+        g2a_t p, q;
+        fq2_t rhs, b;
+        memset(&p, 0, sizeof p);
+        fq_from_u64(&p.x.c0, k);
+        fq_from_u64(&p.x.c1, 1);
+        fq2_mul(&rhs, &p.x, &p.x);
+        fq2_mul(&rhs, &rhs, &p.x);
+        g2_b(&b);
+        fq2_add(&rhs, &rhs, &b);
+        if (!fq2_sqrt(&p.y, &rhs)) continue;
+        g2_mul(&q, &p, cofactor, limbs);
+        if (q.inf) continue;
+        g2_to_bytes(out192, &q);
+        return 0;
+    }
+    return 1;
+}
+
+/* op 0: a + b; 1: -a; 2: k * a (k: canonical Fr, 32 bytes LE); 3: on-curve
+ * check of a (returns 0 on curve).  Nonzero return: malformed input. */
+int or_g2_op(int op, const uint8_t *a, const uint8_t *b, const uint8_t *k32, uint8_t *out192) {
+    g2a_t pa, pb, res;
+    if (!g2_from_bytes(&pa, a)) return 1;
+    switch (op) {
+        case 0:
+            if (!g2_from_bytes(&pb, b)) return 1;
+            g2_add(&res, &pa, &pb);
+            break;
+        case 1:
+            res = pa;
+            if (!pa.inf) fq2_neg(&res.y, &pa.y);
+            break;
+        case 2: {
+            uint64_t k[4];
+            memcpy(k, k32, 32);
+            g2_mul(&res, &pa, k, 4);
+            break;
+        }
+        case 3:
+            return 0;
+        default:
+            return 1;
+    }
+    g2_to_bytes(out192, &res);
+    return 0;
+}
+
+/* prod_i e(P_i, Q_i) == 1 ?  1: yes, 0: no, -1: malformed point.  `fexp` is
+ * (p^12 - 1) / r as little-endian limbs. */
+int or_pairing_product_is_one(const uint8_t *g1s96, const uint8_t *g2s192, size_t n, const uint64_t *fexp,
+                              size_t limbs) {
+    fq12_t acc, one;
+    fq12_one(&acc);
+    for (size_t i = 0; i < n; i++) {
+        g1a_t p;
+        g2a_t q;
+        if (!g1a_from_bytes(&p, g1s96 + 96 * i) || !g2_from_bytes(&q, g2s192 + 192 * i)) return -1;
+        if (p.inf || q.inf) continue;
+        fq12_t f;
+        miller_loop(&f, &p, &q);
+        fq12_mul(&acc, &acc, &f);
+    }
+    fq12_pow(&acc, &acc, fexp, limbs);
+    fq12_one(&one);
+    return fq12_eq(&acc, &one) ? 1 : 0;
+}
