@@ -131,13 +131,14 @@ def pairing_product_is_one(pairs) -> bool:
 
 def srs_verifier_param(num_vars: int, seed: int) -> dict:
     """g (G1 (x, y)), h and h_mask (192-byte G2) of the testing SRS of
-    oracle.srs_layers(num_vars, seed): h_mask[i] = t_i h."""
-    layers = oracle.srs_layers(num_vars, seed)
-    g = oracle.affine_to_point(layers[num_vars][:96])
-
+    oracle.srs_layers(num_vars, seed) (and of the device generator with the
+    same seed): h_mask[i] = t_i h.  Needs only the seed's stream, not the
+    layers."""
     def stream_fr(i: int) -> int:
         return oracle.fr_int(oracle.fr_from_wide(oracle.chacha20_block(seed, i)))
 
+    # the SRS's last layer [g]: g = s_g G1 with s_g from block num_vars (or_srs_gen)
+    g = oracle.affine_to_point(oracle.msm(oracle.g1_generator(), stream_fr(num_vars).to_bytes(32, "little")))
     ts = [stream_fr(i) for i in range(num_vars)]
     s = stream_fr(num_vars + 1)
     h = g2_mul(g2_base(), s)

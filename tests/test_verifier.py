@@ -130,3 +130,18 @@ def test_gpu_proof_verifies_and_keys_equal_oracle(gpu, oracle, cpu, pr, ver, nv)
     bad = copy.deepcopy(proof)
     bad.batch_openings.g_prime_proof[0] = g1_mul(oracle, bad.batch_openings.g_prime_proof[0], 2)
     assert not ver.hyperplonk_verify(vk, pub, bad)
+
+
+@pytest.mark.gpu
+def test_gpu_headline_proof_verifies(gpu, oracle, pr, ver):
+    """The nv=20 proof of the default bench workload (vanilla fixture seed 2,
+    device-generated testing SRS seed 0) is accepted."""
+    nv = 20
+    layers = gpu.generate_srs(nv, 0)
+    assert oracle.affine_to_point(oracle.packets_to_affine(layers[nv])) == pr.srs_verifier_param(nv, 0)["g"]
+    sel, wit, perm, pub = snark.vanilla_fixture(nv, 2)
+    pk = snark.preprocess(gpu, nv, 16, sel, perm, layers)
+    del layers
+    proof = snark.prove(gpu, pk, pub, wit)
+    vk = pk.verifying_key(pr.srs_verifier_param(nv, 0))
+    assert ver.hyperplonk_verify(vk, pub, proof)
