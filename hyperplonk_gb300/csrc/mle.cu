@@ -47,13 +47,23 @@ __global__ void k_from_mont(const Fr *src, Fr *dst, size_t n) {
         store_fr(&dst[i], from_mont(load_fr(&src[i])));
 }
 
+// out[i] (+)= sum_j c_j polys_j[i].  From three terms on the products are
+// summed unreduced (FrAcc) and reduced once per element.
 __global__ void k_linear_combination(Fr *out, FrPtrList polys, FrScalarList coefs, int count,
                                      size_t n, bool accumulate) {
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n;
          i += size_t(gridDim.x) * blockDim.x) {
-        Fr acc = accumulate ? load_fr(&out[i]) : Fr::zero();
-        for (int j = 0; j < count; j++) acc = acc + load_fr(&polys.p[j][i]) * coefs.s[j];
-        store_fr(&out[i], acc);
+        if (count >= 3) {
+            FrAcc X;
+            acc_zero(X);
+            if (accumulate) acc_add_shifted(X, load_fr(&out[i]));
+            for (int j = 0; j < count; j++) acc_mul_add(X, load_fr(&polys.p[j][i]), coefs.s[j]);
+            store_fr(&out[i], acc_reduce(X));
+        } else {
+            Fr acc = accumulate ? load_fr(&out[i]) : Fr::zero();
+            for (int j = 0; j < count; j++) acc = acc + load_fr(&polys.p[j][i]) * coefs.s[j];
+            store_fr(&out[i], acc);
+        }
     }
 }
 
@@ -513,11 +523,14 @@ __device__ __forceinline__ Fr block_sum(Fr v) {  // blockDim.x = 256; result in 
     return v;
 }
 
+// Block partials of sum_i a[i] b[i]: each thread's products summed unreduced
+// (FrAcc), one reduction per thread.
 __global__ void __launch_bounds__(256) k_dot_partials(const Fr *a, const Fr *b, size_t n, Fr *partials) {
-    Fr acc = Fr::zero();
+    FrAcc X;
+    acc_zero(X);
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
-        acc = acc + load_fr(&a[i]) * load_fr(&b[i]);
-    acc = block_sum(acc);
+        acc_mul_add(X, load_fr(&a[i]), load_fr(&b[i]));
+    Fr acc = block_sum(acc_reduce(X));
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
 
@@ -572,7 +585,8 @@ extern "C" HpCudaStatus hp_cuda_v1_mle_evaluate_many(HpCudaContext *ctx, size_t 
             Scratch rd(ctx, nv * sizeof(Fr)), eq(ctx, n * sizeof(Fr));
             check_cuda(cudaMemcpyAsync(rd.ptr, pts[k].data(), nv * sizeof(Fr), cudaMemcpyHostToDevice, ctx->stream));
             hp::build_eq(ctx, rd.as<Fr>(), nv, eq.as<Fr>());
-            const unsigned grid = hp::grid_for(ctx, n, 256, 8);
+            // a few blocks per SM: long per-thread runs amortise the reduction
+            const unsigned grid = hp::grid_for(ctx, n, 256, 2);
             Scratch part(ctx, size_t(grid) * sizeof(Fr));
             for (size_t j : group) {
                 hp::k_dot_partials<<<grid, 256, 0, ctx->stream>>>(tables[j], eq.as<Fr>(), n, part.as<Fr>());

@@ -238,84 +238,6 @@ __global__ void __launch_bounds__(kRoundThreads) k_sumcheck_round_regs(SumcheckD
     finish_round_in_last_block(desc, partials, int(gridDim.x), counter, weights, degree, out, acc);
 }
 
-// Unreduced sums of Montgomery products.  The last factor product of a slot
-// value is not reduced per pair: the 512-bit a*b goes into a 17-limb
-// accumulator (no overflow below 2^32 products of values < r), reduced once
-// per thread at the end, as REDC(sum a_i b_i) = sum REDC(a_i b_i) mod r.
-// This halves the multiply work of that product and replaces the per-pair
-// modular add by a carry chain.
-struct FrAcc {
-    uint32_t w[17];
-};
-
-__device__ __forceinline__ void acc_zero(FrAcc &X) {
-#pragma unroll
-    for (int i = 0; i < 17; i++) X.w[i] = 0;
-}
-
-__device__ __forceinline__ void acc_mul_add(FrAcc &X, const Fr &a, const Fr &b) {
-    uint32_t z[16];
-    school_wide<8>(a.v, b.v, z);
-    X.w[0] = add_cc(X.w[0], z[0]);
-#pragma unroll
-    for (int i = 1; i < 16; i++) X.w[i] = addc_cc(X.w[i], z[i]);
-    X.w[16] = addc(X.w[16], 0);
-}
-
-// X += a * 2^256, whose REDC is a (products of arity 1)
-__device__ __forceinline__ void acc_add_shifted(FrAcc &X, const Fr &a) {
-    X.w[8] = add_cc(X.w[8], a.v[0]);
-#pragma unroll
-    for (int i = 1; i < 8; i++) X.w[8 + i] = addc_cc(X.w[8 + i], a.v[i]);
-    X.w[16] = addc(X.w[16], 0);
-}
-
-// REDC(X) = X 2^-256 mod r, in [0, r): 8 Montgomery rows over the low 16
-// limbs (result < 2^256 + r < 4r, so at most 3 subtractions of r), plus the
-// share of limb 16, w 2^512 2^-256 = w 2^256 = to_mont(w).
-__device__ Fr acc_reduce(const FrAcc &X) {
-    uint32_t t[17];
-#pragma unroll
-    for (int i = 0; i < 16; i++) t[i] = X.w[i];
-    t[16] = 0;
-#pragma unroll
-    for (int i = 0; i < 8; i++) {
-        const uint32_t m = t[i] * FrParams::INV;
-        uint32_t carry = 0;
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-            const uint64_t d = uint64_t(m) * FrParams::p(j) + (uint64_t(t[i + j]) + carry);
-            t[i + j] = uint32_t(d);
-            carry = uint32_t(d >> 32);
-        }
-#pragma unroll
-        for (int j = i + 8; j < 17; j++) {
-            const uint64_t d = uint64_t(t[j]) + carry;
-            t[j] = uint32_t(d);
-            carry = uint32_t(d >> 32);
-        }
-    }
-    Fr r;
-#pragma unroll
-    for (int i = 0; i < 8; i++) r.v[i] = t[8 + i];
-    uint32_t hi = t[16];
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        uint32_t u[8];
-        u[0] = sub_cc(r.v[0], FrParams::p(0));
-#pragma unroll
-        for (int i = 1; i < 8; i++) u[i] = subc_cc(r.v[i], FrParams::p(i));
-        const uint32_t h2 = subc(hi, 0);
-        const bool keep = h2 == 0xffffffffu;  // (hi, r) < p
-#pragma unroll
-        for (int i = 0; i < 8; i++) r.v[i] = keep ? r.v[i] : u[i];
-        hi = keep ? hi : h2;
-    }
-    Fr w = Fr::zero();
-    w.v[0] = X.w[16];
-    return r + to_mont(w);
-}
-
 // dst_f[i] = src_f[2i] + r (src_f[2i+1] - src_f[2i]) for the `count` factor
 // tables, i < 2^log_half: the fold of a large round, ahead of the (slot, pair)
 // kernel below (elementwise, so every pass is coalesced and HBM-bound).
