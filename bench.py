@@ -48,6 +48,7 @@ sys.path.insert(0, str(ROOT))
 
 FQ_MUL_IMAD = 588  # 32-bit-limb CIOS, n = 12: 2n^2 + 2n^2 + n
 FR_MUL_IMAD = 264
+FQ_MUL_WIDE = 252  # wide multiply-adds of the library's Fq product: 3 x 36 (Karatsuba) + 12 x 12 (reduction rows)
 PROVE_SEED = 2
 
 
@@ -337,6 +338,16 @@ class Session:
         t = self.torch.empty(arr.nbytes, dtype=self.torch.uint8, pin_memory=True)
         t.numpy()[:] = arr.reshape(-1)
         return t
+
+    def wide_rate(self) -> float:
+        """mad.wide.u32 (32x32->64 multiply-add) issues per second on this GPU."""
+        probe = ctypes.CDLL(str(ROOT / "hyperplonk_gb300" / "_build" / "libhp_probe.so"))
+        probe.hp_probe_wide_rate.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+        w = ctypes.c_double()
+        rc = probe.hp_probe_wide_rate(self.local, ctypes.byref(w))
+        if rc != 0:
+            raise RuntimeError(f"wide-multiply probe failed ({rc})")
+        return w.value
 
     def integer_rates(self):
         probe = ctypes.CDLL(str(ROOT / "hyperplonk_gb300" / "_build" / "libhp_probe.so"))
@@ -727,6 +738,17 @@ def run_gb300(args, world, rank, local, pg):
         "clocks": clk,
     }
     result.update(extra)
+    # the same kernel against the pipe it actually fills: a Karatsuba Fq
+    # product issues 108 + 144 wide multiply-adds, so the live mad.wide rate
+    # / 252 caps the product rate before any addition, carry or load
+    wide = s.wide_rate()
+    if acc_ms_total > 0:
+        fq_done = acc_work / FQ_MUL_IMAD / (acc_ms_total / 1e3)
+        result["roofline"]["pipe"] = {
+            "bound": "mad.wide.u32 issue (32x32->64 multiply-add)", "wide_per_s": wide,
+            "wide_per_fq_mul": FQ_MUL_WIDE, "fq_mul_cap_per_s": wide / FQ_MUL_WIDE,
+            "achieved_fq_mul_per_s": fq_done, "frac": fq_done / (wide / FQ_MUL_WIDE),
+            "source": "measured live (libhp_probe: independent mad.wide.u32 chains)"}
     # the whole 2^nv MSM (sort, accumulation, reduction, host finish) against
     # the fixed accounting of the IMAD work, timed alone by the library hooks
     msm_ms = msm[0] / max(1, msm[1])
