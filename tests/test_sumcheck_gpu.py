@@ -76,6 +76,17 @@ def test_mixed_products(gpu, cpu, oracle):
     run_both(gpu, cpu, vg, vc, 9)
 
 
+def test_mixed_arity_large_rounds(gpu, cpu, oracle):
+    """Arity 1..5 products at nv = 15: the first rounds run the fold kernel
+    and the (slot, pair) kernel over the folded tables (arity-1 slots take
+    the shifted accumulator, arity 5 the <6> instantiation), the later ones
+    the fused and one-block kernels."""
+    nv = 15
+    prods = [(3, [0]), (R - 2, [1, 2]), (5, [2, 3, 4]), (7, [0, 5, 1, 6]), (11, [6, 5, 4, 3, 2]), (13, [1])]
+    vg, vc, _, _ = build_pair(gpu, cpu, oracle, nv, 7, prods, 7)
+    run_both(gpu, cpu, vg, vc, 15)
+
+
 def test_repeated_factors_max_degree_34(gpu, cpu, oracle):
     nv = 6
     prods = [(3, [0] * 34), (5, [1, 0, 1]), (R - 7, [2] * 17 + [1] * 10), (9, [2])]
