@@ -421,7 +421,7 @@ def run_sumcheck(args, world, rank, local, pg):
         out["finals"] = finals
 
     def e2e_fn():
-        m = [be.mle_from_evaluations(nv, t) for t in tables]
+        m = be.mle_from_evaluations_many(nv, tables)
         vp = workloads.sumcheck_polynomial(nv, m, coefs)
         protocol.sumcheck_prove(be, vp, IOPTranscript(workloads.SUMCHECK_LABEL), [])
 

@@ -222,6 +222,22 @@ class CudaBackend:
                                                     ctypes.byref(out)), "mle_upload")
         return self._new(out, num_vars)
 
+    def mle_from_evaluations_many(self, num_vars: int, tables: Sequence) -> list:
+        """Several tables of the same size in one upload call (one validation
+        synchronisation); equal to mle_from_evaluations of each."""
+        datas = [table_bytes(t) for t in tables]
+        for d in datas:
+            n = _nbytes(d)
+            if num_vars >= 64 or n % 32 or n // 32 != (1 << num_vars):
+                raise InvalidParameters(f"evaluation count {n // 32} does not match {num_vars} variables")
+        if not datas:
+            return []
+        ptrs = (_native.c_u8p * len(datas))(*[_native.buf(d) for d in datas])
+        out = (ctypes.c_void_p * len(datas))()
+        check_status(self.lib.hp_cuda_v1_mle_upload_many(self.ctx.raw, num_vars, ptrs, len(datas), 1 << num_vars,
+                                                         out), "mle_upload_many")
+        return [self._new(ctypes.c_void_p(a), num_vars) for a in out]
+
     def generate_srs(self, num_vars: int, seed: int) -> list:
         """Testing SRS of num_vars variables from fixture seed `seed`, computed
         on the device: num_vars + 1 layers of 97-byte packets (uint8 arrays),

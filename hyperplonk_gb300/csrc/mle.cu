@@ -430,6 +430,38 @@ extern "C" HpCudaStatus hp_cuda_v1_mle_upload(HpCudaContext *ctx, size_t num_var
     });
 }
 
+extern "C" HpCudaStatus hp_cuda_v1_mle_upload_many(HpCudaContext *ctx, size_t num_vars,
+                                                   const uint8_t *const *evaluations, size_t count,
+                                                   size_t evaluation_count, HpCudaDeviceAddress *out) {
+    if (out)
+        for (size_t i = 0; i < count; i++) out[i] = nullptr;
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(out != nullptr && (count == 0 || evaluations != nullptr) && num_vars <= hp::kMaxNumVars);
+        const size_t n = table_len(num_vars);
+        require(evaluation_count == n);
+        for (size_t i = 0; i < count; i++) require(evaluations[i] != nullptr);
+        if (count == 0) return;
+        // every copy and conversion queued back to back, one validation
+        // synchronisation for the batch; a non-canonical table fails the
+        // whole call and every buffer of it is released
+        std::vector<OwnedBuffer> bufs;
+        bufs.reserve(count);
+        ctx->clear_flags();
+        for (size_t i = 0; i < count; i++) {
+            bufs.emplace_back(ctx, n * kFrBytes);
+            check_cuda(cudaMemcpyAsync(bufs.back().ptr, evaluations[i], n * kFrBytes, cudaMemcpyHostToDevice,
+                                       ctx->stream));
+            hp::k_to_mont_check<<<hp::grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(bufs.back().as<Fr>(), n,
+                                                                                   ctx->d_flags);
+            check_launch();
+        }
+        const uint32_t flags = ctx->sync_flags();
+        if (flags & hp::kFlagNonCanonical) fail(HP_CUDA_STATUS_INVALID_PARAMETERS);
+        for (size_t i = 0; i < count; i++) out[i] = bufs[i].release();
+    });
+}
+
 extern "C" HpCudaStatus hp_cuda_v1_mle_download(HpCudaContext *ctx, HpCudaDeviceAddress polynomial,
                                                 size_t num_vars, uint8_t *out_evaluations,
                                                 size_t evaluation_count) {

@@ -137,7 +137,10 @@ def prove(backend, pk: ProvingKey, pub_input: list, witnesses: list, transcript_
     acc = PcsAccumulator(nv)
     # 1. witnesses
     if witness_mles is None:
-        witness_mles = [backend.mle_from_evaluations(nv, w) for w in witnesses]
+        if hasattr(backend, "mle_from_evaluations_many"):  # one upload call, one validation sync
+            witness_mles = backend.mle_from_evaluations_many(nv, witnesses)
+        else:
+            witness_mles = [backend.mle_from_evaluations(nv, w) for w in witnesses]
     commits = backend.multi_commit(pk.pcs_param, witness_mles)
     mark("witness_commit")
     for c in commits:

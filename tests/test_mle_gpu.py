@@ -182,3 +182,20 @@ def test_evaluate_many_shared_points_use_eq_dot_products(gpu, oracle):
     assert many == [gpu.evaluate_mle(m, p) for m, p in zip(mles, points)]
     cpu = oracle.CpuBackend()
     assert many == [cpu.evaluate_mle(cpu.mle_from_evaluations(nv, t), p) for t, p in zip(tables, points)]
+
+
+def test_upload_many_equals_single_uploads(gpu, oracle):
+    from hyperplonk_gb300.errors import InvalidParameters
+    nv = 9
+    tables = [oracle.random_fr(40 + k, 1 << nv) for k in range(4)]
+    many = gpu.mle_from_evaluations_many(nv, tables)
+    for t, m in zip(tables, many):
+        assert gpu.download(m) == t
+        assert gpu.evaluate_mle(m, [3] * nv) == gpu.evaluate_mle(gpu.mle_from_evaluations(nv, t), [3] * nv)
+    assert gpu.mle_from_evaluations_many(nv, []) == []
+    bad = bytearray(tables[2])
+    bad[32 * 17:32 * 18] = (0x73EDA753299D7D483339D80809A1D80553BDA402FFFE5BFEFFFFFFFF00000001).to_bytes(32, "little")
+    with pytest.raises(InvalidParameters):
+        gpu.mle_from_evaluations_many(nv, [tables[0], bytes(bad), tables[1]])
+    with pytest.raises(InvalidParameters):
+        gpu.mle_from_evaluations_many(nv, [tables[0], tables[1][:-32]])
