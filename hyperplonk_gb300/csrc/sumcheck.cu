@@ -16,11 +16,13 @@
 // with the message of round k, so each factor table is read once and its
 // folded half written once per round, and the last block of the launch sums
 // the block partials, extrapolates, scales and writes canonical bytes.
-// Large rounds: one pair per thread, per-thread slot sums in shared memory.
-// Rounds of up to a few thousand pairs: one (slot, pair) item per thread,
-// so the latency chain per thread is one product, not the whole polynomial.
-// Products of arity > 8 or more than 48 slots use a shared-memory kernel and
-// a separate one-block finalize.
+// Rounds of more than 64 pairs: one (slot, pair) item per thread, so the
+// latency chain per thread is one product, not the whole polynomial (large
+// rounds after an elementwise fold of every table; smaller ones with the fold
+// fused).  Rounds of <= 64 pairs: one block over (factor, pair) and
+// (product, pair) items.  Products of any arity up to the degree bound and
+// any slot count go through the (slot, pair) kernel; the per-pair kernel
+// with per-thread slot sums in shared memory remains for HP_BIG_SLOTS=0.
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
@@ -40,78 +42,6 @@ using hp::guard;
 using hp::require;
 
 namespace hp {
-
-// Shared-memory layout per thread (T threads per block, column-major by slot
-// so thread t's entries are sm[slot * T + t]):
-//   [0, 2F)           lo_f, d_f  (folded pair value and its step)
-//   [2F, 2F + M)      running evaluations of the current product
-//   [2F + M, ...+S)   accumulators, one per (product, t) slot
-__global__ void k_sumcheck_round(SumcheckDesc desc, FrPtrList src, FrMutPtrList dst, bool fold,
-                                 Fr r, size_t pairs, Fr *partials) {
-    extern __shared__ Fr sm[];
-    const int T = blockDim.x;
-    const int t = threadIdx.x;
-    const int F = desc.factor_count;
-    const int M = desc.max_arity;
-    const int S = desc.slot_count;
-    Fr *fv = sm;
-    Fr *ev = sm + 2 * F * T;
-    Fr *acc = ev + M * T;
-    for (int s = 0; s < S; s++) acc[s * T + t] = Fr::zero();
-
-    for (size_t b = blockIdx.x * size_t(T) + t; b < pairs; b += size_t(gridDim.x) * T) {
-        for (int f = 0; f < F; f++) {
-            Fr lo, hi;
-            if (fold) {
-                const Fr *s = src.p[f] + 4 * b;
-                Fr a0 = load_fr(s), a1 = load_fr(s + 1), a2 = load_fr(s + 2), a3 = load_fr(s + 3);
-                lo = a0 + r * (a1 - a0);
-                hi = a2 + r * (a3 - a2);
-                Fr *d = dst.p[f] + 2 * b;
-                store_fr(d, lo);
-                store_fr(d + 1, hi);
-            } else {
-                const Fr *s = src.p[f] + 2 * b;
-                lo = load_fr(s);
-                hi = load_fr(s + 1);
-            }
-            fv[(2 * f) * T + t] = lo;
-            fv[(2 * f + 1) * T + t] = hi - lo;
-        }
-        for (int p = 0; p < desc.product_count; p++) {
-            const int begin = desc.offsets[p], m = desc.offsets[p + 1] - begin;
-            const int slot = desc.slot_base[p];
-            Fr prod = fv[(2 * desc.indices[begin]) * T + t];
-            ev[t] = prod;
-            for (int j = 1; j < m; j++) {
-                Fr v = fv[(2 * desc.indices[begin + j]) * T + t];
-                ev[j * T + t] = v;
-                prod = prod * v;
-            }
-            acc[slot * T + t] = acc[slot * T + t] + prod;
-            for (int k = 1; k <= m; k++) {
-                Fr e = ev[t] + fv[(2 * desc.indices[begin] + 1) * T + t];
-                ev[t] = e;
-                prod = e;
-                for (int j = 1; j < m; j++) {
-                    Fr ej = ev[j * T + t] + fv[(2 * desc.indices[begin + j] + 1) * T + t];
-                    ev[j * T + t] = ej;
-                    prod = prod * ej;
-                }
-                acc[(slot + k) * T + t] = acc[(slot + k) * T + t] + prod;
-            }
-        }
-    }
-    // block tree reduction of every slot
-    for (int s = 0; s < S; s++) {
-        __syncthreads();
-        for (int half = T / 2; half > 0; half >>= 1) {
-            if (t < half) acc[s * T + t] = acc[s * T + t] + acc[s * T + t + half];
-            __syncthreads();
-        }
-        if (t == 0) partials[size_t(s) * gridDim.x + blockIdx.x] = acc[s * T];  // slot-major
-    }
-}
 
 // Register-resident round for products of arity <= MAXM (every VP of the
 // prover: degree <= 5).  One pair per thread per iteration; the fold of all
@@ -254,7 +184,8 @@ __global__ void __launch_bounds__(256) k_sumcheck_fold(FrPtrList src, FrMutPtrLi
     }
 }
 
-// One thread per (slot, pair) item, slot = (product p, node t): the thread
+// One thread per (slot, pair) item, slot = (product p, node t), products of
+// any arity (MAXM = the largest, unrolled; 0: a runtime loop): the thread
 // steps the m factors of p to t at its pair and multiplies them, a chain of
 // m - 1 products with the last one accumulated unreduced -- no per-thread
 // slot table, so occupancy is set by registers alone.  Block = kWideThreads
@@ -312,28 +243,32 @@ __global__ void HP_WIDE_BOUNDS k_sumcheck_round_wide(SumcheckDesc desc, FrPtrLis
     const size_t stride = size_t(blocks_per_slot) * kWideThreads;
     for (size_t b = size_t(blk) * kWideThreads + threadIdx.x; b < pairs; b += stride) {
         Fr v;
-#pragma unroll
-        for (int j = 0; j < MAXM; j++) {
-            if (j < m) {
-                const int f = desc.indices[begin + j];
-                Fr lo, hi;
-                if (fold) {
-                    const Fr *q = src.p[f] + 4 * b;
-                    const Fr a0 = load_fr(q), a1 = load_fr(q + 1), a2 = load_fr(q + 2), a3 = load_fr(q + 3);
-                    lo = a0 + r * (a1 - a0);
-                    hi = a2 + r * (a3 - a2);
-                    if (k == 0 && desc.writer[f] == begin + j) {
-                        Fr *d = dst.p[f] + 2 * b;
-                        store_fr(d, lo);
-                        store_fr(d + 1, hi);
-                    }
-                } else {
-                    const Fr *q = src.p[f] + 2 * b;
-                    lo = load_fr(q);
-                    hi = load_fr(q + 1);
+        auto factor = [&](int j) {
+            const int f = desc.indices[begin + j];
+            Fr lo, hi;
+            if (fold) {
+                const Fr *q = src.p[f] + 4 * b;
+                const Fr a0 = load_fr(q), a1 = load_fr(q + 1), a2 = load_fr(q + 2), a3 = load_fr(q + 3);
+                lo = a0 + r * (a1 - a0);
+                hi = a2 + r * (a3 - a2);
+                if (k == 0 && desc.writer[f] == begin + j) {
+                    Fr *d = dst.p[f] + 2 * b;
+                    store_fr(d, lo);
+                    store_fr(d + 1, hi);
                 }
-                slot_step(X, v, lo, hi, j, m, k);
+            } else {
+                const Fr *q = src.p[f] + 2 * b;
+                lo = load_fr(q);
+                hi = load_fr(q + 1);
             }
+            slot_step(X, v, lo, hi, j, m, k);
+        };
+        if constexpr (MAXM > 0) {
+#pragma unroll
+            for (int j = 0; j < MAXM; j++)
+                if (j < m) factor(j);
+        } else {
+            for (int j = 0; j < m; j++) factor(j);
         }
     }
     Fr a = acc_reduce(X);
@@ -369,21 +304,6 @@ __device__ void finalize_from_sums(const SumcheckDesc &desc, const Fr *sums, con
         a = warp_sum(a);
         if (lane == 0) out[x] = from_mont(a);
     }
-}
-
-__global__ void k_sumcheck_finalize(SumcheckDesc desc, const Fr *partials, int blocks, const Fr *weights,
-                                    int degree, Fr *out) {
-    extern __shared__ Fr sums[];
-    const int S = desc.slot_count;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
-    for (int s = warp; s < S; s += warps) {
-        Fr a = Fr::zero();
-        for (int b = lane; b < blocks; b += 32) a = a + partials[size_t(s) * blocks + b];
-        a = warp_sum(a);
-        if (lane == 0) sums[s] = a;
-    }
-    __syncthreads();
-    finalize_from_sums(desc, sums, weights, degree, out);
 }
 
 // A round of at most kSmallPairs pairs in one block, finalize included (the
@@ -568,14 +488,6 @@ static void release_state(HpCudaContext *ctx, HpCudaSumCheckProverState *s) {
     s->fold_a = s->fold_b = s->weights = s->partials = nullptr;
 }
 
-static int round_block_size(const SumcheckDesc &d, size_t *smem_out) {
-    size_t per_thread = size_t(2 * d.factor_count + d.max_arity + d.slot_count) * sizeof(Fr);
-    int T = 256;
-    while (T > 32 && per_thread * T > 200 * 1024) T /= 2;
-    if (per_thread * T > 200 * 1024) fail(HP_CUDA_STATUS_NOT_IMPLEMENTED);
-    *smem_out = per_thread * T;
-    return T;
-}
 
 }  // namespace hp
 
@@ -643,8 +555,6 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_create(
             size_t fcount = std::max(factor_count, size_t(1));
             s->fold_a = ctx->scratch(fcount * a_len * sizeof(Fr));
             s->fold_b = ctx->scratch(fcount * b_len * sizeof(Fr));
-            size_t smem;
-            hp::round_block_size(d, &smem);
         } catch (...) {
             hp::release_state(ctx, s);
             delete s;
@@ -690,32 +600,42 @@ static void enqueue_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, cons
         dst.p[f] = const_cast<Fr *>(state_table(s, dst_which, f));
         rd.p[f] = fold ? dst.p[f] : src.p[f];
     }
+    // the per-pair kernels take arity <= 8 and at most 48 slots (per-thread
+    // slot tables); the (slot, pair) kernel takes any shape with products
     const bool regs = d.max_arity <= 8 && d.slot_count <= kMaxSlotsV2;
+    const bool small = regs && pairs <= size_t(kSmallPairs);
     bool all_written = true;
     for (int f = 0; f < d.factor_count; f++) all_written = all_written && d.writer[f] != kNoWriter;
-    const bool slots_ok = d.max_arity <= 8 && d.product_count > 0;
-    const bool wide = slots_ok && (all_written || !fold) && pairs >= wide_min_pairs() && pairs <= wide_max_pairs();
-    const bool big = slots_ok && pairs > wide_max_pairs() && big_slot_rounds();
-    if (wide || big) {
+    bool use_slots = false, separate_fold = false;
+    if (d.product_count > 0 && !small) {
+        if (pairs > wide_max_pairs()) {
+            use_slots = big_slot_rounds() || !regs;
+            separate_fold = true;
+        } else if (pairs >= wide_min_pairs() || !regs) {
+            use_slots = true;
+            separate_fold = !all_written;  // the fused fold stores only factors some product reads
+        }
+    }
+    if (use_slots) {
         int tok = ctx->prof_begin("sumcheck_round", st);
         const size_t tiles = (pairs + kWideThreads - 1) / kWideThreads;
         int bps = int(std::min(tiles, size_t(1) << 20));
         FrPtrList tables = src;
         bool fused_fold = fold;
-        if (big) {
-            // fold every table first, then one pass over the folded tables;
-            // about two waves of blocks over the GPU in all
-            if (fold) {
-                int log_half = 0;
-                while ((size_t(1) << log_half) < 2 * pairs) log_half++;
-                const size_t total = size_t(d.factor_count) << log_half;
-                const size_t sms = size_t(ctx->sm_count > 0 ? ctx->sm_count : 152);
-                const unsigned fgrid = unsigned(std::min<size_t>((total + 255) / 256, sms * 8));
-                k_sumcheck_fold<<<fgrid, 256, 0, st>>>(src, dst, d.factor_count, log_half, r);
-                check_launch();
-                tables = rd;
-                fused_fold = false;
-            }
+        if (fold && separate_fold) {
+            // fold every table first, then one pass over the folded tables
+            int log_half = 0;
+            while ((size_t(1) << log_half) < 2 * pairs) log_half++;
+            const size_t total = size_t(d.factor_count) << log_half;
+            const size_t sms = size_t(ctx->sm_count > 0 ? ctx->sm_count : 152);
+            const unsigned fgrid = unsigned(std::max<size_t>(1, std::min<size_t>((total + 255) / 256, sms * 8)));
+            k_sumcheck_fold<<<fgrid, 256, 0, st>>>(src, dst, d.factor_count, log_half, r);
+            check_launch();
+            tables = rd;
+            fused_fold = false;
+        }
+        if (pairs > wide_max_pairs()) {
+            // about big_blocks_per_sm() blocks per SM over all slots
             const size_t target = size_t(ctx->sm_count > 0 ? ctx->sm_count : 152) * big_blocks_per_sm();
             bps = int(std::max<size_t>(1, std::min(tiles, (target + d.slot_count - 1) / d.slot_count)));
         }
@@ -733,7 +653,8 @@ static void enqueue_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, cons
         if (d.max_arity <= 2) launch(k_sumcheck_round_wide<2>);
         else if (d.max_arity <= 4) launch(k_sumcheck_round_wide<4>);
         else if (d.max_arity <= 6) launch(k_sumcheck_round_wide<6>);
-        else launch(k_sumcheck_round_wide<8>);
+        else if (d.max_arity <= 8) launch(k_sumcheck_round_wide<8>);
+        else launch(k_sumcheck_round_wide<0>);  // any arity, loop not unrolled
         check_launch();
         ctx->prof_end(tok, st);
         return;
@@ -755,45 +676,26 @@ static void enqueue_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, cons
         ctx->prof_end(tok, st);
         return;
     }
-    unsigned grid;
+    if (!regs) fail(HP_CUDA_STATUS_NOT_IMPLEMENTED);  // unreachable: !regs implies products, hence slots
+    const unsigned grid = grid_for(ctx, pairs, kRoundThreads, HP_ROUND_BLOCKS_PER_SM);
     Scratch spill;
-    Fr *partials = nullptr;
+    Fr *partials = round_partials(ctx, s, size_t(grid) * d.slot_count * sizeof(Fr), spill, st);
     int tok = ctx->prof_begin("sumcheck_round", st);
-    if (regs) {
-        grid = grid_for(ctx, pairs, kRoundThreads, HP_ROUND_BLOCKS_PER_SM);
-        partials = round_partials(ctx, s, size_t(grid) * d.slot_count * sizeof(Fr), spill, st);
-        const size_t smem = size_t(d.slot_count) * kRoundThreads * sizeof(Fr);
-        auto launch = [&](auto kernel) {
-            // the kernel's own static shared memory counts against the same
-            // 48 KiB default, so opt in well before the dynamic size reaches it
-            if (smem > 32 * 1024)
-                check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-            kernel<<<grid, kRoundThreads, smem, st>>>(d, src, dst, rd, fold, r, pairs, partials,
-                                                      round_counter(s), state_weights(s),
-                                                      int(s->max_degree), out_dev);
-        };
-        if (d.max_arity <= 2) launch(k_sumcheck_round_regs<2>);
-        else if (d.max_arity <= 4) launch(k_sumcheck_round_regs<4>);
-        else if (d.max_arity <= 6) launch(k_sumcheck_round_regs<6>);
-        else launch(k_sumcheck_round_regs<8>);
-        check_launch();
-        ctx->prof_end(tok, st);
-        return;
-    } else {
-        size_t smem;
-        int T = round_block_size(d, &smem);
-        if (smem > 48 * 1024)
-            check_cuda(cudaFuncSetAttribute(k_sumcheck_round, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            int(smem)));
-        grid = grid_for(ctx, pairs, unsigned(T), 2);
-        partials = round_partials(ctx, s, size_t(grid) * d.slot_count * sizeof(Fr), spill, st);
-        k_sumcheck_round<<<grid, T, smem, st>>>(d, src, dst, fold, r, pairs, partials);
-        check_launch();
-    }
-    ctx->prof_end(tok, st);
-    k_sumcheck_finalize<<<1, 256, size_t(d.slot_count) * sizeof(Fr), st>>>(d, partials, int(grid),
-                                                           state_weights(s), int(s->max_degree), out_dev);
+    const size_t smem = size_t(d.slot_count) * kRoundThreads * sizeof(Fr);
+    auto launch = [&](auto kernel) {
+        // the kernel's own static shared memory counts against the same
+        // 48 KiB default, so opt in well before the dynamic size reaches it
+        if (smem > 32 * 1024)
+            check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        kernel<<<grid, kRoundThreads, smem, st>>>(d, src, dst, rd, fold, r, pairs, partials, round_counter(s),
+                                                  state_weights(s), int(s->max_degree), out_dev);
+    };
+    if (d.max_arity <= 2) launch(k_sumcheck_round_regs<2>);
+    else if (d.max_arity <= 4) launch(k_sumcheck_round_regs<4>);
+    else if (d.max_arity <= 6) launch(k_sumcheck_round_regs<6>);
+    else launch(k_sumcheck_round_regs<8>);
     check_launch();
+    ctx->prof_end(tok, st);
 }
 
 // Rounds of wide_min_pairs() .. wide_max_pairs() pairs use the (slot, pair)

@@ -10,7 +10,7 @@
 namespace hp {
 
 constexpr int kMaxProducts = 64;
-constexpr int kMaxIndices = 256;
+constexpr int kMaxIndices = 1024;
 constexpr int kMaxDegree = 64;
 constexpr int kMaxFactors = 32;  // distinct factor tables of one state
 
