@@ -582,6 +582,7 @@ static size_t wide_max_pairs();
 static size_t wide_min_pairs();
 static bool big_slot_rounds();
 static size_t big_blocks_per_sm();
+static int separate_fold_arity();
 
 // Enqueues one round of state s on stream st: fold with r (rounds > 1) and
 // message into out_dev (degree + 1 canonical Fr, device).  Scratch is ordered
@@ -613,7 +614,12 @@ static void enqueue_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, cons
             separate_fold = true;
         } else if (pairs >= wide_min_pairs() || !regs) {
             use_slots = true;
-            separate_fold = !all_written;  // the fused fold stores only factors some product reads
+            // the fused fold stores only factors some product reads; products
+            // of arity >= separate_fold_arity() (HP_SEPARATE_FOLD_ARITY,
+            // default 3) fold in a separate pass: one more launch, but each
+            // item's chain loses the 2m products of re-folding its factors
+            // (GB300, nv = 20: arity-4/5 middle rounds 56-60 -> 35-43 us)
+            separate_fold = !all_written || d.max_arity >= separate_fold_arity();
         }
     }
     if (use_slots) {
@@ -712,6 +718,10 @@ static size_t wide_max_pairs() {
 }
 static size_t wide_min_pairs() {
     static const size_t v = env_size("HP_WIDE_MIN_PAIRS", size_t(kSmallPairs) + 1);
+    return v;
+}
+static int separate_fold_arity() {
+    static const int v = int(env_size("HP_SEPARATE_FOLD_ARITY", 3));
     return v;
 }
 // Rounds above wide_max_pairs(): k_sumcheck_fold + the (slot, pair) kernel
