@@ -65,24 +65,52 @@ def parse():
     ap.add_argument("--num-vars", type=int, default=None,
                     help="default 20 (prove, commit, sumcheck); the batch workload's SRS has 22")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--msm-tuning", default=None, metavar="FILE",
+                    help="load an MSM tuning table (hp_cuda_v1_msm_tuning_load) before preparing the SRS")
+    ap.add_argument("--autotune", action="store_true",
+                    help="prove / commit / batch: run the MSM autotuner on the workload's MSM sizes before warm-up")
     return ap.parse_args()
 
 
 def window_bits(n: int) -> int:
-    """Window width the library picks for an n-point layer (msm.cu)."""
-    env = os.environ.get("HP_MSM_WINDOW_BITS")
-    if env and 4 <= int(env) <= 22:
-        return int(env)
-    best, best_cost = 4, float("inf")
-    for c in range(4, 21):
-        top_bits = 255 - c * (math.ceil(256 / c) - 1)
-        top_buckets = float(1 << (top_bits - 1)) if top_bits >= 2 else 1.0
-        if c > 4 and n / top_buckets > 2048.0:
-            continue
-        cost = math.ceil(256 / c) * 10.0 * n + 28.0 * (1 << (c - 1))
-        if cost < best_cost:
-            best, best_cost = c, cost
-    return best
+    """Window width the library uses for an n-point layer (size rule or tuned entry)."""
+    from hyperplonk_gb300 import tuning
+    return tuning.query(tuning.ALONE, n)[0]
+
+
+# MSM geometry of this run: the tuning file loaded and the autotuner's entries
+TUNING_INFO: dict = {}
+
+
+def load_tuning(args, local: int) -> None:
+    if args.msm_tuning:
+        import torch
+        from hyperplonk_gb300 import tuning
+        tuning.load(args.msm_tuning, device=torch.cuda.get_device_name(local))
+        TUNING_INFO["file"] = args.msm_tuning
+
+
+def autotune(args, be, params, alone_nvs, shared_nvs) -> None:
+    """--autotune: measure the geometry of the workload's MSM sizes (alone)
+    and of its shared launch of small MSMs, untimed, before the warm-up."""
+    if not args.autotune:
+        return
+    from hyperplonk_gb300 import tuning
+    t0 = time.perf_counter()
+    entries = tuning.autotune(be, params, sorted(set(alone_nvs)))
+    if shared_nvs:
+        entries += tuning.autotune(be, params, list(shared_nvs)[:64], mode=tuning.SHARED)
+    TUNING_INFO["autotune_s"] = round(time.perf_counter() - t0, 2)
+    TUNING_INFO["autotune"] = [
+        {"mode": "alone" if e.mode == tuning.ALONE else "shared", "size": e.size, "window_bits": e.window_bits,
+         "segment": e.segment, "chunk": e.chunk, "model_ms": round(e.model_ms, 4), "tuned_ms": round(e.tuned_ms, 4)}
+        for e in entries]
+
+
+def shared_mix(nvs) -> list:
+    """The sizes that run_msms puts into the shared launch: fewer than 2^22
+    (window, point) records."""
+    return [k for k in nvs if math.ceil(256 / window_bits(1 << k)) * (1 << k) < (1 << 22)]
 
 
 def accumulate_imad(n: int) -> int:
@@ -397,7 +425,8 @@ def common_fields(args, world, metric, value, unit, step_s, workload, config, e2
             "data": "synthetic: ChaCha20 fixture streams, device-generated testing SRS",
             "config": dict({"workload": workload, "l2": "256 MiB flush between steps; inputs > L2",
                             "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}, **config),
-            "e2e": e2e, "gpu_launches": int(nl), "clocks": clk}
+            "e2e": e2e, "gpu_launches": int(nl), "clocks": clk,
+            **({"msm_tuning": dict(TUNING_INFO)} if TUNING_INFO else {})}
 
 
 def run_sumcheck(args, world, rank, local, pg):
@@ -477,6 +506,7 @@ def run_batch(args, world, rank, local, pg):
     layers = s.srs_layers(nv_srs, 0)
     params = be.prepare_prover_param(nv_srs, layers)
     del layers
+    autotune(args, be, params, ks, shared_mix(ks))
     wl = workloads.BatchWorkload(be, params, ks, nvs)
     out = {}
 
@@ -616,6 +646,7 @@ def measured_peaks() -> dict:
 
 
 def run_gb300(args, world, rank, local, pg):
+    load_tuning(args, local)
     if args.workload == "sumcheck":
         return run_sumcheck(args, world, rank, local, pg)
     if args.workload == "batch":
@@ -633,6 +664,7 @@ def run_gb300(args, world, rank, local, pg):
         from hyperplonk_gb300 import _native
         params = be.prepare_prover_param(nv, layers)
         del layers
+        autotune(args, be, params, [nv], [])
         hv = np.empty(32 * n, dtype=np.uint8)
         s.check(s.lib.hp_cuda_v1_fixture_random_fr(0, 0, n, _native.buf(hv)), "fixture_random_fr")
         host = s.pinned(hv)
@@ -658,6 +690,8 @@ def run_gb300(args, world, rank, local, pg):
         sel, wit, perm, pub = snark.vanilla_fixture(nv, PROVE_SEED)
         pk = snark.preprocess(be, nv, min(16, n), sel, perm, layers, commit=False)
         del layers, sel, perm
+        opening = [nv - 1 - i for i in range(nv)]  # the batch opening's quotient MSMs
+        autotune(args, be, pk.pcs_param, [nv] + [k for k in opening if k >= 10], shared_mix(opening))
         pinned = [s.pinned(w) for w in wit]
         wit_host = [p.numpy() for p in pinned]
         resident = [be.mle_from_evaluations(nv, w) for w in wit_host]

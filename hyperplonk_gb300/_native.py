@@ -22,6 +22,13 @@ class Status(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("native_code", ctypes.c_int32)]
 
 
+class MsmTuning(ctypes.Structure):
+    """HpCudaMsmTuning (include/hp_cuda.h)."""
+    _fields_ = [("size", ctypes.c_uint64), ("mode", ctypes.c_uint32), ("window_bits", ctypes.c_uint32),
+                ("segment", ctypes.c_uint32), ("chunk", ctypes.c_uint32), ("model_ms", ctypes.c_double),
+                ("tuned_ms", ctypes.c_double)]
+
+
 # name -> argument types (all return Status)
 SIGNATURES: dict[str, list] = {
     "hp_cuda_v1_context_create": [ctypes.c_int32, c_voidpp],
@@ -70,6 +77,11 @@ SIGNATURES: dict[str, list] = {
     "hp_host_v1_merlin_free": [c_voidp],
     "hp_host_v1_keccak_f1600": [c_u8p],
     "hp_cuda_v1_sumcheck_prove_rounds": [c_voidp, c_voidp, c_voidp, c_size, c_u8p, c_u8p],
+    "hp_cuda_v1_msm_autotune": [c_voidp, c_voidp, c_sizep, c_size, ctypes.c_int32, ctypes.POINTER(MsmTuning)],
+    "hp_cuda_v1_msm_tuning_query": [ctypes.c_int32, c_size, ctypes.POINTER(ctypes.c_uint32)],
+    "hp_cuda_v1_msm_tuning_save": [ctypes.c_char_p],
+    "hp_cuda_v1_msm_tuning_load": [ctypes.c_char_p, ctypes.c_char_p],
+    "hp_cuda_v1_msm_tuning_clear": [],
 }
 
 _lib = None

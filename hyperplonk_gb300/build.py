@@ -37,7 +37,8 @@ def sources() -> list[pathlib.Path]:
 
 
 def _headers() -> list[pathlib.Path]:
-    return sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + sorted((ROOT / "include").glob("*.h"))
+    return (sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.inc"))
+            + sorted((ROOT / "include").glob("*.h")))
 
 
 def _stale(obj: pathlib.Path, src: pathlib.Path, headers: list[pathlib.Path]) -> bool:

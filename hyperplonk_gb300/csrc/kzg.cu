@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "host_ec.h"
+#include "kzg.cuh"
 #include "mle.cuh"
 #include "msm.cuh"
 #include "runtime.cuh"
@@ -28,15 +29,6 @@ using hp::fail;
 using hp::Fr;
 using hp::guard;
 using hp::require;
-
-struct HpCudaMultilinearKzgPreparedProverParam {
-    size_t num_vars = 0;
-    std::vector<hp::MsmLayer> layers;
-    std::vector<bool> uploaded;
-    // prefix layers for batched MSMs over the first n bases of layer k,
-    // keyed by (k, n), built on first use
-    std::map<std::pair<size_t, size_t>, hp::MsmLayer> prefixes;
-};
 
 namespace hp {
 
@@ -59,8 +51,7 @@ static const MsmLayer &ready_layer(const HpCudaMultilinearKzgPreparedProverParam
 // Independent MSMs, task i writing its partial rows at the running offset.
 // MSMs of >= 4 M (point, window) records fill the GPU alone: one msm_run
 // each, overlapped on worker streams; all smaller ones share one launch per
-// phase (msm_run_many) on another worker stream.  HP_MSM_MANY=0 runs every
-// MSM alone on the worker streams, HP_MSM_MANY=1 all of them together.
+// phase (msm_run_many) on another worker stream (msm_runs_alone).
 static void run_msms(HpCudaContext *ctx, std::vector<MsmTask> tasks, Xyzz *parts) {
     if (tasks.empty()) return;
     size_t o = 0;
@@ -68,11 +59,9 @@ static void run_msms(HpCudaContext *ctx, std::vector<MsmTask> tasks, Xyzz *parts
         t.out_row = o;
         o += size_t(msm_shape(*t.layer).partials);
     }
-    const char *env = std::getenv("HP_MSM_MANY");
-    const size_t big_records = env && env[0] == '0' ? 0 : env && env[0] == '1' ? SIZE_MAX : (size_t(1) << 22);
     std::vector<MsmTask> big, small;
     for (const auto &t : tasks)
-        (size_t(t.layer->windows) * t.n >= big_records ? big : small).push_back(t);
+        (msm_runs_alone(size_t(t.layer->windows) * t.n) ? big : small).push_back(t);
     std::stable_sort(big.begin(), big.end(), [](const MsmTask &a, const MsmTask &b) { return a.n > b.n; });
     const size_t lanes = big.size() + (small.empty() ? 0 : 1);
     const int k = int(std::min<size_t>(lanes, HpCudaContext::kWorkers));

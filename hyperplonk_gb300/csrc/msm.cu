@@ -38,15 +38,28 @@ int msm_window_bits(size_t n) {
         int c = std::atoi(env);
         if (c >= 4 && c <= 22) return c;
     }
+    const MsmTuning t = msm_tuning_alone(n);
+    if (t.c && msm_window_fits(n, t.c)) return t.c;
+    return msm_window_bits_model(n);
+}
+
+bool msm_window_fits(size_t n, int c) {
+    if (c < 4 || c > 22) return false;
+    // records are (window * n + point) in 31 bits
+    if (size_t(msm_windows(c)) * n >= (size_t(1) << 31)) return false;
+    // The top window holds only 255 - c(W-1) bits of a scalar (< 2^255): its
+    // n records fall into that many bits' worth of buckets.  Skip widths that
+    // would pile more than 2048 records onto one bucket.
+    const int top_bits = 255 - c * (msm_windows(c) - 1);
+    const double top_buckets = top_bits >= 2 ? double(size_t(1) << (top_bits - 1)) : 1.0;
+    return c == 4 || double(n) / top_buckets <= 2048.0;
+}
+
+int msm_window_bits_model(size_t n) {
     int best = 4;
     double best_cost = 1e300;
     for (int c = 4; c <= 20; c++) {
-        // The top window holds only 255 - c(W-1) bits of a scalar (< 2^255):
-        // its n records fall into that many bits' worth of buckets.  Skip
-        // widths that would pile more than 2048 records onto one bucket.
-        const int top_bits = 255 - c * (msm_windows(c) - 1);
-        const double top_buckets = top_bits >= 2 ? double(size_t(1) << (top_bits - 1)) : 1.0;
-        if (c > 4 && double(n) / top_buckets > 2048.0) continue;
+        if (!msm_window_fits(n, c)) continue;
         double cost = double(msm_windows(c)) * 10.0 * double(n) + 28.0 * double(size_t(1) << (c - 1));
         if (cost < best_cost) {
             best_cost = cost;
@@ -56,15 +69,28 @@ int msm_window_bits(size_t n) {
     return best;
 }
 
-MsmShape msm_shape(const MsmLayer &layer) {
-    MsmShape s;
-    s.buckets = size_t(1) << (layer.c - 1);
+uint32_t msm_default_seg(int c) {
     // 16-bucket segments from 2^17 buckets up; shorter below, because a
     // segment is a chain of 2 seg dependent additions and smaller MSMs are
     // latency-bound (measured: 2^15 buckets seg 4 1.29 ms vs seg 8 1.42 ms
     // and seg 16 1.70 ms; 2^11 buckets seg 1 best; 2^19 seg 16 9.20 ms vs
     // seg 8 9.56 ms and seg 32 9.47 ms)
-    s.seg = std::min<size_t>(16, std::max<size_t>(1, s.buckets >> 13));
+    const size_t buckets = size_t(1) << (c - 1);
+    size_t seg = std::min<size_t>(16, std::max<size_t>(1, buckets >> 13));
+    // the subset reduction takes at most msm_max_segments() segments
+    while (buckets / seg > msm_max_segments()) seg *= 2;
+    return uint32_t(seg);
+}
+
+static bool seg_fits(size_t seg, size_t buckets) {
+    return seg >= 1 && seg <= 64 && (seg & (seg - 1)) == 0 && seg <= buckets && buckets / seg <= msm_max_segments();
+}
+
+MsmShape msm_shape(const MsmLayer &layer) {
+    MsmShape s;
+    s.buckets = size_t(1) << (layer.c - 1);
+    s.seg = msm_default_seg(layer.c);
+    if (layer.seg && seg_fits(layer.seg, s.buckets)) s.seg = layer.seg;
     // tuning override: HP_MSM_SEG=s (power of two, 1..64)
     if (const char *env = std::getenv("HP_MSM_SEG")) {
         const long v = std::atol(env);
@@ -262,10 +288,18 @@ static void msm_finish_layer(HpCudaContext *ctx, MsmLayer &layer) {
     layer.minus_d = d;
 }
 
+void msm_apply_tuning(MsmLayer &layer) {
+    // a tuned segment and chunk belong to the window width they were measured with
+    const MsmTuning t = msm_tuning_alone(layer.n);
+    layer.seg = t.c == layer.c ? t.seg : 0;
+    layer.chunk = t.c == layer.c ? t.chunk : 0;
+}
+
 bool msm_prepare_layer(HpCudaContext *ctx, MsmLayer &layer, const uint8_t *packets, size_t n) {
     layer.n = n;
     layer.c = msm_window_bits(n);
     layer.windows = msm_windows(layer.c);
+    msm_apply_tuning(layer);
     layer.bases = static_cast<Affine *>(ctx->scratch(size_t(layer.windows) * n * sizeof(Affine)));
     Scratch raw(ctx, n * 97);
     check_cuda(cudaMemcpyAsync(raw.ptr, packets, n * 97, cudaMemcpyHostToDevice, ctx->stream));
@@ -279,15 +313,47 @@ bool msm_prepare_layer(HpCudaContext *ctx, MsmLayer &layer, const uint8_t *packe
     return true;
 }
 
-void msm_prepare_prefix(HpCudaContext *ctx, MsmLayer &prefix, const MsmLayer &source, size_t n) {
-    require(n >= 1 && n <= source.n);
+void msm_prepare_prefix_c(HpCudaContext *ctx, MsmLayer &prefix, const MsmLayer &source, size_t n, int c) {
+    require(n >= 1 && n <= source.n && c >= 4 && c <= 22);
     prefix.n = n;
-    prefix.c = msm_window_bits(n);
-    prefix.windows = msm_windows(prefix.c);
+    prefix.c = c;
+    prefix.windows = msm_windows(c);
+    // records are (window * n + point) in 31 bits
+    require(size_t(prefix.windows) * n < (size_t(1) << 31));
+    prefix.seg = 0;
+    prefix.chunk = 0;
     prefix.bases = static_cast<Affine *>(ctx->scratch(size_t(prefix.windows) * n * sizeof(Affine)));
     check_cuda(cudaMemcpyAsync(prefix.bases, source.bases, n * sizeof(Affine), cudaMemcpyDeviceToDevice,
                                ctx->stream));
     msm_finish_layer(ctx, prefix);
+}
+
+void msm_prepare_prefix(HpCudaContext *ctx, MsmLayer &prefix, const MsmLayer &source, size_t n) {
+    msm_prepare_prefix_c(ctx, prefix, source, n, msm_window_bits(n));
+    msm_apply_tuning(prefix);
+}
+
+void msm_retune_layer(HpCudaContext *ctx, MsmLayer &layer) {
+    const int c = msm_window_bits(layer.n);
+    if (c != layer.c) {
+        MsmLayer fresh;
+        try {
+            msm_prepare_prefix_c(ctx, fresh, layer, layer.n, c);
+        } catch (...) {
+            msm_release_layer(ctx, fresh);
+            throw;
+        }
+        msm_release_layer(ctx, layer);
+        layer = fresh;
+    }
+    msm_apply_tuning(layer);
+}
+
+void msm_random_scalars(HpCudaContext *ctx, Fr *out, size_t n, uint64_t seed, cudaStream_t stream) {
+    k_msm_delta<<<grid_for(ctx, n, 256), 256, 0, stream>>>(out, n, seed);
+    check_launch();
+    k_msm_to_mont<<<grid_for(ctx, n, 256), 256, 0, stream>>>(out, n);
+    check_launch();
 }
 
 void msm_release_layer(HpCudaContext *ctx, MsmLayer &layer) {
@@ -460,8 +526,13 @@ struct AccumulateGeometry {
     unsigned grid;    // blocks of 128 threads
 };
 
-AccumulateGeometry accumulate_geometry(size_t records) {
-    size_t L = records < (size_t(1) << 21) ? kSmallChunkRecords : kChunkRecords;
+uint32_t msm_default_chunk(size_t records) {
+    return records < (size_t(1) << 21) ? kSmallChunkRecords : kChunkRecords;
+}
+
+// `tuned`: a chunk length from the tuning table, 0 for the size rule
+AccumulateGeometry accumulate_geometry(size_t records, uint32_t tuned) {
+    size_t L = tuned >= 2 && tuned <= 1024 ? tuned : msm_default_chunk(records);
     // tuning override: HP_ACC_CHUNK=L (2 <= L <= 1024)
     if (const char *env = std::getenv("HP_ACC_CHUNK")) {
         const long v = std::atol(env);
@@ -601,6 +672,9 @@ constexpr int kSubsetThreads = 128;
 constexpr int kSubsetPerThread = 8;
 constexpr int kSubsetPerBlock = kSubsetThreads * kSubsetPerThread;
 
+// k_msm_rows sums at most 64 subset blocks per row
+size_t msm_max_segments() { return size_t(64) * kSubsetPerBlock; }
+
 // Blocks of T threads (a power of two <= kSubsetThreads), `per` elements per
 // thread: T * per = kSubsetPerBlock when there are several chunks; a single
 // chunk of few elements takes fewer threads and elements per thread (the
@@ -673,7 +747,7 @@ void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz 
     k_msm_scatter<<<grid_for(ctx, n, 256), 256, 0, st>>>(scalars, layer.delta, n, layer.n, layer.c, layer.windows,
                                                         cursor.as<uint32_t>(), recs.as<uint32_t>());
     check_launch();
-    const AccumulateGeometry geo = accumulate_geometry(records);
+    const AccumulateGeometry geo = accumulate_geometry(records, layer.chunk);
     Scratch pieces(ctx, std::max<size_t>(2 * geo.chunks, 1) * sizeof(Xyzz), st);
     int tok = ctx->prof_begin("msm_accumulate", st);
     k_msm_accumulate<<<geo.grid, 128, 0, st>>>(OneTable{layer.bases}, offsets.as<uint32_t>(), recs.as<uint32_t>(),
@@ -830,7 +904,8 @@ __global__ void k_msmm_rows(const MsmInst *in, int count, const Xyzz *stage, Xyz
 }
 
 // One group: at most kMaxInstances instances, all of it resident at once.
-static void msm_run_group(HpCudaContext *ctx, const MsmTask *tasks, size_t count, Xyzz *out_rows, cudaStream_t st) {
+static void msm_run_group(HpCudaContext *ctx, const MsmTask *tasks, size_t count, Xyzz *out_rows, cudaStream_t st,
+                          uint32_t chunk) {
     std::vector<MsmInst> in(count);
     std::vector<uint32_t> bucket_base(count);
     std::vector<const Affine *> tables(count);
@@ -890,7 +965,10 @@ static void msm_run_group(HpCudaContext *ctx, const MsmTask *tasks, size_t count
     k_msmm_scatter<<<grid_for(ctx, points, 256), 256, 0, st>>>(inst, cnt, uint32_t(points), cursor.as<uint32_t>(),
                                                               recs.as<uint32_t>());
     check_launch();
-    const AccumulateGeometry geo = accumulate_geometry(records);
+    // a launch of one MSM takes that layer's tuned chunk, a shared one the
+    // entry for its record count
+    if (!chunk && count == 1) chunk = tasks[0].layer->chunk;
+    const AccumulateGeometry geo = accumulate_geometry(records, chunk ? chunk : msm_tuning_many_chunk(records));
     Scratch pieces(ctx, std::max<size_t>(2 * geo.chunks, 1) * sizeof(Xyzz), st);
     k_msm_accumulate<<<geo.grid, 128, 0, st>>>(ManyTables{dbase.as<uint32_t>(), dtab.as<const Affine *>(), cnt},
                                                offsets.as<uint32_t>(), recs.as<uint32_t>(), uint32_t(B), geo.chunk,
@@ -911,20 +989,32 @@ static void msm_run_group(HpCudaContext *ctx, const MsmTask *tasks, size_t count
     check_launch();
 }
 
-void msm_run_many(HpCudaContext *ctx, const MsmTask *tasks, size_t count, Xyzz *out_rows, cudaStream_t stream) {
+static_assert(kMsmManyMaxInstances == size_t(kMaxInstances), "one instance table per launch");
+
+uint32_t msm_effective_chunk(size_t records, uint32_t tuned) { return accumulate_geometry(records, tuned).chunk; }
+
+bool msm_runs_alone(size_t records) {
+    const char *env = std::getenv("HP_MSM_MANY");
+    if (env && env[0] == '0') return true;
+    if (env && env[0] == '1') return false;
+    return records >= (size_t(1) << 22);
+}
+
+void msm_run_many(HpCudaContext *ctx, const MsmTask *tasks, size_t count, Xyzz *out_rows, cudaStream_t stream,
+                  uint32_t chunk) {
     const cudaStream_t st = stream ? stream : ctx->stream;
     // groups of <= kMaxInstances instances and <= 2^27 records (bounded scratch)
     size_t i = 0;
     int whole = ctx->prof_begin("msm_many", st);
     while (i < count) {
         size_t j = i, records = 0;
-        while (j < count && j - i < size_t(kMaxInstances)) {
+        while (j < count && j - i < kMsmManyMaxInstances) {
             const size_t r = size_t(tasks[j].layer->windows) * tasks[j].n;
-            if (j > i && records + r > (size_t(1) << 27)) break;
+            if (j > i && records + r > kMsmManyMaxRecords) break;
             records += r;
             j++;
         }
-        msm_run_group(ctx, tasks + i, j - i, out_rows, st);
+        msm_run_group(ctx, tasks + i, j - i, out_rows, st, chunk);
         i = j;
     }
     ctx->prof_end(whole, st);

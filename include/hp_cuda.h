@@ -321,6 +321,52 @@ HpCudaStatus hp_cuda_v1_kernel_launch_count(uint64_t *out);
  * work or timing events with the backend's. */
 HpCudaStatus hp_cuda_v1_context_stream(HpCudaContext *ctx, void **out_stream);
 
+/* MSM autotuner (no counterpart in the reference, whose MSM geometry is fixed
+ * in backend/src/ascend910b3/native/msm*.cpp).  The MSM's window width,
+ * reduction segment length and accumulation chunk length come from a
+ * process-wide tuning table, else from a size rule; the table holds measured
+ * entries keyed by ceil(log2 points) for an MSM run alone (mode 0) and by
+ * ceil(log2 records) for a launch shared by many MSMs (mode 1).  Tuning never
+ * changes a result: every candidate's point is checked against the size
+ * rule's (InvalidState on a mismatch, table unchanged).
+ *
+ * msm_autotune: mode 0 measures an MSM of 2^num_vars[i] points (the first
+ * bases of params' layer 0) for each i, records the fastest geometry, then
+ * re-prepares params' layers accordingly (window tables rebuilt where the
+ * width changed) and drops its cached prefix layers; out gets count entries.
+ * Mode 1 measures one shared launch over all count sizes (<= 64, prefix
+ * layers of layer 0 as batch_msm builds them) and records its chunk length;
+ * out gets one entry.  InvalidState when layer 0 is not uploaded or a
+ * geometry override (HP_MSM_WINDOW_BITS, HP_MSM_SEG, HP_ACC_CHUNK) is set in
+ * the environment.  Takes seconds per size (median device time of several
+ * runs per candidate).
+ *
+ * msm_tuning_query: the geometry a new layer of `size` points (mode 0:
+ * out3 = window bits, segment, chunk) or a shared launch of `size` records
+ * (mode 1: out3 = 0, 0, chunk) would use now; needs no device.
+ * msm_tuning_save / msm_tuning_load: the table as a text file; load merges
+ * its entries and, when `device` is non-null, rejects a file measured on
+ * another device name (InvalidParameters).  At the first lookup the table
+ * takes the library's built-in entries measured on an NVIDIA GB300 (when the
+ * current device has that name), then the file named by the environment
+ * variable HP_CUDA_MSM_TUNING over them; HP_CUDA_MSM_TUNING=off keeps it
+ * empty.  msm_tuning_clear: empties the table (the size rules apply again). */
+typedef struct HpCudaMsmTuning {
+    uint64_t size;        /* points (mode 0) or records of the launch (mode 1) */
+    uint32_t mode;        /* 0 alone, 1 shared launch */
+    uint32_t window_bits; /* mode 0 */
+    uint32_t segment;     /* mode 0 */
+    uint32_t chunk;
+    double model_ms;      /* median device time with the size rule's geometry */
+    double tuned_ms;      /* median device time with the chosen geometry */
+} HpCudaMsmTuning;
+HpCudaStatus hp_cuda_v1_msm_autotune(HpCudaContext *ctx, HpCudaMultilinearKzgPreparedProverParam *params,
+                                     const size_t *num_vars, size_t count, int32_t mode, HpCudaMsmTuning *out);
+HpCudaStatus hp_cuda_v1_msm_tuning_query(int32_t mode, size_t size, uint32_t *out3);
+HpCudaStatus hp_cuda_v1_msm_tuning_save(const char *path);
+HpCudaStatus hp_cuda_v1_msm_tuning_load(const char *path, const char *device);
+HpCudaStatus hp_cuda_v1_msm_tuning_clear(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -549,6 +549,19 @@ public:
         return out;
     }
 
+    /* ---- MSM autotuner (no counterpart in the reference; see hp_cuda.h) ----
+     * mode 0: one entry per size, and pp's layers are re-prepared with them;
+     * mode 1: one entry for a launch shared by all the sizes (<= 64). */
+    std::vector<HpCudaMsmTuning> msm_autotune(const PreparedProverParam &pp, const std::vector<size_t> &num_vars,
+                                              int mode = 0) const {
+        own(pp);
+        if (num_vars.empty()) return {};
+        std::vector<HpCudaMsmTuning> out(mode == 0 ? num_vars.size() : 1);
+        check(hp_cuda_v1_msm_autotune(ctx_->raw, pp.p_->raw, num_vars.data(), num_vars.size(), mode, out.data()),
+              "msm_autotune");
+        return out;
+    }
+
 private:
     Mle wrap(HpCudaDeviceAddress a, size_t nv) const { return Mle(std::make_shared<detail::Buffer>(ctx_, a), nv); }
     void own(const Mle &m) const {
@@ -568,5 +581,25 @@ private:
     }
     std::shared_ptr<detail::Context> ctx_;
 };
+
+/* The process-wide MSM tuning table (hp_cuda_v1_msm_tuning_*). */
+namespace tuning {
+struct Geometry {
+    uint32_t window_bits, segment, chunk;
+};
+/* mode 0: the geometry a new layer of `size` points takes; mode 1: the chunk
+ * (window_bits = segment = 0) of a shared launch of `size` records. */
+inline Geometry query(int mode, size_t size) {
+    uint32_t g[3] = {0, 0, 0};
+    check(hp_cuda_v1_msm_tuning_query(mode, size, g), "msm_tuning_query");
+    return Geometry{g[0], g[1], g[2]};
+}
+inline void save(const std::string &path) { check(hp_cuda_v1_msm_tuning_save(path.c_str()), "msm_tuning_save"); }
+/* device: reject a file measured on another device name; empty: accept any. */
+inline void load(const std::string &path, const std::string &device = std::string()) {
+    check(hp_cuda_v1_msm_tuning_load(path.c_str(), device.empty() ? nullptr : device.c_str()), "msm_tuning_load");
+}
+inline void clear() { check(hp_cuda_v1_msm_tuning_clear(), "msm_tuning_clear"); }
+}  // namespace tuning
 
 }  // namespace hp_cuda

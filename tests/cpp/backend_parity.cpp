@@ -786,6 +786,31 @@ static void sumcheck_empty_whole_polynomial_messages_and_call_order_contract(con
     CHECK(be.download(kat) == (Table{fr::from_u64(2), fr::from_u64(3), fr::from_u64(5), fr::from_u64(7)}));
 }
 
+// Not a port: the MSM autotuner (an extension of this backend) measures and
+// re-prepares the layers without changing any commitment.
+static void msm_autotune_keeps_commitments(const CudaBackend &be) {
+    tuning::clear();
+    const size_t pv = 8;
+    std::vector<std::vector<uint8_t>> affine;
+    const auto layers = srs_layers(pv, 0xA7, &affine);
+    const PreparedProverParam pp = be.prepare_prover_param(pv, layers);
+    const auto entries = be.msm_autotune(pp, {6, 8});
+    CHECK(entries.size() == 2);
+    for (const auto &e : entries) {
+        const tuning::Geometry g = tuning::query(0, size_t(e.size));
+        CHECK(e.mode == 0 && g.window_bits == e.window_bits && g.segment == e.segment && g.chunk == e.chunk);
+        CHECK(e.tuned_ms > 0 && e.tuned_ms <= e.model_ms);
+    }
+    const auto shared = be.msm_autotune(pp, {3, 5, 6, 7}, 1);
+    CHECK(shared.size() == 1 && shared[0].mode == 1 && tuning::query(1, size_t(shared[0].size)).chunk == shared[0].chunk);
+    for (size_t nv = 0; nv <= pv; nv++) {
+        const Table values = field_table(nv, 0xA8 ^ nv);
+        CHECK(be.commit(pp, be.mle_from_evaluations(nv, values)) == independent_commitment(affine, pv, nv, values));
+    }
+    EXPECT_INVALID_PARAMETERS(be.msm_autotune(pp, {9}));  // more points than layer 0 holds
+    tuning::clear();
+}
+
 // ---------------------------------------------------------------------------
 
 int main() {
@@ -825,6 +850,7 @@ int main() {
         {"sumcheck_repeated_factors_mixed_arity_max_degree_34_are_independent",
          sumcheck_repeated_factors_mixed_arity_max_degree_34_are_independent},
         {"sumcheck_rejects_zero_dimension_and_zero_degree", sumcheck_rejects_zero_dimension_and_zero_degree},
+        {"msm_autotune_keeps_commitments", msm_autotune_keeps_commitments},
         {"sumcheck_empty_whole_polynomial_messages_and_call_order_contract",
          sumcheck_empty_whole_polynomial_messages_and_call_order_contract},
     };
