@@ -49,9 +49,11 @@ static const MsmLayer &ready_layer(const HpCudaMultilinearKzgPreparedProverParam
 
 // Download `total` XYZZ partials and finish each MSM into a packet.
 // Independent MSMs, task i writing its partial rows at the running offset.
-// MSMs of >= 4 M (point, window) records fill the GPU alone: one msm_run
-// each, overlapped on worker streams; all smaller ones share one launch per
-// phase (msm_run_many) on another worker stream (msm_runs_alone).
+// MSMs whose scalars are all 0 or 1 are sums of bases (msm_run_binary, one
+// worker stream for all of them).  Of the others, MSMs of >= 4 M (point,
+// window) records fill the GPU alone: one msm_run each, overlapped on worker
+// streams; all smaller ones share one launch per phase (msm_run_many) on
+// another worker stream (msm_runs_alone).
 static void run_msms(HpCudaContext *ctx, std::vector<MsmTask> tasks, Xyzz *parts) {
     if (tasks.empty()) return;
     size_t o = 0;
@@ -59,17 +61,32 @@ static void run_msms(HpCudaContext *ctx, std::vector<MsmTask> tasks, Xyzz *parts
         t.out_row = o;
         o += size_t(msm_shape(*t.layer).partials);
     }
-    std::vector<MsmTask> big, small;
-    for (const auto &t : tasks)
-        (msm_runs_alone(size_t(t.layer->windows) * t.n) ? big : small).push_back(t);
+    const std::vector<char> binary = msm_binary_tasks(ctx, tasks.data(), tasks.size());
+    std::vector<MsmTask> big, small, sums;
+    for (size_t i = 0; i < tasks.size(); i++) {
+        const MsmTask &t = tasks[i];
+        (binary[i] ? sums : msm_runs_alone(size_t(t.layer->windows) * t.n) ? big : small).push_back(t);
+    }
     std::stable_sort(big.begin(), big.end(), [](const MsmTask &a, const MsmTask &b) { return a.n > b.n; });
-    const size_t lanes = big.size() + (small.empty() ? 0 : 1);
+    const size_t lanes = big.size() + (small.empty() ? 0 : 1) + (sums.empty() ? 0 : 1);
     const int k = int(std::min<size_t>(lanes, HpCudaContext::kWorkers));
     ctx->fork(k);
     size_t w = 0;
+    if (!sums.empty()) {
+        const cudaStream_t st = ctx->workers[w++ % size_t(k)];
+        for (const auto &t : sums) msm_run_binary(ctx, *t.layer, t.scalars, t.n, parts + t.out_row, st);
+    }
     if (!small.empty()) msm_run_many(ctx, small.data(), small.size(), parts, ctx->workers[w++ % size_t(k)]);
     for (const auto &t : big) msm_run(ctx, *t.layer, t.scalars, parts + t.out_row, ctx->workers[w++ % size_t(k)], t.n);
     ctx->join(k);
+}
+
+// One MSM over the whole layer on the context stream: a sum of bases when
+// every scalar is 0 or 1, else msm_run.
+static void run_one_msm(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz *parts) {
+    const MsmTask task{&layer, scalars, layer.n, 0};
+    if (msm_binary_tasks(ctx, &task, 1)[0]) msm_run_binary(ctx, layer, scalars, layer.n, parts);
+    else msm_run(ctx, layer, scalars, parts);
 }
 
 static void finish_msms(HpCudaContext *ctx, const Xyzz *dev, const std::vector<const MsmLayer *> &layers,
@@ -154,7 +171,7 @@ extern "C" HpCudaStatus hp_cuda_v1_multilinear_kzg_commit(
         const hp::MsmLayer &layer = hp::ready_layer(params, params->num_vars - num_vars);
         hp::MsmShape sh = hp::msm_shape(layer);
         hp::Scratch parts(ctx, size_t(sh.partials) * sizeof(hp::Xyzz));
-        hp::msm_run(ctx, layer, scalars, parts.as<hp::Xyzz>());
+        hp::run_one_msm(ctx, layer, scalars, parts.as<hp::Xyzz>());
         hp::finish_msms(ctx, parts.as<hp::Xyzz>(), {&layer}, out_commitment);
     });
 }
@@ -265,7 +282,7 @@ extern "C" HpCudaStatus hp_cuda_v1_msm(HpCudaContext *ctx, const uint8_t *bases,
         if (ctx->sync_flags() & hp::kFlagNonCanonical) fail(HP_CUDA_STATUS_INVALID_PARAMETERS);
         hp::MsmShape sh = hp::msm_shape(layer);
         hp::Scratch parts(ctx, size_t(sh.partials) * sizeof(hp::Xyzz));
-        hp::msm_run(ctx, layer, s.as<Fr>(), parts.as<hp::Xyzz>());
+        hp::run_one_msm(ctx, layer, s.as<Fr>(), parts.as<hp::Xyzz>());
         hp::finish_msms(ctx, parts.as<hp::Xyzz>(), {&layer}, out_point);
     });
 }

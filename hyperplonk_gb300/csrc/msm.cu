@@ -284,6 +284,11 @@ static void msm_finish_layer(HpCudaContext *ctx, MsmLayer &layer) {
                                cudaMemcpyDeviceToHost, ctx->stream));
     ctx->sync();
     host::Xyzz64 d = msm_combine_host(sh, hp_parts.data());
+    // D on the device for the binary path (same byte layout as Xyzz), -D for the host finish
+    layer.d_sum = static_cast<Xyzz *>(ctx->scratch(sizeof(Xyzz)));
+    static_assert(sizeof(host::Xyzz64) == sizeof(Xyzz), "host and device XYZZ share a layout");
+    check_cuda(cudaMemcpyAsync(layer.d_sum, &d, sizeof(Xyzz), cudaMemcpyHostToDevice, ctx->stream));
+    ctx->sync();
     d.y = host::fq_sub(host::Fq64{{0, 0, 0, 0, 0, 0}}, d.y);
     layer.minus_d = d;
 }
@@ -359,8 +364,10 @@ void msm_random_scalars(HpCudaContext *ctx, Fr *out, size_t n, uint64_t seed, cu
 void msm_release_layer(HpCudaContext *ctx, MsmLayer &layer) {
     if (layer.bases) ctx->scratch_free(layer.bases);
     if (layer.delta) ctx->scratch_free(layer.delta);
+    if (layer.d_sum) ctx->scratch_free(layer.d_sum);
     layer.bases = nullptr;
     layer.delta = nullptr;
+    layer.d_sum = nullptr;
 }
 
 // ---------------------------------------------------------------------------
@@ -1018,6 +1025,121 @@ void msm_run_many(HpCudaContext *ctx, const MsmTask *tasks, size_t count, Xyzz *
         i = j;
     }
     ctx->prof_end(whole, st);
+}
+
+// ---------------------------------------------------------------------------
+// Binary scalars (every scalar 0 or 1)
+// ---------------------------------------------------------------------------
+
+struct ClassifyTask {
+    const Fr *scalars;
+    size_t n;
+};
+
+// flags[t] = 1 when task t has a scalar outside {0, 1} (canonical value)
+__global__ void k_msm_classify(const ClassifyTask *tasks, uint32_t *flags) {
+    const ClassifyTask t = tasks[blockIdx.y];
+    uint32_t other = 0;
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < t.n; i += size_t(gridDim.x) * blockDim.x) {
+        const Fr c = from_mont(load_fr(&t.scalars[i]));
+        uint32_t high = c.v[0] >> 1;
+#pragma unroll
+        for (int k = 1; k < 8; k++) high |= c.v[k];
+        other |= high;
+    }
+    if (__syncthreads_or(other != 0) && threadIdx.x == 0) atomicOr(&flags[blockIdx.y], 1u);
+}
+
+std::vector<char> msm_binary_tasks(HpCudaContext *ctx, const MsmTask *tasks, size_t count) {
+    std::vector<char> binary(count, 0);
+    const char *env = std::getenv("HP_MSM_BINARY");
+    if (count == 0 || (env && env[0] == '0')) return binary;
+    std::vector<ClassifyTask> host(count);
+    size_t max_n = 1;
+    for (size_t i = 0; i < count; i++) {
+        host[i] = ClassifyTask{tasks[i].scalars, tasks[i].n};
+        max_n = std::max(max_n, tasks[i].n);
+    }
+    Scratch dt(ctx, count * sizeof(ClassifyTask)), flags(ctx, count * 4);
+    check_cuda(cudaMemcpyAsync(dt.ptr, host.data(), count * sizeof(ClassifyTask), cudaMemcpyHostToDevice,
+                               ctx->stream));
+    check_cuda(cudaMemsetAsync(flags.ptr, 0, count * 4, ctx->stream));
+    // a memory pass over every table: about two waves of 256-thread blocks
+    const unsigned x = unsigned(std::max<size_t>(
+        1, std::min<size_t>((max_n + 255) / 256, (size_t(2) * ctx->sm_count * 8 + count - 1) / count)));
+    k_msm_classify<<<dim3(x, unsigned(count)), 256, 0, ctx->stream>>>(dt.as<ClassifyTask>(), flags.as<uint32_t>());
+    check_launch();
+    std::vector<uint32_t> f(count);
+    check_cuda(cudaMemcpyAsync(f.data(), flags.ptr, count * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    for (size_t i = 0; i < count; i++) binary[i] = f[i] == 0;
+    return binary;
+}
+
+// Block b sums the selected bases of indices [b * 128 * kBinaryPerThread, ...):
+// thread t takes every 128th index of the block's range (coalesced loads),
+// mixed additions into XYZZ, then a shared-memory tree over the block.
+constexpr int kBinaryThreads = 128;
+constexpr int kBinaryPerThread = 8;
+
+__global__ void __launch_bounds__(kBinaryThreads) k_msm_binary_blocks(const Affine *bases, const Fr *scalars,
+                                                                       size_t n, Xyzz *block_sums) {
+    __shared__ Xyzz sm[kBinaryThreads];
+    const size_t first = size_t(blockIdx.x) * kBinaryThreads * kBinaryPerThread;
+    Xyzz acc = xyzz_inf();
+    for (int k = 0; k < kBinaryPerThread; k++) {
+        const size_t i = first + size_t(k) * kBinaryThreads + threadIdx.x;
+        if (i >= n) break;
+        if (from_mont(load_fr(&scalars[i])).v[0] == 0) continue;  // classified: 0 or 1
+        const Affine a = load_affine(&bases[i]);
+        if (affine_is_inf(a)) continue;
+        acc = xyzz_add_affine(acc, a.x, a.y);
+    }
+    sm[threadIdx.x] = acc;
+    __syncthreads();
+    for (int half = kBinaryThreads / 2; half > 0; half >>= 1) {
+        if (threadIdx.x < half) sm[threadIdx.x] = xyzz_add(sm[threadIdx.x], sm[threadIdx.x + half]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) store_xyzz(&block_sums[blockIdx.x], sm[0]);
+}
+
+// One block: the sum of the block sums (+ D when present) into the last of
+// `rows` partial rows, infinity into the others.
+__global__ void __launch_bounds__(kBinaryThreads) k_msm_binary_final(const Xyzz *block_sums, size_t blocks,
+                                                                      const Xyzz *d_sum, int rows, Xyzz *out) {
+    __shared__ Xyzz sm[kBinaryThreads];
+    Xyzz acc = xyzz_inf();
+    for (size_t b = threadIdx.x; b < blocks; b += kBinaryThreads) acc = xyzz_add(acc, load_xyzz(&block_sums[b]));
+    sm[threadIdx.x] = acc;
+    __syncthreads();
+    for (int half = kBinaryThreads / 2; half > 0; half >>= 1) {
+        if (threadIdx.x < half) sm[threadIdx.x] = xyzz_add(sm[threadIdx.x], sm[threadIdx.x + half]);
+        __syncthreads();
+    }
+    for (int r = threadIdx.x; r < rows - 1; r += kBinaryThreads) store_xyzz(&out[r], xyzz_inf());
+    if (threadIdx.x == 0) {
+        Xyzz total = sm[0];
+        if (d_sum) total = xyzz_add(total, load_xyzz(d_sum));
+        store_xyzz(&out[rows - 1], total);
+    }
+}
+
+void msm_run_binary(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, size_t n, Xyzz *out_partials,
+                    cudaStream_t stream) {
+    const cudaStream_t st = stream ? stream : ctx->stream;
+    require(n >= 1 && n <= layer.n);
+    const MsmShape sh = msm_shape(layer);
+    const size_t per_block = size_t(kBinaryThreads) * kBinaryPerThread;
+    const size_t blocks = (n + per_block - 1) / per_block;
+    Scratch sums(ctx, blocks * sizeof(Xyzz), st);
+    int tok = ctx->prof_begin("msm_binary", st);
+    k_msm_binary_blocks<<<unsigned(blocks), kBinaryThreads, 0, st>>>(layer.bases, scalars, n, sums.as<Xyzz>());
+    check_launch();
+    k_msm_binary_final<<<1, kBinaryThreads, 0, st>>>(sums.as<Xyzz>(), blocks, layer.delta ? layer.d_sum : nullptr,
+                                                    sh.partials, out_partials);
+    check_launch();
+    ctx->prof_end(tok, st);
 }
 
 host::Xyzz64 msm_combine_host(const MsmShape &shape, const host::Xyzz64 *device_partials) {

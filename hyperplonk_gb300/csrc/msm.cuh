@@ -2,6 +2,7 @@
 #pragma once
 #include <cstddef>
 #include <cstdint>
+#include <vector>
 
 #include "g1.cuh"
 #include "host_ec.h"
@@ -29,6 +30,7 @@ struct MsmLayer {
     Affine *bases = nullptr;  // windows * n points (device, context scratch)
     Fr *delta = nullptr;      // n canonical Fr < 2^254 (device), or null
     host::Xyzz64 minus_d{};   // -sum d_i P_i, added by the host finish
+    Xyzz *d_sum = nullptr;    // D = sum d_i P_i (device, one point), or null
 };
 
 // Window width for a new layer of n points: HP_MSM_WINDOW_BITS, else the
@@ -123,6 +125,18 @@ constexpr size_t kMsmManyMaxRecords = size_t(1) << 27;
 // The chunk length an accumulation of `records` records runs with, given a
 // tuned value (0: none): HP_ACC_CHUNK, else the tuned value, else the size rule.
 uint32_t msm_effective_chunk(size_t records, uint32_t tuned);
+
+// Binary scalars.  An MSM whose scalars are all 0 or 1 (the product-check
+// tables frac and prod of a circuit whose permutation is the identity) is
+// the sum of the selected bases: one mixed addition per 1 instead of one per
+// (point, window) record.  msm_binary_tasks classifies every task of a call
+// in one launch and one synchronisation (HP_MSM_BINARY=0: none is binary);
+// msm_run_binary writes the same partial rows msm_run would combine to (all
+// but the last at infinity, the last = the sum + D so that the host finish,
+// which adds -D, is unchanged).
+std::vector<char> msm_binary_tasks(HpCudaContext *ctx, const MsmTask *tasks, size_t count);
+void msm_run_binary(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, size_t n, Xyzz *out_partials,
+                    cudaStream_t stream = nullptr);
 
 // Host: combine the partials of one MSM into a point.
 host::Xyzz64 msm_combine_host(const MsmShape &shape, const host::Xyzz64 *partials);
