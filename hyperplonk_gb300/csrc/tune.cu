@@ -9,7 +9,7 @@
 // for each; this file measures them instead:
 //
 //  - mode 0 (one MSM on its own), keyed by ceil(log2 n): coordinate descent
-//    from the size rule's choice -- window widths c0-2..c0+2, then segment
+//    from the size rule's choice -- window widths c0-4..c0+2, then segment
 //    lengths seg/4..seg*4, then chunk lengths 4..64 -- each candidate timed
 //    as the median of a few runs with CUDA events on the context stream,
 //    over pseudo-random scalars and the first n bases of the parameters'
@@ -277,7 +277,7 @@ HpCudaMsmTuning tune_alone(HpCudaContext *ctx, const MsmLayer &source, size_t n)
     double best_ms = model_ms;
 
     // 1. window width (each candidate is its own window table)
-    for (int c = std::max(4, c0 - 2); c <= std::min(22, c0 + 2); c++) {
+    for (int c = std::max(4, c0 - 4); c <= std::min(22, c0 + 2); c++) {
         if (c == c0 || !msm_window_fits(n, c)) continue;
         auto cand = std::make_unique<LayerGuard>(ctx);
         msm_prepare_prefix_c(ctx, cand->layer, source, n, c);
