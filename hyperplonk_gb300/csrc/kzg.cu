@@ -49,8 +49,8 @@ static const MsmLayer &ready_layer(const HpCudaMultilinearKzgPreparedProverParam
 
 // Download `total` XYZZ partials and finish each MSM into a packet.
 // Independent MSMs, task i writing its partial rows at the running offset.
-// MSMs whose scalars are all 0 or 1 are sums of bases (msm_run_binary, one
-// worker stream for all of them).  Of the others, MSMs of >= 4 M (point,
+// MSMs whose scalars are all 0 or 1 are sums of bases (msm_run_binary, a
+// worker stream each).  Of the others, MSMs of >= 4 M (point,
 // window) records fill the GPU alone: one msm_run each, overlapped on worker
 // streams; all smaller ones share one launch per phase (msm_run_many) on
 // another worker stream (msm_runs_alone).
@@ -68,14 +68,13 @@ static void run_msms(HpCudaContext *ctx, std::vector<MsmTask> tasks, Xyzz *parts
         (binary[i] ? sums : msm_runs_alone(size_t(t.layer->windows) * t.n) ? big : small).push_back(t);
     }
     std::stable_sort(big.begin(), big.end(), [](const MsmTask &a, const MsmTask &b) { return a.n > b.n; });
-    const size_t lanes = big.size() + (small.empty() ? 0 : 1) + (sums.empty() ? 0 : 1);
+    const size_t lanes = big.size() + (small.empty() ? 0 : 1) + sums.size();
     const int k = int(std::min<size_t>(lanes, HpCudaContext::kWorkers));
     ctx->fork(k);
     size_t w = 0;
-    if (!sums.empty()) {
-        const cudaStream_t st = ctx->workers[w++ % size_t(k)];
-        for (const auto &t : sums) msm_run_binary(ctx, *t.layer, t.scalars, t.n, parts + t.out_row, st);
-    }
+    // sums of bases end in a latency-bound tree: one worker stream each, so the tails overlap
+    for (const auto &t : sums)
+        msm_run_binary(ctx, *t.layer, t.scalars, t.n, parts + t.out_row, ctx->workers[w++ % size_t(k)]);
     if (!small.empty()) msm_run_many(ctx, small.data(), small.size(), parts, ctx->workers[w++ % size_t(k)]);
     for (const auto &t : big) msm_run(ctx, *t.layer, t.scalars, parts + t.out_row, ctx->workers[w++ % size_t(k)], t.n);
     ctx->join(k);

@@ -1076,20 +1076,21 @@ std::vector<char> msm_binary_tasks(HpCudaContext *ctx, const MsmTask *tasks, siz
     return binary;
 }
 
-// Block b sums the selected bases of indices [b * 128 * kBinaryPerThread, ...):
-// thread t takes every 128th index of the block's range (coalesced loads),
-// mixed additions into XYZZ, then a shared-memory tree over the block.
+// A grid of at most 4 blocks per SM (the accumulation kernel's residency:
+// 128 registers a thread) strides over the indices, thread t of block b
+// taking b * 128 + t + k * (grid * 128) (coalesced loads): mixed additions of
+// the selected bases into XYZZ, then a shared-memory tree over the block.
+// Measured at 2^20 points: 196 registers and 8-index ranges per thread
+// (2 blocks per SM) took 0.98 ms.
 constexpr int kBinaryThreads = 128;
-constexpr int kBinaryPerThread = 8;
+constexpr int kBinaryPerThread = 8;  // indices per thread below the grid cap
 
-__global__ void __launch_bounds__(kBinaryThreads) k_msm_binary_blocks(const Affine *bases, const Fr *scalars,
-                                                                       size_t n, Xyzz *block_sums) {
+__global__ void __launch_bounds__(kBinaryThreads, 4) k_msm_binary_blocks(const Affine *bases, const Fr *scalars,
+                                                                          size_t n, Xyzz *block_sums) {
     __shared__ Xyzz sm[kBinaryThreads];
-    const size_t first = size_t(blockIdx.x) * kBinaryThreads * kBinaryPerThread;
     Xyzz acc = xyzz_inf();
-    for (int k = 0; k < kBinaryPerThread; k++) {
-        const size_t i = first + size_t(k) * kBinaryThreads + threadIdx.x;
-        if (i >= n) break;
+    for (size_t i = size_t(blockIdx.x) * kBinaryThreads + threadIdx.x; i < n;
+         i += size_t(gridDim.x) * kBinaryThreads) {
         if (from_mont(load_fr(&scalars[i])).v[0] == 0) continue;  // classified: 0 or 1
         const Affine a = load_affine(&bases[i]);
         if (affine_is_inf(a)) continue;
@@ -1131,7 +1132,7 @@ void msm_run_binary(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars
     require(n >= 1 && n <= layer.n);
     const MsmShape sh = msm_shape(layer);
     const size_t per_block = size_t(kBinaryThreads) * kBinaryPerThread;
-    const size_t blocks = (n + per_block - 1) / per_block;
+    const size_t blocks = std::min<size_t>((n + per_block - 1) / per_block, size_t(4) * ctx->sm_count);
     Scratch sums(ctx, blocks * sizeof(Xyzz), st);
     int tok = ctx->prof_begin("msm_binary", st);
     k_msm_binary_blocks<<<unsigned(blocks), kBinaryThreads, 0, st>>>(layer.bases, scalars, n, sums.as<Xyzz>());
