@@ -442,19 +442,34 @@ extern "C" HpCudaStatus hp_cuda_v1_mle_upload_many(HpCudaContext *ctx, size_t nu
         require(evaluation_count == n);
         for (size_t i = 0; i < count; i++) require(evaluations[i] != nullptr);
         if (count == 0) return;
-        // every copy and conversion queued back to back, one validation
-        // synchronisation for the batch; a non-canonical table fails the
-        // whole call and every buffer of it is released
+        // table i's copy and conversion on worker stream i (mod the worker
+        // count), so copies run side by side and each conversion overlaps the
+        // next copies; one validation synchronisation for the batch.  A
+        // non-canonical table fails the whole call and every buffer of it is
+        // released (after the workers have joined back).
         std::vector<OwnedBuffer> bufs;
         bufs.reserve(count);
+        for (size_t i = 0; i < count; i++) bufs.emplace_back(ctx, n * kFrBytes);
         ctx->clear_flags();
-        for (size_t i = 0; i < count; i++) {
-            bufs.emplace_back(ctx, n * kFrBytes);
-            check_cuda(cudaMemcpyAsync(bufs.back().ptr, evaluations[i], n * kFrBytes, cudaMemcpyHostToDevice,
-                                       ctx->stream));
-            hp::k_to_mont_check<<<hp::grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(bufs.back().as<Fr>(), n,
-                                                                                   ctx->d_flags);
-            check_launch();
+        {
+            const int k = int(std::min<size_t>(count, HpCudaContext::kWorkers));
+            ctx->fork(k);
+            struct Join {
+                HpCudaContext *c;
+                int k;
+                ~Join() {
+                    try {
+                        c->join(k);
+                    } catch (...) {
+                    }
+                }
+            } join{ctx, k};
+            for (size_t i = 0; i < count; i++) {
+                const cudaStream_t st = ctx->workers[i % size_t(k)];
+                check_cuda(cudaMemcpyAsync(bufs[i].ptr, evaluations[i], n * kFrBytes, cudaMemcpyHostToDevice, st));
+                hp::k_to_mont_check<<<hp::grid_for(ctx, n, 256), 256, 0, st>>>(bufs[i].as<Fr>(), n, ctx->d_flags);
+                check_launch();
+            }
         }
         const uint32_t flags = ctx->sync_flags();
         if (flags & hp::kFlagNonCanonical) fail(HP_CUDA_STATUS_INVALID_PARAMETERS);

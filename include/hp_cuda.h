@@ -80,9 +80,9 @@ HpCudaStatus hp_cuda_v1_buffer_retire(HpCudaContext *ctx, HpCudaDeviceAddress ad
 HpCudaStatus hp_cuda_v1_mle_upload(HpCudaContext *ctx, size_t num_vars, const uint8_t *evaluations,
                                    size_t evaluation_count, HpCudaDeviceAddress *out);
 /* `count` tables of 2^num_vars canonical Fr uploaded in one call: the same
- * result as `count` hp_cuda_v1_mle_upload calls (bridge.h:46), with the
- * copies and conversions queued back to back and one validation
- * synchronisation.  A non-canonical element in any table fails the whole
+ * result as `count` hp_cuda_v1_mle_upload calls (bridge.h:46), with each
+ * table's copy and conversion on its own worker stream (copies side by side)
+ * and one validation synchronisation.  A non-canonical element in any table fails the whole
  * call (InvalidParameters) and leaves every out slot null.  No counterpart in
  * the reference, whose uploads are one table per call. */
 HpCudaStatus hp_cuda_v1_mle_upload_many(HpCudaContext *ctx, size_t num_vars, const uint8_t *const *evaluations,
