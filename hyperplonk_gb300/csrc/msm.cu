@@ -1031,48 +1031,55 @@ void msm_run_many(HpCudaContext *ctx, const MsmTask *tasks, size_t count, Xyzz *
 // Binary scalars (every scalar 0 or 1)
 // ---------------------------------------------------------------------------
 
-struct ClassifyTask {
-    const Fr *scalars;
-    size_t n;
+// Up to kClassifyList tables per launch, passed by value (no descriptor copy).
+constexpr int kClassifyList = 32;
+struct ClassifyList {
+    const Fr *scalars[kClassifyList];
+    size_t n[kClassifyList];
 };
 
-// flags[t] = 1 when task t has a scalar outside {0, 1} (canonical value)
-__global__ void k_msm_classify(const ClassifyTask *tasks, uint32_t *flags) {
-    const ClassifyTask t = tasks[blockIdx.y];
+// flags[t] = 1 when table t (blockIdx.y) has a scalar outside {0, 1}
+// (canonical value).  flags is host-mapped memory zeroed by the host; blocks
+// only ever store 1 there, so no atomics cross the link.
+__global__ void k_msm_classify(ClassifyList list, uint32_t *flags) {
+    const Fr *scalars = list.scalars[blockIdx.y];
+    const size_t n = list.n[blockIdx.y];
     uint32_t other = 0;
-    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < t.n; i += size_t(gridDim.x) * blockDim.x) {
-        const Fr c = from_mont(load_fr(&t.scalars[i]));
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+        const Fr c = from_mont(load_fr(&scalars[i]));
         uint32_t high = c.v[0] >> 1;
 #pragma unroll
         for (int k = 1; k < 8; k++) high |= c.v[k];
         other |= high;
     }
-    if (__syncthreads_or(other != 0) && threadIdx.x == 0) atomicOr(&flags[blockIdx.y], 1u);
+    if (__syncthreads_or(other != 0) && threadIdx.x == 0) flags[blockIdx.y] = 1u;
 }
 
 std::vector<char> msm_binary_tasks(HpCudaContext *ctx, const MsmTask *tasks, size_t count) {
     std::vector<char> binary(count, 0);
     const char *env = std::getenv("HP_MSM_BINARY");
     if (count == 0 || (env && env[0] == '0')) return binary;
-    std::vector<ClassifyTask> host(count);
-    size_t max_n = 1;
-    for (size_t i = 0; i < count; i++) {
-        host[i] = ClassifyTask{tasks[i].scalars, tasks[i].n};
-        max_n = std::max(max_n, tasks[i].n);
+    void *dev = nullptr;
+    volatile uint32_t *host =
+        reinterpret_cast<volatile uint32_t *>(ctx->mailbox(count * sizeof(uint32_t), &dev));
+    for (size_t i = 0; i < count; i++) host[i] = 0;
+    for (size_t first = 0; first < count; first += kClassifyList) {
+        const size_t m = std::min<size_t>(kClassifyList, count - first);
+        ClassifyList list{};
+        size_t max_n = 1;
+        for (size_t i = 0; i < m; i++) {
+            list.scalars[i] = tasks[first + i].scalars;
+            list.n[i] = tasks[first + i].n;
+            max_n = std::max(max_n, tasks[first + i].n);
+        }
+        // a memory pass over every table: about two waves of 256-thread blocks
+        const unsigned x = unsigned(std::max<size_t>(
+            1, std::min<size_t>((max_n + 255) / 256, (size_t(2) * ctx->sm_count * 8 + m - 1) / m)));
+        k_msm_classify<<<dim3(x, unsigned(m)), 256, 0, ctx->stream>>>(list, static_cast<uint32_t *>(dev) + first);
+        check_launch();
     }
-    Scratch dt(ctx, count * sizeof(ClassifyTask)), flags(ctx, count * 4);
-    check_cuda(cudaMemcpyAsync(dt.ptr, host.data(), count * sizeof(ClassifyTask), cudaMemcpyHostToDevice,
-                               ctx->stream));
-    check_cuda(cudaMemsetAsync(flags.ptr, 0, count * 4, ctx->stream));
-    // a memory pass over every table: about two waves of 256-thread blocks
-    const unsigned x = unsigned(std::max<size_t>(
-        1, std::min<size_t>((max_n + 255) / 256, (size_t(2) * ctx->sm_count * 8 + count - 1) / count)));
-    k_msm_classify<<<dim3(x, unsigned(count)), 256, 0, ctx->stream>>>(dt.as<ClassifyTask>(), flags.as<uint32_t>());
-    check_launch();
-    std::vector<uint32_t> f(count);
-    check_cuda(cudaMemcpyAsync(f.data(), flags.ptr, count * 4, cudaMemcpyDeviceToHost, ctx->stream));
     ctx->sync();
-    for (size_t i = 0; i < count; i++) binary[i] = f[i] == 0;
+    for (size_t i = 0; i < count; i++) binary[i] = host[i] == 0;
     return binary;
 }
 
