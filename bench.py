@@ -772,6 +772,8 @@ def run_gb300(args, world, rank, local, pg):
         "clocks": clk,
     }
     result.update(extra)
+    if TUNING_INFO:
+        result["msm_tuning"] = dict(TUNING_INFO)
     # the same kernel against the pipe it actually fills: a Karatsuba Fq
     # product issues 108 + 144 wide multiply-adds, so the live mad.wide rate
     # / 252 caps the product rate before any addition, carry or load
