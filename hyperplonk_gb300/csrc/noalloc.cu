@@ -2,9 +2,7 @@
 //
 // Who needs it: a host that carves all of the GPU's memory into its own arena
 // at start-up (a proving service that budgets HBM per request and must not
-// have a library allocate behind its back), or code that runs while a CUDA
-// stream capture is active, where cudaMalloc / cudaFree are not allowed or
-// would synchronise the device.  Such callers cannot use
+// have a library allocate behind its back).  Such callers cannot use
 // hp_cuda_v1_mle_evaluate, which takes its fold buffers from the context's
 // memory pool.  This variant keeps its intermediate values in one fixed
 // file-scope device array instead, so a call issues only kernel launches, one
@@ -19,6 +17,9 @@
 //    race on it.  Serialise them, e.g. by issuing them on one stream;
 //  - nothing in the array needs to start at zero: each pass writes every entry
 //    it later reads, so the contents left by the previous call never matter;
+//  - `table` must be device memory of the current device (checked with
+//    cudaPointerGetAttributes; anything else is InvalidParameters), because
+//    the kernels run on the current device;
 //  - the first call on a device looks up the array's device address
 //    (cudaGetSymbolAddress) once; make that first call before any stream
 //    capture begins.
@@ -110,6 +111,16 @@ extern "C" HpCudaStatus hp_cuda_v1_mle_evaluate_noalloc(const void *table, size_
         }
         int dev = 0;
         Fr *scratch = scratch_for_current_device(&dev);
+        // the table must live on the device the kernels run on: a peer
+        // pointer (or a host pointer) would be read across the link or fault
+        cudaPointerAttributes attr;
+        std::memset(&attr, 0, sizeof attr);
+        if (cudaPointerGetAttributes(&attr, table) != cudaSuccess) {
+            (void)cudaGetLastError();
+            fail(HP_CUDA_STATUS_INVALID_PARAMETERS);
+        }
+        if ((attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged) || attr.device != dev)
+            fail(HP_CUDA_STATUS_INVALID_PARAMETERS);
         cudaStream_t s = static_cast<cudaStream_t>(stream);
         // Regions: A = [0, 2^14) pass-1 output, B = [2^14, 2^14+16) pass-2
         // output, then the result slot and its canonical copy.

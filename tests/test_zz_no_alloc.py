@@ -1,8 +1,7 @@
 """The allocation-free evaluation entry (hp_cuda_v1_mle_evaluate_noalloc).
 
-Callers that own all device memory through their own arena, or that run
-inside a CUDA stream capture, cannot let the library allocate; this entry
-keeps its intermediates in a fixed device array.  The test calls it through
+Callers that own all device memory through their own arena cannot let the
+library allocate; this entry keeps its intermediates in a fixed device array.  The test calls it through
 the C ABI and checks its result against the allocating entry
 hp_cuda_v1_mle_evaluate on the same inputs, twice in a row (the shared array
 keeps the previous call's contents, which must not matter).  This file is
@@ -77,3 +76,15 @@ def test_noalloc_rejects_tables_above_the_limit(gpu, oracle):
     out = (ctypes.c_uint8 * 32)()
     with pytest.raises(InvalidParameters):
         check_status(fn(ctypes.c_void_p(mle.address), 25, _native.buf(pt), out, None), "mle_evaluate_noalloc")
+
+
+def test_noalloc_rejects_a_host_pointer(gpu):
+    """A table that is not memory of the current device is refused before any
+    kernel runs."""
+    fn = _bind(gpu.lib)
+    host_table = (ctypes.c_uint8 * (32 * 4))()
+    pt = encode_frs([3, 5])
+    out = (ctypes.c_uint8 * 32)()
+    with pytest.raises(InvalidParameters):
+        check_status(fn(ctypes.cast(host_table, ctypes.c_void_p), 2, _native.buf(pt), out, None),
+                     "mle_evaluate_noalloc")
