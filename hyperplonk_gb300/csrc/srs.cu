@@ -204,8 +204,14 @@ extern "C" HpCudaStatus hp_cuda_v1_srs_generate(HpCudaContext *ctx, size_t num_v
 // Selectors from stream `seed` elements [k n, (k+1) n) for q_L, q_R, q_M, q_C
 // (k = 0..3); w1, w2 from stream `witness_seed` elements [4n, 5n) and [5n, 6n);
 // w3 solves the gate.  selectors / permutation may be null (witnesses only).
+// Wired variant (`wired`): w2[i] = w1[wire(i)] with wire(i) = (A i + B) mod n,
+// A odd (a bijection of Z_n), B = seed * C + 1, and the permutation swaps w2
+// cell i with w1 cell wire(i) (2-cycles; w3 cells fixed), so the copy
+// constraints hold and are not the identity.
+constexpr uint64_t kWireA = 0x9E3779B97F4A7C15ULL, kWireC = 0xD1B54A32D192ED03ULL;
+
 static void vanilla_fixture(uint64_t seed, uint64_t witness_seed, size_t num_vars, uint8_t *selectors,
-                            uint8_t *witnesses, uint8_t *permutation) {
+                            uint8_t *witnesses, uint8_t *permutation, bool wired = false) {
     {
         const size_t n = size_t(1) << num_vars;
         hp::host::Fr64 minus_one;
@@ -232,7 +238,9 @@ static void vanilla_fixture(uint64_t seed, uint64_t witness_seed, size_t num_var
                     Fr64 ql = hp::fixture_element(seed, i), qr = hp::fixture_element(seed, n + i);
                     Fr64 qm = hp::fixture_element(seed, 2 * n + i), qc = hp::fixture_element(seed, 3 * n + i);
                     Fr64 w1 = hp::fixture_element(witness_seed, 4 * n + i);
-                    Fr64 w2 = hp::fixture_element(witness_seed, 5 * n + i);
+                    const size_t wire = wired ? size_t((kWireA * i + seed * kWireC + 1) & (n - 1)) : i;
+                    Fr64 w2 = wired ? hp::fixture_element(witness_seed, 4 * n + wire)
+                                    : hp::fixture_element(witness_seed, 5 * n + i);
                     Fr64 w3 = add(add(mont_mul(ql, w1), mont_mul(qr, w2)), add(mont_mul(mont_mul(qm, w1), w2), qc));
                     const Fr64 sel[5] = {ql, qr, minus_one, qm, qc};
                     const Fr64 wit[3] = {w1, w2, w3};
@@ -241,9 +249,13 @@ static void vanilla_fixture(uint64_t seed, uint64_t witness_seed, size_t num_var
                     for (int k = 0; k < 3; k++) {
                         to_canonical(wit[k], witnesses + (size_t(k) * n + i) * 32);
                         if (!permutation) continue;
-                        uint8_t *p = permutation + (size_t(k) * n + i) * 32;
+                        // sigma(cell): w1 cell wire -> w2 cell i, w2 cell i -> w1 cell wire
+                        const size_t row = (wired && k == 0) ? wire : i;
+                        const uint64_t label = !wired || k == 2 ? uint64_t(k) * n + i
+                                               : k == 0       ? uint64_t(n) + i
+                                                              : uint64_t(wire);
+                        uint8_t *p = permutation + (size_t(k) * n + row) * 32;
                         std::memset(p, 0, 32);
-                        uint64_t label = uint64_t(k) * n + i;
                         std::memcpy(p, &label, 8);
                     }
                 }
@@ -258,6 +270,15 @@ extern "C" HpCudaStatus hp_cuda_v1_fixture_vanilla_plonk(uint64_t seed, size_t n
     return guard([&] {
         require(selectors != nullptr && witnesses != nullptr && permutation != nullptr && num_vars <= 28);
         vanilla_fixture(seed, seed, num_vars, selectors, witnesses, permutation);
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_fixture_vanilla_plonk_wired(uint64_t seed, size_t num_vars, uint8_t *selectors,
+                                                               uint8_t *witnesses, uint8_t *permutation) {
+    return guard([&] {
+        require(selectors != nullptr && witnesses != nullptr && permutation != nullptr && num_vars >= 1 &&
+                num_vars <= 28);
+        vanilla_fixture(seed, seed, num_vars, selectors, witnesses, permutation, true);
     });
 }
 

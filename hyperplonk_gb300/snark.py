@@ -182,7 +182,7 @@ def prove(backend, pk: ProvingKey, pub_input: list, witnesses: list, transcript_
 # vanilla-plonk fixture (full-prove workload)
 # ---------------------------------------------------------------------------
 
-def vanilla_fixture(num_vars: int, seed: int, num_pub_input: int = 16):
+def vanilla_fixture(num_vars: int, seed: int, num_pub_input: int = 16, wired: bool = False):
     """Selectors [q_L, q_R, q_O, q_M, q_C] and witnesses [w1, w2, w3] as
     canonical table packets (uint8 arrays), the identity permutation over the
     three witness columns (labels column * 2^nv + row, common/permutation.rs
@@ -190,7 +190,10 @@ def vanilla_fixture(num_vars: int, seed: int, num_pub_input: int = 16):
 
     q_L, q_R, q_M, q_C, w1, w2 are uniform (fixture stream `seed`, elements
     [k*N, (k+1)*N) for k = 0..5), q_O = -1 and w3 = q_L w1 + q_R w2 + q_M w1 w2
-    + q_C, so the repo's gate holds on every row.  Built by the host fixture
+    + q_C, so the repo's gate holds on every row.  With `wired`, the copy
+    constraints are not the identity: w2[i] = w1[wire(i)] for a bijection
+    wire of the rows, and the permutation swaps those cells
+    (hp_cuda_v1_fixture_vanilla_plonk_wired).  Built by the host fixture
     generator of libhp_cuda.so."""
     from . import _native
     from .errors import check_status
@@ -199,7 +202,8 @@ def vanilla_fixture(num_vars: int, seed: int, num_pub_input: int = 16):
     sel = np.empty((5, 32 * n), dtype=np.uint8)
     wit = np.empty((3, 32 * n), dtype=np.uint8)
     perm = np.empty((3, 32 * n), dtype=np.uint8)
-    check_status(lib.hp_cuda_v1_fixture_vanilla_plonk(
+    entry = lib.hp_cuda_v1_fixture_vanilla_plonk_wired if wired else lib.hp_cuda_v1_fixture_vanilla_plonk
+    check_status(entry(
         ctypes.c_uint64(seed), num_vars, sel.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
         wit.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), perm.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))),
         "fixture_vanilla_plonk")

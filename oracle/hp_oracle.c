@@ -1195,6 +1195,98 @@ void or_random_fr(uint64_t seed, uint64_t first, size_t n, uint8_t *out) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* Vanilla-plonk fixture (the full-prove workload), restated independently  */
+/* of the product's generator.  Gate of hyperplonk/src/custom_gate.rs:86-96  */
+/* (q_L w1 + q_R w2 + q_O w3 + q_M w1 w2 + q_C = 0, selectors [q_L, q_R,     */
+/* q_O, q_M, q_C]); q_L, q_R, q_M, q_C = stream `seed` elements [k n,        */
+/* (k+1) n) for k = 0..3, w1 = elements [4n, 5n), q_O = -1 and w3 solves the */
+/* gate.  w1 and w2 come from stream `witness_seed` (= `seed` for the       */
+/* circuit's own witness; another value gives another satisfying witness).  */
+/*  - plain (wired = 0): w2 = elements [5n, 6n) and the identity permutation */
+/*    over the 3 witness columns (label of cell (column k, row i) = k n + i,  */
+/*    backend/src/common/permutation.rs:12-15);                              */
+/*  - wired (wired = 1): w2[i] = w1[pi(i)] with pi(i) = (A i + B) mod n, A  */
+/*    odd (a bijection of Z_n), B = seed * C1 + 1; every w2 cell i and w1   */
+/*    cell pi(i) are swapped by the permutation (a 2-cycle: the copy         */
+/*    constraint w2[i] = w1[pi(i)] holds), w3 cells stay fixed.  The         */
+/*    product check then sees random fractions instead of ones.              */
+/* ------------------------------------------------------------------------ */
+
+#define WIRE_A 0x9E3779B97F4A7C15ULL
+#define WIRE_C1 0xD1B54A32D192ED03ULL
+
+typedef struct {
+    uint64_t seed, witness_seed;
+    size_t n;
+    int wired;
+    uint8_t *sel, *wit, *perm;
+} fixture_ctx;
+
+static size_t wire_of(uint64_t seed, size_t n, size_t i) {
+    return (size_t)((WIRE_A * (uint64_t)i + seed * WIRE_C1 + 1) & (uint64_t)(n - 1));
+}
+
+static void stream_fr(uint64_t seed, uint64_t index, fr_t *out) {
+    uint8_t blk[64];
+    chacha20_block(seed, index, blk);
+    fr_from_wide64(out, blk); /* Montgomery form */
+}
+
+static void put_label(uint8_t *dst, uint64_t label) {
+    memset(dst, 0, 32);
+    for (int b = 0; b < 8; b++) dst[b] = (uint8_t)(label >> (8 * b));
+}
+
+static void fixture_range(void *vctx, size_t b, size_t e, int worker) {
+    (void)worker;
+    fixture_ctx *c = (fixture_ctx *)vctx;
+    const size_t n = c->n;
+    fr_t minus_one, zero;
+    fr_zero(&zero);
+    fr_one(&minus_one);
+    fr_sub(&minus_one, &zero, &minus_one);
+    for (size_t i = b; i < e; i++) {
+        fr_t ql, qr, qm, qc, w1, w2, w3, t;
+        stream_fr(c->seed, i, &ql);
+        stream_fr(c->seed, n + i, &qr);
+        stream_fr(c->seed, 2 * n + i, &qm);
+        stream_fr(c->seed, 3 * n + i, &qc);
+        stream_fr(c->witness_seed, 4 * n + i, &w1);
+        size_t pi = c->wired ? wire_of(c->seed, n, i) : i;
+        stream_fr(c->witness_seed, c->wired ? 4 * n + pi : 5 * n + i, &w2);
+        fr_mul(&w3, &ql, &w1);
+        fr_mul(&t, &qr, &w2);
+        fr_add(&w3, &w3, &t);
+        fr_mul(&t, &qm, &w1);
+        fr_mul(&t, &t, &w2);
+        fr_add(&w3, &w3, &t);
+        fr_add(&w3, &w3, &qc);
+        const fr_t *sel[5] = {&ql, &qr, &minus_one, &qm, &qc};
+        const fr_t *wit[3] = {&w1, &w2, &w3};
+        for (int k = 0; k < 5; k++) fr_to_bytes(c->sel + 32 * ((size_t)k * n + i), sel[k]);
+        for (int k = 0; k < 3; k++) fr_to_bytes(c->wit + 32 * ((size_t)k * n + i), wit[k]);
+        if (c->wired) {
+            put_label(c->perm + 32 * pi, (uint64_t)n + i);       /* w1 cell pi(i) -> w2 cell i */
+            put_label(c->perm + 32 * (n + i), (uint64_t)pi);     /* w2 cell i -> w1 cell pi(i) */
+        } else {
+            put_label(c->perm + 32 * i, (uint64_t)i);
+            put_label(c->perm + 32 * (n + i), (uint64_t)n + i);
+        }
+        put_label(c->perm + 32 * (2 * n + i), 2 * (uint64_t)n + i);
+    }
+}
+
+/* Writes 5 selector tables (sel: 5 * 2^nv Fr), 3 witness tables and 3
+ * permutation tables, canonical LE32, table-major.  Returns 1 for nv > 28. */
+int or_fixture_vanilla_plonk(uint64_t seed, uint64_t witness_seed, size_t nv, int wired, uint8_t *sel, uint8_t *wit,
+                             uint8_t *perm) {
+    if (nv > 28) return 1;
+    fixture_ctx c = {seed, witness_seed, (size_t)1 << nv, wired != 0, sel, wit, perm};
+    parallel_for(c.n, fixture_range, &c);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* Testing SRS (subroutines/src/pcs/multilinear_kzg/srs.rs:158-235)          */
 /* g = s*G1 and t[0..nv) from the fixture stream `seed` (t_i = block i,      */
 /* s = block nv).  Layer i (i < nv) = g * eq(t[i..], x) over 2^(nv-i) x with */

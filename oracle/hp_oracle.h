@@ -38,6 +38,8 @@ int or_kzg_open(const uint8_t *const *layers96, const uint8_t *poly, size_t nv, 
                 uint8_t *out_q96, uint8_t *out_eval);
 void or_random_fr(uint64_t seed, uint64_t first, size_t n, uint8_t *out);
 int or_srs_gen(size_t nv, uint64_t seed, uint8_t *out);
+int or_fixture_vanilla_plonk(uint64_t seed, uint64_t witness_seed, size_t nv, int wired, uint8_t *sel, uint8_t *wit,
+                             uint8_t *perm);
 void or_g1_generator(uint8_t *out96);
 
 #ifdef __cplusplus

@@ -141,13 +141,10 @@ def point_to_affine(p) -> bytes:
 
 def packets_to_affine(packets) -> bytes:
     """97-byte G1 packets -> 96-byte affine (infinity -> zeros)."""
-    b = bytes(packets)
-    n = len(b) // 97
-    out = bytearray(96 * n)
-    for i in range(n):
-        if b[97 * i] == 0:
-            out[96 * i:96 * i + 96] = b[97 * i + 1:97 * i + 97]
-    return bytes(out)
+    a = np.frombuffer(bytes(packets), dtype=np.uint8).reshape(-1, 97)
+    out = a[:, 1:].copy()
+    out[a[:, 0] != 0] = 0
+    return out.tobytes()
 
 
 def affine_to_packets(affine) -> bytes:

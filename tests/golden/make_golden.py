@@ -7,7 +7,7 @@ compact .npz files beside this script.  Large MSM inputs whose bases are the
 consecutive multiples 1*G, 2*G, ... are stored as a marker plus the SHA-256
 of the reference's bases file; the tests rebuild them and check the digest.
 
-Usage: python tests/golden/make_golden.py [--reference /path/to/reference]
+Usage: python tests/golden/make_golden.py --reference /path/to/reference
 This is the only file in the repository that reads the reference tree.
 """
 from __future__ import annotations
@@ -129,7 +129,8 @@ def consecutive_digest_cached(n: int, _unused) -> str:
 
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__)
-    ap.add_argument("--reference", default="/root/reference", type=pathlib.Path)
+    ap.add_argument("--reference", required=True, type=pathlib.Path,
+                    help="root of a checkout of the reference repository")
     args = ap.parse_args()
     pack(HERE, args.reference)
 

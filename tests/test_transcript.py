@@ -55,3 +55,30 @@ def test_iop_transcript_challenges_match():
         t.append_serializable_element(b"aux info", (2).to_bytes(8, "little") + (20).to_bytes(8, "little"))
         t.append_field_element(b"x", 12345)
     assert a.get_and_append_challenge_vectors(b"0check r", 5) == b.get_and_append_challenge_vectors(b"0check r", 5)
+
+
+# Published Merlin 1.0 known answers (the simple and the long transcript of
+# the merlin crate's equivalence tests, reproduced by its other-language
+# implementations): they pin the STROBE-128 framing, not only Keccak-f.
+MERLIN_SIMPLE = "d5a21972d0d5fe320c0d263fac7fffb8145aa640af6e9bca177c03c7efcf0615"
+MERLIN_LONG = "a8c933f54fae76e3f9bea93648c1308e7dfa2152dd51674ff3ca438351cf003c"
+
+
+@pytest.mark.parametrize("cls", [MerlinTranscript, tref.Merlin], ids=["native", "oracle"])
+def test_merlin_published_simple_vector(cls):
+    t = cls(b"test protocol")
+    t.append_message(b"some label", b"some data")
+    assert t.challenge_bytes(b"challenge", 32).hex() == MERLIN_SIMPLE
+
+
+@pytest.mark.parametrize("cls", [MerlinTranscript, tref.Merlin], ids=["native", "oracle"])
+def test_merlin_published_long_vector(cls):
+    t = cls(b"test protocol")
+    t.append_message(b"step1", b"some data")
+    data = bytes([99]) * 1024
+    chl = b""
+    for _ in range(32):
+        chl = t.challenge_bytes(b"challenge", 32)
+        t.append_message(b"bigdata", data)
+        t.append_message(b"challengedata", chl)
+    assert chl.hex() == MERLIN_LONG
