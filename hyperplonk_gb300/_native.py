@@ -29,6 +29,20 @@ class MsmTuning(ctypes.Structure):
                 ("tuned_ms", ctypes.c_double)]
 
 
+class RuntimeCounters(ctypes.Structure):
+    """HpCudaRuntimeCounters (include/hp_cuda.h)."""
+    _fields_ = [(name, ctypes.c_uint64) for name in (
+        "device_allocs", "host_allocs", "pool_allocs", "pool_alloc_bytes", "frees", "h2d_copies", "h2d_bytes",
+        "d2h_copies", "d2h_bytes", "d2d_copies", "d2d_bytes", "other_copies", "other_bytes", "memsets", "syncs",
+        "injected_failures")]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+INJECT_NONE, INJECT_POOL_ALLOCATION, INJECT_SYNCHRONIZE = 0, 1, 2
+
+
 # name -> argument types (all return Status)
 SIGNATURES: dict[str, list] = {
     "hp_cuda_v1_context_create": [ctypes.c_int32, c_voidpp],
@@ -70,6 +84,9 @@ SIGNATURES: dict[str, list] = {
     "hp_cuda_v1_srs_generate": [c_voidp, c_size, ctypes.c_uint64, c_u8p, c_size],
     "hp_cuda_v1_fixture_vanilla_plonk": [ctypes.c_uint64, c_size, c_u8p, c_u8p, c_u8p],
     "hp_cuda_v1_fixture_vanilla_plonk_witness": [ctypes.c_uint64, ctypes.c_uint64, c_size, c_u8p],
+    "hp_cuda_v1_fixture_vanilla_plonk_wired": [ctypes.c_uint64, c_size, c_u8p, c_u8p, c_u8p],
+    "hp_cuda_v1_debug_runtime_counters": [ctypes.POINTER(RuntimeCounters)],
+    "hp_cuda_v1_debug_inject_failure": [ctypes.c_int32, ctypes.c_uint64],
     "hp_host_v1_merlin_new": [c_u8p, c_size, c_voidpp],
     "hp_host_v1_merlin_append": [c_voidp, c_u8p, c_size, c_u8p, c_size],
     "hp_host_v1_merlin_challenge": [c_voidp, c_u8p, c_size, c_u8p, c_size],
@@ -125,3 +142,19 @@ def buf(data) -> ctypes.Array:
     import numpy as np
     arr = np.ascontiguousarray(np.frombuffer(data, dtype=np.uint8)) if not isinstance(data, np.ndarray) else data
     return arr.ctypes.data_as(c_u8p)
+
+
+def runtime_counters() -> dict:
+    """The library's CUDA runtime call counters (hp_cuda_v1_debug_runtime_counters)."""
+    from .errors import check_status
+    c = RuntimeCounters()
+    check_status(load().hp_cuda_v1_debug_runtime_counters(ctypes.byref(c)), "debug_runtime_counters")
+    return c.as_dict()
+
+
+def inject_failure(what: int, nth: int) -> None:
+    """Arms (nth >= 1) or disarms (nth = 0) an injected failure
+    (hp_cuda_v1_debug_inject_failure)."""
+    from .errors import check_status
+    check_status(load().hp_cuda_v1_debug_inject_failure(what, nth), "debug_inject_failure")
+

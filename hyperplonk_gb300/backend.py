@@ -15,6 +15,8 @@ None for the point at infinity.
 from __future__ import annotations
 
 import contextlib
+import os
+import sys
 import ctypes
 from typing import Iterable, Optional, Sequence
 
@@ -89,6 +91,19 @@ def _nbytes(data) -> int:
 # handles
 # --------------------------------------------------------------------------
 
+def _destroy_or_abort(op: str, status) -> None:
+    """A handle destructor's status: a failure is a contract violation that
+    cannot be reported to a caller (destructors have none), so the process
+    aborts after saying what failed, as the reference's device backend does
+    (backend/src/ascend910b3/mod.rs:46-47, context.rs:126-128)."""
+    if status.kind == 0:
+        return
+    sys.stderr.write(f"hyperplonk_gb300: {op} failed while destroying a handle (status kind {status.kind}, "
+                     f"native code {status.native_code}); aborting\n")
+    sys.stderr.flush()
+    os.abort()
+
+
 class CudaContext:
     """One device, one stream (bridge.h: single host thread, single stream)."""
 
@@ -118,10 +133,10 @@ class CudaContext:
         self.raw = None
 
     def __del__(self):
-        try:
-            self.close()
-        except Exception:
-            pass
+        raw = getattr(self, "raw", None)
+        if raw is not None and raw.value:
+            self.raw = None
+            _destroy_or_abort("context_destroy", self.lib.hp_cuda_v1_context_destroy(raw))
 
 
 class CudaMle:
@@ -145,13 +160,11 @@ class CudaMle:
 
     def __del__(self):
         ctx = self._ctx
-        if ctx is not None and ctx.raw is not None and self._addr:
-            try:
-                with ctx.held():
-                    ctx.lib.hp_cuda_v1_buffer_retire(ctx.raw, ctypes.c_void_p(self._addr))
-            except Exception:
-                pass
-        self._addr = 0
+        addr, self._addr = self._addr, 0
+        if ctx is not None and ctx.raw is not None and addr:
+            with ctx.held():
+                status = ctx.lib.hp_cuda_v1_buffer_retire(ctx.raw, ctypes.c_void_p(addr))
+            _destroy_or_abort("buffer_retire", status)
 
 
 class CudaPreparedProverParam:
@@ -160,13 +173,11 @@ class CudaPreparedProverParam:
 
     def __del__(self):
         ctx = self._ctx
-        if ctx is not None and ctx.raw is not None and self.raw is not None:
-            try:
-                with ctx.held():
-                    ctx.lib.hp_cuda_v1_multilinear_kzg_params_destroy(ctx.raw, self.raw)
-            except Exception:
-                pass
-        self.raw = None
+        raw, self.raw = self.raw, None
+        if ctx is not None and ctx.raw is not None and raw is not None:
+            with ctx.held():
+                status = ctx.lib.hp_cuda_v1_multilinear_kzg_params_destroy(ctx.raw, raw)
+            _destroy_or_abort("multilinear_kzg_params_destroy", status)
 
 
 class CudaSumCheckProverState:
@@ -177,13 +188,11 @@ class CudaSumCheckProverState:
 
     def __del__(self):
         ctx = self._ctx
-        if ctx is not None and ctx.raw is not None and self.raw is not None:
-            try:
-                with ctx.held():
-                    ctx.lib.hp_cuda_v1_sumcheck_prover_state_destroy(ctx.raw, self.raw)
-            except Exception:
-                pass
-        self.raw = None
+        raw, self.raw = self.raw, None
+        if ctx is not None and ctx.raw is not None and raw is not None:
+            with ctx.held():
+                status = ctx.lib.hp_cuda_v1_sumcheck_prover_state_destroy(ctx.raw, raw)
+            _destroy_or_abort("sumcheck_prover_state_destroy", status)
 
 
 def _addr_array(mles: Sequence[CudaMle]):

@@ -18,10 +18,19 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libhp_cuda.so"
-PROBE_LIB = BUILD / "libhp_probe.so"  # integer-pipe ceilings, read by bench.py
+PROBE_DIR = ROOT / "bench_probe"  # integer-pipe ceilings, read by bench.py (not part of the library)
+PROBE_LIB = PROBE_DIR / "_build" / "libhp_probe.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", f"-I{ROOT / 'include'}"]
+
+
+# CUDA runtime entry points the library's own calls go through
+# csrc/runtime_audit.cpp for (counting and host-side failure injection)
+AUDITED = ["cudaMalloc", "cudaHostAlloc", "cudaMallocHost", "cudaMallocAsync", "cudaMallocFromPoolAsync",
+           "cudaFree", "cudaFreeHost", "cudaFreeAsync", "cudaMemcpy", "cudaMemcpyAsync", "cudaMemset",
+           "cudaMemsetAsync", "cudaStreamSynchronize", "cudaEventSynchronize", "cudaDeviceSynchronize"]
+WRAP_FLAGS = [f"-Xlinker=--wrap={name}" for name in AUDITED]
 
 
 def _nvcc() -> str:
@@ -76,12 +85,13 @@ def build(verbose: bool = False, extra_flags: list[str] | None = None) -> pathli
     objs = [str(BUILD / (s.stem + ".o")) for s in sources()]
     if jobs or not LIB.exists():
         tmp = BUILD / "libhp_cuda.so.tmp"
-        run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *objs])
+        run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *objs, *WRAP_FLAGS])
         os.replace(tmp, LIB)
-    probe_src = CSRC / "probe" / "int_probe.cu"
-    if not PROBE_LIB.exists() or _stale(PROBE_LIB, probe_src, headers):
-        tmp = BUILD / "libhp_probe.so.tmp"
-        run([nvcc, *ARCH, *flags, "-shared", "-cudart", "static", str(probe_src), "-o", str(tmp)])
+    probe_src = PROBE_DIR / "int_probe.cu"
+    if probe_src.exists() and (not PROBE_LIB.exists() or _stale(PROBE_LIB, probe_src, headers)):
+        PROBE_LIB.parent.mkdir(exist_ok=True)
+        tmp = PROBE_LIB.parent / "libhp_probe.so.tmp"
+        run([nvcc, *ARCH, *flags, f"-I{CSRC}", "-shared", "-cudart", "static", str(probe_src), "-o", str(tmp)])
         os.replace(tmp, PROBE_LIB)
     return LIB
 

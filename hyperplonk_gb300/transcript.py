@@ -49,8 +49,9 @@ class MerlinTranscript:
     def __del__(self):
         raw = getattr(self, "raw", None)
         if raw is not None and raw.value:
-            self.lib.hp_host_v1_merlin_free(raw)
             self.raw = None
+            from .backend import _destroy_or_abort
+            _destroy_or_abort("merlin_free", self.lib.hp_host_v1_merlin_free(raw))
 
 
 class IOPTranscript:

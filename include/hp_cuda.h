@@ -226,10 +226,11 @@ HpCudaStatus hp_cuda_v1_mle_evaluate_many(HpCudaContext *ctx, size_t count, cons
                                           uint8_t *out_evaluations);
 /* Evaluation of a resident MLE that allocates no device memory.  No
  * counterpart in the reference.  For callers that cannot call cudaMalloc:
- * hosts that own all device memory through their own pre-reserved arena, or
- * code running inside a CUDA stream capture, where allocation is not allowed.
- * `table` is a device pointer to 2^num_vars Fr in this library's layout (for
- * example an address returned by hp_cuda_v1_mle_upload); `point` holds
+ * hosts that own all device memory through their own pre-reserved arena.
+ * `table` is a device pointer, on the current device, to 2^num_vars Fr in
+ * this library's layout (for example an address returned by
+ * hp_cuda_v1_mle_upload); a host pointer or another device's memory is
+ * InvalidParameters.  `point` holds
  * num_vars canonical Fr; the canonical result goes to out_evaluation (32
  * bytes, host).  Work runs on `stream` (a cudaStream_t; null = the legacy
  * default stream) of the current device, which the call synchronises.
@@ -267,6 +268,16 @@ HpCudaStatus hp_cuda_v1_fixture_random_fr(uint64_t seed, uint64_t first, size_t 
  * tables back to back.  Host-only. */
 HpCudaStatus hp_cuda_v1_fixture_vanilla_plonk(uint64_t seed, size_t num_vars, uint8_t *selectors,
                                               uint8_t *witnesses, uint8_t *permutation);
+/* The same circuit with copy constraints that are not the identity (the
+ * reference's non-identity-permutation end-to-end test,
+ * hyperplonk/src/snark.rs:1008, on this fixture): w2[i] = w1[wire(i)] with
+ * wire(i) = (0x9E3779B97F4A7C15 * i + seed * 0xD1B54A32D192ED03 + 1) mod N (a
+ * bijection: the multiplier is odd), w3 solving the gate, and the
+ * permutation swapping w2 cell i (label N + i) with w1 cell wire(i) (label
+ * wire(i)); w3 cells keep their labels.  Selectors as above.  num_vars >= 1.
+ * Host-only. */
+HpCudaStatus hp_cuda_v1_fixture_vanilla_plonk_wired(uint64_t seed, size_t num_vars, uint8_t *selectors,
+                                                    uint8_t *witnesses, uint8_t *permutation);
 /* Another satisfying witness of the same circuit (serving workload: one
  * circuit per num_vars, independent witnesses per request): selectors from
  * stream `circuit_seed` as above, w1 and w2 from elements [4N, 5N) and
@@ -366,6 +377,46 @@ HpCudaStatus hp_cuda_v1_msm_tuning_query(int32_t mode, size_t size, uint32_t *ou
 HpCudaStatus hp_cuda_v1_msm_tuning_save(const char *path);
 HpCudaStatus hp_cuda_v1_msm_tuning_load(const char *path, const char *device);
 HpCudaStatus hp_cuda_v1_msm_tuning_clear(void);
+
+/* Runtime audit and failure injection (test support; no counterpart in the
+ * reference's bridge -- its native tests wrap the runtime's copy, sync and
+ * allocation calls at link time, backend/src/ascend910b3/native/
+ * CMakeLists.txt:106-116 with tests/runtime_audit.h, and the library does
+ * the same to itself).
+ *
+ * debug_runtime_counters: process-wide counts of the CUDA runtime calls the
+ * library has made since load, by kind; copies are split by direction with
+ * their bytes.  Read them before and after a call and compare.  Needs no
+ * device.
+ *
+ * debug_inject_failure: what = HP_CUDA_INJECT_POOL_ALLOCATION makes the
+ * nth stream-ordered pool allocation from now fail with
+ * cudaErrorMemoryAllocation (nothing is allocated); HP_CUDA_INJECT_SYNCHRONIZE
+ * makes the nth stream / event synchronisation from now complete and then
+ * report cudaErrorLaunchFailure, which the caller sees as an execution
+ * failure (InvalidState) while the device and the context stay usable;
+ * HP_CUDA_INJECT_NONE disarms both.  nth = 0 disarms that kind.  The
+ * environment variable HP_CUDA_FAIL_ALLOC_AT=n arms the allocation failure
+ * when the library loads.  Process wide; for tests only. */
+typedef struct HpCudaRuntimeCounters {
+    uint64_t device_allocs;    /* cudaMalloc */
+    uint64_t host_allocs;      /* cudaHostAlloc, cudaMallocHost */
+    uint64_t pool_allocs;      /* cudaMallocFromPoolAsync, cudaMallocAsync */
+    uint64_t pool_alloc_bytes;
+    uint64_t frees;            /* cudaFree, cudaFreeHost, cudaFreeAsync */
+    uint64_t h2d_copies, h2d_bytes;
+    uint64_t d2h_copies, d2h_bytes;
+    uint64_t d2d_copies, d2d_bytes;
+    uint64_t other_copies, other_bytes;
+    uint64_t memsets;
+    uint64_t syncs;            /* stream, event and device synchronisations */
+    uint64_t injected_failures;
+} HpCudaRuntimeCounters;
+#define HP_CUDA_INJECT_NONE 0
+#define HP_CUDA_INJECT_POOL_ALLOCATION 1
+#define HP_CUDA_INJECT_SYNCHRONIZE 2
+HpCudaStatus hp_cuda_v1_debug_runtime_counters(HpCudaRuntimeCounters *out);
+HpCudaStatus hp_cuda_v1_debug_inject_failure(int32_t what, uint64_t nth);
 
 #ifdef __cplusplus
 }
