@@ -26,8 +26,14 @@ torch.cuda.synchronize() on both sides of the timed loop; a 256 MiB buffer is
 written between steps to flush L2 (the prepared SRS, ~2.6 GB at nv=20, is
 larger than L2 anyway).  The dominant kernel (k_msm_accumulate) is timed by
 the library's own CUDA-event hooks on the same stream.  --impl reference
-times the CPU restatement of the reference's CPU path (oracle, all host
-threads) on a bounded sample of the workload.
+times the CPU restatement of the reference's CPU path (the oracle: its C
+backend, its own prover driver oracle/prover.py and its Python transcript,
+all host threads) on one full step of the same workload at the same size per
+step, with the oracle's own fixture and SRS generators; it loads nothing of
+the product package.
+
+--gpus N without a launcher runs N local ranks through torch.distributed.run
+(replicas, one process per GPU).
 """
 from __future__ import annotations
 
@@ -240,15 +246,17 @@ def _oracle():
 
 class CpuMsmSample:
     """The oracle's multithreaded Pippenger MSM (the CPU restatement of ark-ec
-    msm_unchecked as used by backend/src/cpu/multilinear_kzg.rs:40-59) on a
-    2^log_n-point sample (testing SRS and fixture scalars, seed 0)."""
+    msm_unchecked as used by backend/src/cpu/multilinear_kzg.rs:40-59): one
+    multilinear-KZG commit of 2^nv stream-0 scalars over layer 0 of the
+    oracle's testing SRS of nv variables (seed 0) -- the commit workload at
+    its own size."""
 
-    def __init__(self, log_n: int = 16):
+    def __init__(self, nv: int):
         orc = _oracle()
-        self.orc, self.log_n = orc, log_n
+        self.orc, self.nv = orc, nv
         self.threads = orc.set_threads(0)
-        self.bases = orc.srs_layers(log_n, 0)[0]
-        self.scalars = orc.random_fr(0, 1 << log_n)
+        self.bases = orc.srs_layers(nv, 0)[0]
+        self.scalars = orc.random_fr(0, 1 << nv)
 
     def step(self) -> float:
         t0 = time.perf_counter()
@@ -257,46 +265,43 @@ class CpuMsmSample:
 
 
 class CpuProveSample:
-    """The oracle prover: the same driver over the oracle's CpuBackend
-    (backend/src/cpu restated, multithreaded MSM) and the oracle's Python
-    transcript, on the configuration-3 circuit at 2^nv gates."""
+    """The oracle's own prover (oracle/prover.py: the reference's prover
+    driver restated over the C restatement of backend/src/cpu, with the
+    oracle's Python transcript) proving the full-prove workload's circuit of
+    2^nv gates; fixture and testing SRS from the oracle's generators (or the
+    SRS layers passed in, 96-byte affine).  No product code runs."""
 
-    def __init__(self, nv: int):
-        from hyperplonk_gb300 import snark
+    def __init__(self, nv: int, srs_layers=None, wired: bool = False):
         orc = _oracle()
-        import transcript_ref as tref  # oracle/transcript_ref.py (path set by _oracle)
-        self.snark, self.tcls = snark, tref.OracleIOPTranscript
+        import prover as oprover  # oracle/prover.py (path set by _oracle)
+        self.op, self.nv = oprover, nv
         self.threads = orc.set_threads(0)
         self.cpu = orc.CpuBackend()
-        self.nv = nv
-        sel, self.wit, perm, self.pub = snark.vanilla_fixture(nv, PROVE_SEED)
-        self.pk = snark.preprocess(self.cpu, nv, min(16, 1 << nv), sel, perm, orc.srs_layers(nv, 0), commit=False)
+        sel, self.wit, perm, self.pub = oprover.vanilla_fixture(nv, PROVE_SEED, wired=wired)
+        layers = srs_layers if srs_layers is not None else orc.srs_layers(nv, 0)
+        self.pk = oprover.ProvingKey(self.cpu, nv, min(16, 1 << nv), sel, perm, layers)
 
     def step(self) -> float:
         t0 = time.perf_counter()
-        self.snark.prove(self.cpu, self.pk, self.pub, self.wit, transcript_cls=self.tcls).to_bytes()
+        self.proof = self.op.prove(self.cpu, self.pk, self.pub, self.wit)
         return time.perf_counter() - t0
 
 
 class CpuSumcheckSample:
     """The oracle's sumcheck prover (backend/src/cpu/sum_check.rs restated)
-    with the oracle's Python transcript, on the degree-2 instance at 2^nv."""
+    driven by oracle/prover.py with the oracle's Python transcript, on the
+    degree-2 instance at 2^nv (seed 1)."""
 
-    def __init__(self, nv: int):
-        from hyperplonk_gb300 import protocol, workloads
+    def __init__(self, nv: int, seed: int = 1):
         orc = _oracle()
-        import transcript_ref as tref  # oracle/transcript_ref.py (path set by _oracle)
-        self.protocol, self.workloads, self.tcls = protocol, workloads, tref.OracleIOPTranscript
+        import prover as oprover
+        self.op, self.nv, self.seed = oprover, nv, seed
         self.threads = orc.set_threads(0)
-        self.cpu = orc.CpuBackend()
-        self.nv = nv
-        self.mles = [self.cpu.mle_from_evaluations(nv, t) for t in workloads.sumcheck_tables(nv, 1)]
-        self.coefs = workloads.sumcheck_coefficients(1)
+        self.instance = oprover.sumcheck_instance(nv, seed)
 
     def step(self) -> float:
         t0 = time.perf_counter()
-        vp = self.workloads.sumcheck_polynomial(self.nv, self.mles, self.coefs)
-        self.protocol.sumcheck_prove(self.cpu, vp, self.tcls(self.workloads.SUMCHECK_LABEL), [])
+        self.op.sumcheck_prove_instance(self.nv, self.seed, self.instance)
         return time.perf_counter() - t0
 
 
@@ -369,7 +374,7 @@ class Session:
 
     def wide_rate(self) -> float:
         """mad.wide.u32 (32x32->64 multiply-add) issues per second on this GPU."""
-        probe = ctypes.CDLL(str(ROOT / "hyperplonk_gb300" / "_build" / "libhp_probe.so"))
+        probe = ctypes.CDLL(str(ROOT / "bench_probe" / "_build" / "libhp_probe.so"))
         probe.hp_probe_wide_rate.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
         w = ctypes.c_double()
         rc = probe.hp_probe_wide_rate(self.local, ctypes.byref(w))
@@ -378,7 +383,7 @@ class Session:
         return w.value
 
     def integer_rates(self):
-        probe = ctypes.CDLL(str(ROOT / "hyperplonk_gb300" / "_build" / "libhp_probe.so"))
+        probe = ctypes.CDLL(str(ROOT / "bench_probe" / "_build" / "libhp_probe.so"))
         probe.hp_probe_integer_rates.argtypes = [ctypes.c_int] + [ctypes.POINTER(ctypes.c_double)] * 3
         imad, fqm, frm = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         rc = probe.hp_probe_integer_rates(self.local, ctypes.byref(imad), ctypes.byref(fqm), ctypes.byref(frm))
@@ -689,7 +694,7 @@ def run_gb300(args, world, rank, local, pg):
         from hyperplonk_gb300 import snark
         sel, wit, perm, pub = snark.vanilla_fixture(nv, PROVE_SEED)
         pk = snark.preprocess(be, nv, min(16, n), sel, perm, layers, commit=False)
-        del layers, sel, perm
+        del sel, perm
         opening = [nv - 1 - i for i in range(nv)]  # the batch opening's quotient MSMs
         autotune(args, be, pk.pcs_param, [nv] + [k for k in opening if k >= 10], shared_mix(opening))
         pinned = [s.pinned(w) for w in wit]
@@ -736,6 +741,27 @@ def run_gb300(args, world, rank, local, pg):
         for _ in range(3):
             snark.prove(be, pk, pub, None, witness_mles=resident, phases=phases)
         extra["phases_ms"] = {k: 1e3 * v / 3 for k, v in phases.items()}
+        # the same circuit with copy constraints that are not the identity:
+        # frac and prod hold random fractions, so their commitments take the
+        # full MSM (the identity permutation's 0/1 tables take the
+        # sum-of-bases path); same SRS, witnesses resident
+        wsel, wwit, wperm, wpub = snark.vanilla_fixture(nv, PROVE_SEED, wired=True)
+        wpk = snark.ProvingKey(nv, min(16, n), snark.VANILLA_GATE, pk.pcs_param,
+                               [be.mle_from_evaluations(nv, t) for t in wsel],
+                               [be.mle_from_evaluations(nv, t) for t in wperm])
+        wres = [be.mle_from_evaluations(nv, t) for t in wwit]
+        del wsel, wwit, wperm
+        wfn = lambda: snark.prove(be, wpk, wpub, None, witness_mles=wres).to_bytes()  # noqa: E731
+        for _ in range(2):
+            wfn()
+        s.torch.cuda.synchronize()
+        wper = s.timed(wfn, max(3, args.steps))
+        extra["general_circuit"] = {
+            "workload": "the same circuit with non-identity copy constraints (w2[i] = w1[wire(i)], "
+                        "hp_cuda_v1_fixture_vanilla_plonk_wired), witnesses resident",
+            "proofs_per_s": world / max_over_ranks(pg, statistics.mean(wper)),
+            "ms_per_proof": 1e3 * statistics.mean(wper), "p50_ms": 1e3 * statistics.median(wper)}
+        del wpk, wres
 
     step_s = max_over_ranks(pg, statistics.mean(per))
     e2e_s = max_over_ranks(pg, statistics.mean(per_e2e))
@@ -791,89 +817,89 @@ def run_gb300(args, world, rank, local, pg):
     result["msm_total"] = {"ms": msm_ms, "accounting_imad": msm_accounting_imad(n),
                            "frac_of_imad_peak": msm_accounting_imad(n) / (msm_ms / 1e3) / imad if msm_ms else None}
     if rank == 0 and not args.no_cpu_baseline:
-        result["cpu_baseline"] = cpu_baseline(args.workload, nv)
+        result["cpu_baseline"] = cpu_baseline(args.workload, nv, layers if args.workload == "prove" else None)
     if rank == 0:
         print(json.dumps(result))
 
 
-def cpu_baseline(workload: str, nv: int) -> dict:
+def cpu_baseline(workload: str, nv: int, srs_layers=None) -> dict:
+    """The oracle on this host's cores, on one step of the same workload at
+    the same size (`srs_layers`: the SRS the GPU arm used, as packets, to skip
+    regenerating it on the CPU; the oracle's own SRS is byte-identical)."""
     if workload == "commit":
-        sample = CpuMsmSample(16)
+        sample = CpuMsmSample(nv)
         per = statistics.median([sample.step() for _ in range(3)])
-        return {"value": (1 << 16) / per, "unit": "pts/s", "cores": sample.threads, "kind": "port",
-                "sample": f"oracle Pippenger MSM of 2^16 points (testing SRS nv=16, fixture seed 0), median of 3, "
+        return {"value": (1 << nv) / per, "unit": "pts/s", "cores": sample.threads, "kind": "port",
+                "sample": f"oracle Pippenger MSM of 2^{nv} points (the commit at its size), median of 3, "
                           f"{per:.3f} s each"}
     if workload == "sumcheck":
-        snv = min(nv, 18)
-        sample = CpuSumcheckSample(snv)
+        sample = CpuSumcheckSample(nv)
         per = statistics.median([sample.step() for _ in range(3)])
-        scale = 1 << (nv - snv)
-        return {"value": 1.0 / (per * scale), "unit": "proofs/s", "cores": sample.threads, "kind": "port",
-                "sample": f"oracle sumcheck prover on the same instance at 2^{snv}, median of 3 = {per:.2f} s, "
-                          f"scaled linearly by {scale} to 2^{nv}"}
-    snv = min(nv, 16)  # oracle prove time is linear in gates from 2^16 up (2.9 s at 16, 11.4 s at 18)
-    sample = CpuProveSample(snv)
-    per = statistics.median([sample.step() for _ in range(2)])
-    scale = 1 << (nv - snv)
-    return {"value": 1.0 / (per * scale), "unit": "proofs/s", "cores": sample.threads, "kind": "port",
-            "sample": f"oracle prover (CPU backend restatement + Python transcript) on the same circuit at 2^{snv} "
-                      f"gates, median of 2 = {per:.2f} s, scaled linearly by {scale} to 2^{nv} gates"}
+        return {"value": 1.0 / per, "unit": "proofs/s", "cores": sample.threads, "kind": "port",
+                "sample": f"oracle sumcheck prove of the same instance at 2^{nv}, median of 3 = {per:.2f} s"}
+    orc = _oracle()
+    layers = None if srs_layers is None else [orc.packets_to_affine(l) for l in srs_layers]
+    sample = CpuProveSample(nv, layers)
+    per = sample.step()
+    return {"value": 1.0 / per, "unit": "proofs/s", "cores": sample.threads, "kind": "port",
+            "sample": f"one oracle proof of the same circuit at 2^{nv} gates ({per:.2f} s): oracle/prover.py over "
+                      f"the oracle's C backend, Python transcript"}
 
 
 def _profile_traffic(nv: int):
-    """DRAM bytes per k_msm_accumulate launch from the committed ncu summary
-    (profiles/msm_accumulate_commit.md, line 'traffic_bytes_per_launch nv=<k>:
-    <bytes>'), scaled to 2^nv points by the (point, window) record count --
-    each record reads one 96-byte base -- when captured at a smaller size;
-    None if absent."""
+    """DRAM bytes (read + write) of one k_msm_accumulate launch of a 2^nv
+    commit, from the committed ncu summary of that kernel at that size
+    (profiles/msm_accumulate_commit.md, line 'traffic_bytes_per_launch
+    nv=<k>: <bytes>'); None when no capture at this size exists."""
     p = ROOT / "profiles" / "msm_accumulate_commit.md"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
-        if line.startswith("traffic_bytes_per_launch"):
+        if line.startswith(f"traffic_bytes_per_launch nv={nv}:"):
             try:
-                k = int(line.split("nv=")[1].split(":")[0])
-                b = float(line.split(":")[1].strip().split()[0])
-                rec = lambda v: math.ceil(256 / window_bits(1 << v)) * (1 << v)  # noqa: E731
-                return b * rec(nv) / rec(k)
+                return float(line.split(":")[1].strip().split()[0])
             except (IndexError, ValueError):
                 return None
     return None
 
 
 def run_reference(args, world, rank):
+    """The reference arm: the oracle (the C restatement of the reference's
+    CPU backend with the oracle's own prover driver and transcript; the
+    reference's Rust/arkworks path cannot be built here) on every host core,
+    one full step of the workload at its stated size per step, fixtures and
+    SRS from the oracle's own generators.  Imports nothing of the product."""
     if rank != 0:
         return
-    nv = args.num_vars or (22 if args.workload == "batch" else 20)
+    nv = args.num_vars or (22 if args.workload == "batch" else 16 if args.workload == "commit" else 20)
+    t_setup = time.perf_counter()
     if args.workload == "batch":
-        return run_reference_batch(args, world, nv)
-    if args.workload == "commit":
-        sample, units, metric, unit, snv = CpuMsmSample(16), 1 << 16, "MSM pts/s", "pts/s", 16
-        desc = "oracle Pippenger MSM of 2^16 points per step"
-        scale = 1
+        sample, units, metric, unit = CpuBatchSample(nv), 1, "batch-plan runs/s", "runs/s"
+        desc = f"the whole batch plan (seed 3, SRS nv={nv}) on the oracle per step"
+    elif args.workload == "commit":
+        sample, units, metric, unit = CpuMsmSample(nv), 1 << nv, "MSM pts/s", "pts/s"
+        desc = f"oracle Pippenger MSM of 2^{nv} points (one commit) per step"
     elif args.workload == "sumcheck":
-        snv = min(nv, 18)
-        sample, units, metric, unit = CpuSumcheckSample(snv), 1, "sumcheck proofs/s", "proofs/s"
-        scale = 1 << (nv - snv)
-        desc = (f"oracle sumcheck prover on the degree-2 instance at 2^{snv} per step, throughput scaled "
-                f"linearly by {scale} to 2^{nv}")
+        sample, units, metric, unit = CpuSumcheckSample(nv), 1, "sumcheck proofs/s", "proofs/s"
+        desc = f"oracle sumcheck prove of the degree-2 instance at 2^{nv} per step"
     else:
-        snv = min(nv, 16)  # oracle prove time is linear in gates from 2^16 up (2.9 s at 16, 11.4 s at 18)
-        sample, units, metric, unit = CpuProveSample(snv), 1, "HyperPlonk proofs/s", "proofs/s"
-        scale = 1 << (nv - snv)
-        desc = (f"oracle prover on the configuration-3 circuit at 2^{snv} gates per step, throughput scaled "
-                f"linearly by {scale} to 2^{nv} gates")
+        sample, units, metric, unit = CpuProveSample(nv), 1, "HyperPlonk proofs/s", "proofs/s"
+        desc = f"one oracle proof of the configuration-3 circuit at 2^{nv} gates per step"
+    setup_s = time.perf_counter() - t_setup
     for _ in range(args.warmup):
         sample.step()
     per = [sample.step() for _ in range(args.steps)]
-    step = sum(per) / len(per) * scale
+    step = sum(per) / len(per)
     v = units / step
     print(json.dumps({
         "impl": "reference", "metric": metric, "value": v, "unit": unit, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64 limbs (Montgomery)",
         "data": "synthetic: ChaCha20 fixture streams, oracle testing SRS",
-        "config": {"workload": f"{args.workload}, num_vars={nv}: bounded CPU sample (2^{snv})", "num_vars": nv},
+        "config": {"workload": f"{args.workload}, num_vars={nv}, full size", "num_vars": nv},
+        "latency_ms": {"p50": 1e3 * statistics.median(per), "min": 1e3 * min(per), "max": 1e3 * max(per)},
+        "setup_s": round(setup_s, 2),
+        "product_code_loaded": sorted(m for m in sys.modules if m.startswith("hyperplonk_gb300")),
         "cpu_baseline": {"value": v, "unit": unit, "cores": sample.threads, "kind": "port",
                          "sample": desc + " (the reference's Rust/arkworks CPU path cannot be built here: no cargo, "
                                           "arkworks not vendored)"},
@@ -881,36 +907,51 @@ def run_reference(args, world, rank):
     }))
 
 
-def run_reference_batch(args, world, nv_srs):
-    """The batch plan on the oracle, estimated from timed 2^16 samples: every
-    MSM scaled linearly by its point count from a 2^16-point oracle MSM, every
-    sumcheck by its table size from a 2^16 oracle sumcheck prove."""
-    from hyperplonk_gb300 import workloads
-    ks, nvs = workloads.batch_plan(3, msm_k=(12, nv_srs), sumcheck_nv=(14, nv_srs))
-    msm, sc = CpuMsmSample(16), CpuSumcheckSample(16)
-    for _ in range(args.warmup):
-        msm.step()
-        sc.step()
-    t_msm = statistics.mean([msm.step() for _ in range(args.steps)])
-    t_sc = statistics.mean([sc.step() for _ in range(args.steps)])
-    step = sum(t_msm * (1 << k) / (1 << 16) for k in ks) + sum(t_sc * (1 << v) / (1 << 16) for v in nvs)
-    v = 1.0 / step
-    print(json.dumps({
-        "impl": "reference", "metric": "batch-plan runs/s", "value": v, "unit": "runs/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u64 limbs (Montgomery)",
-        "data": "synthetic: ChaCha20 fixture streams, oracle testing SRS",
-        "config": {"workload": f"batch plan seed 3 (SRS nv={nv_srs}), estimated from 2^16 oracle samples",
-                   "num_vars": nv_srs},
-        "cpu_baseline": {"value": v, "unit": "runs/s", "cores": msm.threads, "kind": "port",
-                         "sample": f"oracle MSM 2^16 ({t_msm:.3f} s) and oracle sumcheck 2^16 ({t_sc:.3f} s), "
-                                   "each scaled linearly to the plan's sizes"},
-        "e2e": {"value": v, "unit": "runs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }))
+class CpuBatchSample:
+    """The batch plan on the oracle: every MSM over its prefix of layer 0 of
+    the oracle's SRS of nv_srs variables and every sumcheck prove, one after
+    another (the oracle parallelises inside each)."""
+
+    def __init__(self, nv_srs: int):
+        orc = _oracle()
+        import prover as oprover
+        self.orc, self.op = orc, oprover
+        self.threads = orc.set_threads(0)
+        self.layer0 = orc.srs_layers(nv_srs, 0)[0]
+        self.ks, self.nvs = oprover.batch_plan(3, msm_k=(12, nv_srs), sumcheck_nv=(14, nv_srs))
+        self.scalars = oprover.batch_msm_scalars(self.ks, 3)
+        self.instances = [oprover.sumcheck_instance(v, 103 + i) for i, v in enumerate(self.nvs)]
+
+    def step(self) -> float:
+        t0 = time.perf_counter()
+        for k, sc in zip(self.ks, self.scalars):
+            self.orc.msm(self.layer0[:96 << k], sc)
+        for i, (v, inst) in enumerate(zip(self.nvs, self.instances)):
+            self.op.sumcheck_prove_instance(v, 103 + i, inst)
+        return time.perf_counter() - t0
+
+
+def relaunch(n: int) -> int:
+    """`--gpus N` without a launcher: run this command as N local ranks
+    (torch.distributed.run on 127.0.0.1, one process per GPU) and return the
+    launcher's exit status."""
+    import socket
+    with socket.socket() as sock:
+        sock.bind(("127.0.0.1", 0))
+        port = sock.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), str(pathlib.Path(__file__).resolve()),
+           *sys.argv[1:]]
+    return subprocess.call(cmd)
 
 
 def main():
     args = parse()
+    launched = os.environ.get("WORLD_SIZE")
+    if launched is None and args.gpus > 1:
+        sys.exit(relaunch(args.gpus))
+    if launched is not None and int(launched) != args.gpus:
+        sys.exit(f"bench.py: --gpus {args.gpus} under a launcher of WORLD_SIZE {launched}")
     world, rank, local, pg = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)

@@ -1,13 +1,13 @@
 // int_probe.cu -- measures the integer-pipe ceilings the MSM and field
 // kernels are held against: the 32-bit multiply-add (IMAD) issue rate and the
 // Fq / Fr Montgomery multiplication rate of field.cuh, on the current GPU.
-// Built as libhp_probe.so beside libhp_cuda.so; used by bench.py only to
+// Built as bench_probe/_build/libhp_probe.so; used by bench.py only to
 // report a roofline denominator (no product path calls it).
 #include <cuda_runtime.h>
 
 #include <cstdint>
 
-#include "../field.cuh"
+#include "field.cuh"
 
 namespace {
 

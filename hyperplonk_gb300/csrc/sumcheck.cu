@@ -285,6 +285,127 @@ __global__ void HP_WIDE_BOUNDS k_sumcheck_round_wide(SumcheckDesc desc, FrPtrLis
     finish_round_in_last_block(desc, partials, blocks_per_slot, counter, weights, degree, out, sums);
 }
 
+// One thread per (product, pair) item, for the large rounds (more than
+// wide_max_pairs() pairs) of products of arity <= 3: the thread loads its
+// product's m factor rows at its pair once and evaluates all m + 1 slot
+// values of the product (t = 0..m) from those registers.  Per pair, 2m Fr
+// loads feed m + 1 products of m factors, where a (slot, pair) item loads 2m
+// Fr for one.  With `fold` the thread folds its factors with r on the way
+// (the item at a factor's first occurrence, desc.writer, stores the folded
+// pair, so every folded table is written exactly once); that form re-folds a
+// factor once per product reading it and stays opt-in (HP_SUMCHECK_PP_FOLD):
+// by default the separate fold pass runs first.  Products of arity <= 2 keep
+// their slot sums unreduced (17-limb accumulators, one Montgomery reduction
+// per thread at the end); arity 3 keeps reduced sums.  Blocks interleave
+// products (block b: product b % P) so that products sharing a factor read
+// its rows from L2.  One partial per (slot, block), slot-major; the last
+// block finishes the round.  Measured on GB300 (degree-2 sumcheck, 6 tables
+// of 2^20, round 1): 138 us against 161 us for the (slot, pair) kernel; the
+// middle rounds stay with the (slot, pair) kernel, whose shorter per-thread
+// chains hide latency better at a few thousand pairs.
+constexpr int kPpThreads = 128;
+constexpr int kPpBlocksPerSm = HP_ROUND_BLOCKS_PER_SM;
+
+// (HP_PP_MINBLOCKS: a minimum-blocks-per-SM bound, a tuning hook)
+#ifdef HP_PP_MINBLOCKS
+#define HP_PP_BOUNDS __launch_bounds__(kPpThreads, HP_PP_MINBLOCKS)
+#else
+#define HP_PP_BOUNDS __launch_bounds__(kPpThreads)
+#endif
+
+template <int MAXM>
+__global__ void HP_PP_BOUNDS k_sumcheck_round_pp(SumcheckDesc desc, FrPtrList src, FrMutPtrList dst,
+                                                                  bool fold, Fr r, size_t pairs,
+                                                                  int blocks_per_product, Fr *partials,
+                                                                  unsigned *counter, const Fr *weights, int degree,
+                                                                  Fr *out) {
+    constexpr bool kUnreduced = MAXM <= 2;
+    extern __shared__ Fr sums[];  // S slot sums, used by the last block
+    __shared__ Fr wsum[kPpThreads / 32][MAXM + 1];
+    const int P = desc.product_count;
+    const int p = int(blockIdx.x % unsigned(P)), blk = int(blockIdx.x / unsigned(P));
+    const int begin = desc.offsets[p], m = desc.offsets[p + 1] - begin, slot0 = desc.slot_base[p];
+    FrAcc X[kUnreduced ? MAXM + 1 : 1];
+    Fr A[kUnreduced ? 1 : MAXM + 1];
+#pragma unroll
+    for (int t = 0; t <= MAXM; t++) {
+        if constexpr (kUnreduced) acc_zero(X[t]);
+        else A[t] = Fr::zero();
+    }
+    const size_t stride = size_t(blocks_per_product) * kPpThreads;
+    for (size_t b = size_t(blk) * kPpThreads + threadIdx.x; b < pairs; b += stride) {
+        Fr e[MAXM], st[MAXM];
+#pragma unroll
+        for (int j = 0; j < MAXM; j++) {
+            if (j < m) {
+                const int f = desc.indices[begin + j];
+                Fr lo, hi;
+                if (fold) {
+                    const Fr *q = src.p[f] + 4 * b;
+                    const Fr a0 = load_fr(q), a1 = load_fr(q + 1), a2 = load_fr(q + 2), a3 = load_fr(q + 3);
+                    lo = a0 + r * (a1 - a0);
+                    hi = a2 + r * (a3 - a2);
+                    if (desc.writer[f] == begin + j) {
+                        Fr *d = dst.p[f] + 2 * b;
+                        store_fr(d, lo);
+                        store_fr(d + 1, hi);
+                    }
+                } else {
+                    const Fr *q = src.p[f] + 2 * b;
+                    lo = load_fr(q);
+                    hi = load_fr(q + 1);
+                }
+                e[j] = lo;
+                st[j] = hi - lo;
+            }
+        }
+#pragma unroll
+        for (int t = 0; t <= MAXM; t++) {
+            if (t <= m) {
+                if (t > 0) {
+#pragma unroll
+                    for (int j = 0; j < MAXM; j++)
+                        if (j < m) e[j] = e[j] + st[j];  // factor j at node t
+                }
+                Fr v;
+#pragma unroll
+                for (int j = 0; j < MAXM; j++) {
+                    if (j + 1 < m) {
+                        v = j == 0 ? e[0] : v * e[j];
+                    } else if (j + 1 == m) {  // the last factor goes into the slot sum
+                        if constexpr (kUnreduced) {
+                            if (j == 0) acc_add_shifted(X[t], e[0]);
+                            else acc_mul_add(X[t], v, e[j]);
+                        } else {
+                            A[t] = A[t] + (j == 0 ? e[0] : v * e[j]);
+                        }
+                    }
+                }
+            }
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int t = 0; t <= MAXM; t++) {
+        if (t <= m) {
+            Fr a;
+            if constexpr (kUnreduced) a = acc_reduce(X[t]);
+            else a = A[t];
+            a = warp_sum(a);
+            if (lane == 0) wsum[warp][t] = a;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x <= m) {
+        const int t = threadIdx.x;
+        Fr a = wsum[0][t];
+#pragma unroll
+        for (int w = 1; w < kPpThreads / 32; w++) a = a + wsum[w][t];
+        partials[size_t(slot0 + t) * blocks_per_product + blk] = a;
+    }
+    finish_round_in_last_block(desc, partials, blocks_per_product, counter, weights, degree, out, sums);
+}
+
 // Given the slot sums (Montgomery, shared memory) of a round, writes the d+1
 // canonical round evaluations out[x] = sum_s W[x][s] * sums[s], one warp per
 // x.  W (per prover state, built on the host) holds for slot
@@ -580,6 +701,8 @@ static void check_round(HpCudaSumCheckProverState *s, const uint8_t *challenge_o
 
 static size_t wide_max_pairs();
 static size_t wide_min_pairs();
+static bool product_pair_rounds();
+static bool fused_fold_pp();
 static bool big_slot_rounds();
 static size_t big_blocks_per_sm();
 static int separate_fold_arity();
@@ -621,6 +744,41 @@ static void enqueue_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, cons
             // (GB300, nv = 20: arity-4/5 middle rounds 56-60 -> 35-43 us)
             separate_fold = !all_written || d.max_arity >= separate_fold_arity();
         }
+    }
+    if (d.product_count > 0 && pairs > wide_max_pairs() && d.max_arity <= 3 && d.slot_count <= kMaxSlotsV2 &&
+        product_pair_rounds()) {
+        int tok = ctx->prof_begin("sumcheck_round", st);
+        FrPtrList tables = src;
+        bool fused_fold = fold;
+        if (fold && (!all_written || !fused_fold_pp())) {
+            // fold every table first (a factor no product reads has no writer)
+            int log_half = 0;
+            while ((size_t(1) << log_half) < 2 * pairs) log_half++;
+            const size_t total = size_t(d.factor_count) << log_half;
+            const size_t sms = size_t(ctx->sm_count > 0 ? ctx->sm_count : 152);
+            const unsigned fgrid = unsigned(std::max<size_t>(1, std::min<size_t>((total + 255) / 256, sms * 8)));
+            k_sumcheck_fold<<<fgrid, 256, 0, st>>>(src, dst, d.factor_count, log_half, r);
+            check_launch();
+            tables = rd;
+            fused_fold = false;
+        }
+        const size_t P = size_t(d.product_count);
+        const size_t tiles = (pairs + kPpThreads - 1) / kPpThreads;
+        const size_t target = size_t(ctx->sm_count > 0 ? ctx->sm_count : 152) * kPpBlocksPerSm;
+        const int bpp = int(std::max<size_t>(1, std::min(tiles, (target + P - 1) / P)));
+        const unsigned grid = unsigned(P) * unsigned(bpp);
+        Scratch spill;
+        Fr *partials = round_partials(ctx, s, size_t(d.slot_count) * size_t(bpp) * sizeof(Fr), spill, st);
+        const size_t smem = size_t(d.slot_count) * sizeof(Fr);
+        auto launch = [&](auto kernel) {
+            kernel<<<grid, kPpThreads, smem, st>>>(d, tables, dst, fused_fold, r, pairs, bpp, partials,
+                                                   round_counter(s), state_weights(s), int(s->max_degree), out_dev);
+        };
+        if (d.max_arity <= 2) launch(k_sumcheck_round_pp<2>);
+        else launch(k_sumcheck_round_pp<3>);
+        check_launch();
+        ctx->prof_end(tok, st);
+        return;
     }
     if (use_slots) {
         int tok = ctx->prof_begin("sumcheck_round", st);
@@ -722,6 +880,21 @@ static size_t wide_min_pairs() {
 }
 static int separate_fold_arity() {
     static const int v = int(env_size("HP_SEPARATE_FOLD_ARITY", 3));
+    return v;
+}
+// Rounds of more than kSmallPairs pairs over products of arity <= 8 take the
+// (product, pair) kernel; HP_SUMCHECK_PP=0 restores the (slot, pair) and
+// per-pair kernels below for them.
+static bool product_pair_rounds() {
+    static const bool v = env_size("HP_SUMCHECK_PP", 1) != 0;
+    return v;
+}
+// HP_SUMCHECK_PP_FOLD=1: the (product, pair) kernel folds its own factors
+// (each factor re-folded once per product that reads it) instead of the
+// separate fold pass.  Off by default: measured on GB300 at 2^19 pairs, the
+// fused form took 225 us for round 2 against 82 + ~70 us for fold + round.
+static bool fused_fold_pp() {
+    static const bool v = env_size("HP_SUMCHECK_PP_FOLD", 0) != 0;
     return v;
 }
 // Rounds above wide_max_pairs(): k_sumcheck_fold + the (slot, pair) kernel
