@@ -85,6 +85,7 @@ SIGNATURES: dict[str, list] = {
     "hp_cuda_v1_fixture_vanilla_plonk": [ctypes.c_uint64, c_size, c_u8p, c_u8p, c_u8p],
     "hp_cuda_v1_fixture_vanilla_plonk_witness": [ctypes.c_uint64, ctypes.c_uint64, c_size, c_u8p],
     "hp_cuda_v1_fixture_vanilla_plonk_wired": [ctypes.c_uint64, c_size, c_u8p, c_u8p, c_u8p],
+    "hp_cuda_v1_context_memory": [c_voidp, ctypes.c_int32, ctypes.POINTER(ctypes.c_uint64)],
     "hp_cuda_v1_debug_runtime_counters": [ctypes.POINTER(RuntimeCounters)],
     "hp_cuda_v1_debug_inject_failure": [ctypes.c_int32, ctypes.c_uint64],
     "hp_host_v1_merlin_new": [c_u8p, c_size, c_voidpp],

@@ -127,6 +127,13 @@ class CudaContext:
         check_status(self.lib.hp_cuda_v1_context_stream(self.raw, ctypes.byref(out)), "context_stream")
         return out.value or 0
 
+    def memory(self, reset_high: bool = False) -> tuple[int, int, int]:
+        """(bytes in use, high-water mark since the last reset, bytes held)
+        of the context's memory pool (hp_cuda_v1_context_memory)."""
+        out = (ctypes.c_uint64 * 3)()
+        check_status(self.lib.hp_cuda_v1_context_memory(self.raw, 1 if reset_high else 0, out), "context_memory")
+        return int(out[0]), int(out[1]), int(out[2])
+
     def close(self) -> None:
         if self.raw is not None and self.raw.value:
             check_status(self.lib.hp_cuda_v1_context_destroy(self.raw), "context_destroy")

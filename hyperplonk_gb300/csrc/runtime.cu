@@ -269,6 +269,24 @@ extern "C" HpCudaStatus hp_cuda_v1_context_profile_read(HpCudaContext *ctx, cons
     });
 }
 
+extern "C" HpCudaStatus hp_cuda_v1_context_memory(HpCudaContext *ctx, int32_t reset_high, uint64_t *out3) {
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(out3 != nullptr);
+        uint64_t used = 0, high = 0, reserved = 0;  // the attributes are 64-bit values
+        check_cuda(cudaMemPoolGetAttribute(ctx->pool, cudaMemPoolAttrUsedMemCurrent, &used));
+        check_cuda(cudaMemPoolGetAttribute(ctx->pool, cudaMemPoolAttrUsedMemHigh, &high));
+        check_cuda(cudaMemPoolGetAttribute(ctx->pool, cudaMemPoolAttrReservedMemCurrent, &reserved));
+        out3[0] = used;
+        out3[1] = high;
+        out3[2] = reserved;
+        if (reset_high) {
+            uint64_t zero = 0;  // resets the mark to the current use
+            check_cuda(cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrUsedMemHigh, &zero));
+        }
+    });
+}
+
 static std::atomic<uint64_t> g_kernel_launches{0};
 
 void hp::count_launch() { g_kernel_launches.fetch_add(1, std::memory_order_relaxed); }

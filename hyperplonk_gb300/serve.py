@@ -9,8 +9,11 @@ each circuit size; witness MLEs and every derived table stay on the device
 for the life of a proof.
 
 Admission: a request is admitted to the lane with the fewest proofs in flight
-when its HBM estimate fits the budget and the lane has a free slot;
-otherwise it waits in arrival order.  Requests that arrive while others are
+when its device memory fits the budget and the lane has a free slot;
+otherwise it waits in arrival order.  A request's memory is the measured
+high-water mark of one proof of its size alone (ProofServer.prepare with
+measure=True: the lane context's pool high-water mark over one proof, minus
+the memory in use before it), else a table-count upper estimate.  Requests that arrive while others are
 on the GPU start as soon as memory and slots free up.
 
 Coalescing: each in-flight proof runs the unchanged prover driver
@@ -41,10 +44,12 @@ from . import snark
 from .backend import CudaBackend
 from .errors import InvalidParameters
 
-# Device bytes one in-flight proof of 2^nv gates may hold, in Fr tables of 2^nv:
-# 3 witnesses, 6 nums/denoms, frac, prod, 2 product factors, eq tables, the
-# sumcheck fold slots of both zero-checks and the batch opening, merged
-# opening polynomials and MSM scratch; an upper estimate, not a measurement.
+# Device bytes one in-flight proof of 2^nv gates may hold, in Fr tables of 2^nv,
+# for sizes whose use has not been measured: 3 witnesses, 6 nums/denoms,
+# frac, prod, 2 product factors, eq tables, the sumcheck fold slots of both
+# zero-checks and the batch opening, merged opening polynomials and MSM
+# scratch -- an upper estimate (prepare(measure=True) replaces it by the
+# measured high-water mark of one proof).
 TABLES_PER_PROOF = 64
 
 
@@ -164,6 +169,20 @@ class Lane:
         except Exception as e:  # noqa: BLE001 -- re-raised in the proof thread
             op.error = e
 
+    def measure_proof_memory(self, num_vars: int, circuit_seed: int, num_pub: int) -> int:
+        """Device bytes one proof of this size takes on this lane's context at
+        its peak: the pool's high-water mark over one proof of the circuit's
+        own witness, run alone, minus the bytes in use before it."""
+        pk = self.proving_key(num_vars, circuit_seed, num_pub)
+        wit = snark.vanilla_witness(num_vars, circuit_seed, circuit_seed)
+        pub = [int.from_bytes(wit[0][32 * i:32 * i + 32].tobytes(), "little") for i in range(pk.num_pub_input)]
+        with self.mutex:
+            ctx = self.backend.ctx
+            before, _, _ = ctx.memory(reset_high=True)
+            snark.prove(self.backend, pk, pub, wit)
+            _, high, _ = ctx.memory()
+        return max(0, high - before)
+
     # -- circuits -----------------------------------------------------------
     def proving_key(self, num_vars: int, circuit_seed: int, num_pub: int) -> snark.ProvingKey:
         key = (num_vars, circuit_seed, num_pub)
@@ -250,22 +269,32 @@ class ProofServer:
             hbm_budget_bytes = free // 2
         self.stats = {"flushes": 0, "coalesced_calls": 0}
         self.budget = hbm_budget_bytes
+        self.measured: dict[int, int] = {}  # num_vars -> device bytes of one proof (prepare(measure=True))
         self.in_use = 0
         self.lock = threading.Lock()
         self.queue: list[Ticket] = []
         self.tickets: list[Ticket] = []
         self.threads: list[threading.Thread] = []
 
-    def prepare(self, num_vars_list) -> None:
-        """Upload the circuit oracles of these sizes to every lane ahead of requests."""
+    def prepare(self, num_vars_list, measure: bool = False) -> None:
+        """Upload the circuit oracles of these sizes to every lane ahead of
+        requests; with `measure`, also measure each size's device memory per
+        proof (one proof alone on the first lane) for admission."""
         for lane in self.lanes:
             for nv in num_vars_list:
                 lane.proving_key(nv, self.circuit_seed, self.num_pub)
+        if measure:
+            for nv in sorted(set(num_vars_list)):
+                self.measured[nv] = self.lanes[0].measure_proof_memory(nv, self.circuit_seed, self.num_pub)
+
+    def proof_bytes(self, num_vars: int) -> int:
+        """Device memory admission counts for one proof of this size."""
+        return self.measured.get(num_vars) or proof_hbm_estimate(num_vars)
 
     def submit(self, num_vars: int, witnesses: list, pub: list) -> int:
         if not 0 < num_vars <= self.nv_max:
             raise InvalidParameters(f"num_vars {num_vars} outside 1..{self.nv_max}")
-        if proof_hbm_estimate(num_vars) > self.budget:
+        if self.proof_bytes(num_vars) > self.budget:
             raise InvalidParameters("request does not fit the HBM budget")
         t = Ticket(num_vars, witnesses, pub, time.perf_counter())
         with self.lock:
@@ -297,7 +326,7 @@ class ProofServer:
     def _admit(self) -> None:
         while self.queue:
             t = self.queue[0]
-            need = proof_hbm_estimate(t.num_vars)
+            need = self.proof_bytes(t.num_vars)
             lane_i = min(range(len(self.lanes)), key=lambda i: self.lanes[i].inflight)
             lane = self.lanes[lane_i]
             if self.in_use + need > self.budget or lane.inflight >= self.slots_per_lane:

@@ -327,6 +327,12 @@ HpCudaStatus hp_cuda_v1_context_profile_read(HpCudaContext *ctx, const char *ker
                                              uint64_t *launches);
 /* Number of kernels this library has launched in the process so far. */
 HpCudaStatus hp_cuda_v1_kernel_launch_count(uint64_t *out);
+/* Device memory of the context's stream-ordered pool (no counterpart in the
+ * reference; a serving host uses it to budget HBM per request from measured
+ * use): out3 = bytes in use now, the high-water mark of bytes in use since
+ * the last reset, bytes the pool holds from the device.  reset_high != 0
+ * resets the high-water mark to the current use after reading. */
+HpCudaStatus hp_cuda_v1_context_memory(HpCudaContext *ctx, int32_t reset_high, uint64_t *out3);
 
 /* The context's CUDA stream (a cudaStream_t), so a caller can order its own
  * work or timing events with the backend's. */

@@ -55,3 +55,32 @@ def test_server_rejects_oversized_and_reports_errors(gpu, oracle):
     ok = srv.submit(3, wit, [int.from_bytes(wit[0][32 * i:32 * i + 32].tobytes(), "little") for i in range(8)])
     assert isinstance(srv.wait(ok, timeout=60), bytes)  # the lane recovered
     srv.close()
+
+
+def test_admission_waits_for_the_memory_budget(gpu, oracle):
+    """A budget that holds one proof's measured memory but not two: the second
+    request waits in the queue until the first proof has finished, and both
+    proofs equal the requests proven alone."""
+    nv = 9
+    layers = [oracle.affine_to_packets(l) for l in oracle.srs_layers(nv, 14)]
+    srv = serve.ProofServer(0, nv_max=nv, lanes=1, slots_per_lane=2, hbm_budget_bytes=1 << 40, srs_layers=layers)
+    srv.prepare([nv], measure=True)
+    need = srv.measured[nv]
+    assert need > 0
+    srv.budget = need + need // 2
+    reqs = []
+    for i in range(2):
+        wit = snark.vanilla_witness(nv, 2, (5 << 32) | i)
+        pub = [int.from_bytes(wit[0][32 * j:32 * j + 32].tobytes(), "little") for j in range(16)]
+        reqs.append((wit, pub))
+    tickets = [srv.submit(nv, w, p) for w, p in reqs]
+    proofs = [srv.wait(t, timeout=300) for t in tickets]
+    srv.close()
+    first, second = srv.ticket(tickets[0]), srv.ticket(tickets[1])
+    assert second.admitted >= first.finished  # queued behind the budget, not the slots
+    gparam = gpu.prepare_prover_param(nv, layers)
+    sel, _, perm, _ = snark.vanilla_fixture(nv, 2)
+    pk = snark.ProvingKey(nv, 16, snark.VANILLA_GATE, gparam, [gpu.mle_from_evaluations(nv, s) for s in sel],
+                          [gpu.mle_from_evaluations(nv, p) for p in perm])
+    for (wit, pub), got in zip(reqs, proofs):
+        assert snark.prove(gpu, pk, pub, wit).to_bytes() == got
