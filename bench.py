@@ -71,6 +71,8 @@ def parse():
     ap.add_argument("--num-vars", type=int, default=None,
                     help="default 20 (prove, commit, sumcheck); the batch workload's SRS has 22")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="prove workload: skip the batch and serve workloads run beside it (child processes)")
     ap.add_argument("--msm-tuning", default=None, metavar="FILE",
                     help="load an MSM tuning table (hp_cuda_v1_msm_tuning_load) before preparing the SRS")
     ap.add_argument("--autotune", action="store_true",
@@ -417,8 +419,10 @@ def measure(s: Session, pg, steps: int, value_fn, e2e_fn, profile: bool = True, 
         s.profile(False)
     barrier(pg)
     s.torch.cuda.synchronize()
+    s.torch.cuda.nvtx.range_push("timed_e2e")  # the second loop (e2e, or the batch workload's plain run)
     per_e2e = s.timed(e2e_fn, steps)
     s.torch.cuda.synchronize()
+    s.torch.cuda.nvtx.range_pop()
     barrier(pg)
     return per, per_e2e, l1 - l0, clk, acc, msm
 
@@ -818,8 +822,44 @@ def run_gb300(args, world, rank, local, pg):
                            "frac_of_imad_peak": msm_accounting_imad(n) / (msm_ms / 1e3) / imad if msm_ms else None}
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(args.workload, nv, layers if args.workload == "prove" else None)
+    if rank == 0 and world == 1 and args.workload == "prove" and not args.no_extras and args.num_vars is None:
+        s.torch.cuda.synchronize()
+        result["other_workloads"] = other_workloads()
     if rank == 0:
         print(json.dumps(result))
+
+
+def other_workloads() -> dict:
+    """The batch plan (configuration 4) and the serving stream
+    (configuration 5) measured in the same run, each in a child process of
+    this script with its own timed region and clock record; their summaries
+    go into the prove line."""
+    out = {}
+    runs = {"batch": ["--workload", "batch", "--steps", "3", "--warmup", "1"],
+            "serve": ["--workload", "serve"]}
+    for name, extra in runs.items():
+        try:
+            r = subprocess.run([sys.executable, str(pathlib.Path(__file__).resolve()), *extra, "--no-cpu-baseline"],
+                               capture_output=True, text=True, timeout=1200, cwd=ROOT)
+            lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+            if r.returncode != 0 or not lines:
+                out[name] = {"error": f"exit {r.returncode}: {r.stderr.strip()[-300:]}"}
+                continue
+            d = json.loads(lines[-1])
+        except (subprocess.TimeoutExpired, ValueError) as e:
+            out[name] = {"error": str(e)[:300]}
+            continue
+        if name == "batch":
+            out[name] = {"metric": d["metric"], "value": d["value"], "unit": d["unit"],
+                         "ms_per_run": d["ms_per_step"], "plain_ms_per_run": d["plain"]["ms_per_run"],
+                         "batched_over_plain": d["plain"]["batched_over_plain"],
+                         "msm_points_per_run": d["msm_points_per_run"], "clocks": d["clocks"],
+                         "workload": d["config"]["workload"]}
+        else:
+            out[name] = {"metric": d["metric"], "unit": d["unit"],
+                         "plain_capacity_proofs_per_s": d["plain_capacity_proofs_per_s"],
+                         "loads": d["loads"], "clocks": d["clocks"], "workload": d["config"]["workload"]}
+    return out
 
 
 def cpu_baseline(workload: str, nv: int, srs_layers=None) -> dict:

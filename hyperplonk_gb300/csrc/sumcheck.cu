@@ -703,6 +703,7 @@ static size_t wide_max_pairs();
 static size_t wide_min_pairs();
 static bool product_pair_rounds();
 static bool fused_fold_pp();
+static size_t pp_min_pairs();
 static bool big_slot_rounds();
 static size_t big_blocks_per_sm();
 static int separate_fold_arity();
@@ -745,8 +746,8 @@ static void enqueue_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, cons
             separate_fold = !all_written || d.max_arity >= separate_fold_arity();
         }
     }
-    if (d.product_count > 0 && pairs > wide_max_pairs() && d.max_arity <= 3 && d.slot_count <= kMaxSlotsV2 &&
-        product_pair_rounds()) {
+    if (d.product_count > 0 && pairs >= pp_min_pairs() && pairs > wide_max_pairs() && d.max_arity <= 3 &&
+        d.slot_count <= kMaxSlotsV2 && product_pair_rounds()) {
         int tok = ctx->prof_begin("sumcheck_round", st);
         FrPtrList tables = src;
         bool fused_fold = fold;
@@ -893,6 +894,13 @@ static bool product_pair_rounds() {
 // (each factor re-folded once per product that reads it) instead of the
 // separate fold pass.  Off by default: measured on GB300 at 2^19 pairs, the
 // fused form took 225 us for round 2 against 82 + ~70 us for fold + round.
+// Smallest round for the (product, pair) kernel (HP_SUMCHECK_PP_MIN_PAIRS):
+// measured on GB300 (6 tables, 4 arity-2 products) it wins from 2^16 pairs on
+// (2^17: 60 vs 66 us) and loses below (2^14: 43 vs 32 us).
+static size_t pp_min_pairs() {
+    static const size_t v = env_size("HP_SUMCHECK_PP_MIN_PAIRS", size_t(1) << 16);
+    return v;
+}
 static bool fused_fold_pp() {
     static const bool v = env_size("HP_SUMCHECK_PP_FOLD", 0) != 0;
     return v;
