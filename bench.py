@@ -76,7 +76,8 @@ def parse():
     ap.add_argument("--msm-tuning", default=None, metavar="FILE",
                     help="load an MSM tuning table (hp_cuda_v1_msm_tuning_load) before preparing the SRS")
     ap.add_argument("--autotune", action="store_true",
-                    help="prove / commit / batch: run the MSM autotuner on the workload's MSM sizes before warm-up")
+                    help="prove / commit / batch: run the MSM autotuner on the workload's MSM sizes; prove / "
+                         "sumcheck: the sumcheck round-route tuner on the workload's sumcheck shapes; before warm-up")
     return ap.parse_args()
 
 
@@ -113,6 +114,23 @@ def autotune(args, be, params, alone_nvs, shared_nvs) -> None:
         {"mode": "alone" if e.mode == tuning.ALONE else "shared", "size": e.size, "window_bits": e.window_bits,
          "segment": e.segment, "chunk": e.chunk, "model_ms": round(e.model_ms, 4), "tuned_ms": round(e.tuned_ms, 4)}
         for e in entries]
+
+
+def autotune_sumcheck(args, be, run_once) -> None:
+    """--autotune: tune the sumcheck round routes of every sumcheck shape one
+    untimed run of the workload meets (run_once(backend_view)), before the
+    warm-up."""
+    if not args.autotune:
+        return
+    from hyperplonk_gb300 import tuning
+    t0 = time.perf_counter()
+    view = tuning.SumcheckTuningBackend(be)
+    run_once(view)
+    TUNING_INFO["sumcheck_autotune_s"] = round(time.perf_counter() - t0, 2)
+    TUNING_INFO["sumcheck_routes"] = [
+        {"shape_nv_arity_slots": list(key), "pairs": r.pairs, "kernel": r.kernel, "blocks_per_sm": r.blocks_per_sm,
+         "default_kernel": r.default_kernel, "default_us": round(r.default_us, 2), "tuned_us": round(r.tuned_us, 2)}
+        for key, recs in view.tuned.items() for r in recs]
 
 
 def shared_mix(nvs) -> list:
@@ -451,6 +469,8 @@ def run_sumcheck(args, world, rank, local, pg):
     coefs = workloads.sumcheck_coefficients(1)
     resident = [be.mle_from_evaluations(nv, t) for t in tables]
     out = {}
+    autotune_sumcheck(args, be, lambda view: protocol.sumcheck_prove(
+        view, workloads.sumcheck_polynomial(nv, resident, coefs), IOPTranscript(workloads.SUMCHECK_LABEL), []))
 
     def value_fn():
         vp = workloads.sumcheck_polynomial(nv, resident, coefs)
@@ -705,6 +725,7 @@ def run_gb300(args, world, rank, local, pg):
         wit_host = [p.numpy() for p in pinned]
         resident = [be.mle_from_evaluations(nv, w) for w in wit_host]
         out = {}
+        autotune_sumcheck(args, be, lambda view: snark.prove(view, pk, pub, None, witness_mles=resident))
 
         def value_fn():
             out["proof"] = snark.prove(be, pk, pub, None, witness_mles=resident).to_bytes()

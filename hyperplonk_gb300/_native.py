@@ -29,6 +29,13 @@ class MsmTuning(ctypes.Structure):
                 ("tuned_ms", ctypes.c_double)]
 
 
+class RoundTuning(ctypes.Structure):
+    """HpCudaRoundTuning (include/hp_cuda.h)."""
+    _fields_ = [("pairs", ctypes.c_uint64), ("kernel", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_uint32),
+                ("default_kernel", ctypes.c_uint32), ("default_blocks_per_sm", ctypes.c_uint32),
+                ("default_us", ctypes.c_double), ("tuned_us", ctypes.c_double)]
+
+
 class RuntimeCounters(ctypes.Structure):
     """HpCudaRuntimeCounters (include/hp_cuda.h)."""
     _fields_ = [(name, ctypes.c_uint64) for name in (
@@ -100,6 +107,9 @@ SIGNATURES: dict[str, list] = {
     "hp_cuda_v1_msm_tuning_save": [ctypes.c_char_p],
     "hp_cuda_v1_msm_tuning_load": [ctypes.c_char_p, ctypes.c_char_p],
     "hp_cuda_v1_msm_tuning_clear": [],
+    "hp_cuda_v1_sumcheck_autotune": [c_voidp, c_voidp, ctypes.POINTER(RoundTuning), c_size, c_sizep],
+    "hp_cuda_v1_sumcheck_route_query": [c_size, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                         ctypes.POINTER(ctypes.c_uint32)],
 }
 
 _lib = None

@@ -708,16 +708,106 @@ static bool big_slot_rounds();
 static size_t big_blocks_per_sm();
 static int separate_fold_arity();
 
-// Enqueues one round of state s on stream st: fold with r (rounds > 1) and
-// message into out_dev (degree + 1 canonical Fr, device).  Scratch is ordered
-// on st.  Does not advance the state.
-static void enqueue_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, const Fr &r, cudaStream_t st,
-                          Fr *out_dev) {
+// ---------------------------------------------------------------------------
+// Round routes: which kernel runs a round, and its grid
+// ---------------------------------------------------------------------------
+
+// The shape facts a round's route depends on.
+struct RoundShape {
+    size_t pairs;
+    bool fold;         // round > 1: the previous challenge is folded in
+    bool regs;         // arity <= 8 and <= kMaxSlotsV2 slots (per-thread kernels)
+    bool all_written;  // every factor is read by some product (fused folds store it)
+    bool products;     // at least one product
+    int max_arity;
+    int slots;
+};
+
+static RoundShape round_shape(const HpCudaSumCheckProverState *s) {
     const SumcheckDesc &d = s->desc;
-    const bool fold = s->round > 0;
+    RoundShape sh;
+    sh.pairs = table_len(s->num_vars - s->round - 1);
+    sh.fold = s->round > 0;
+    sh.regs = d.max_arity <= 8 && d.slot_count <= kMaxSlotsV2;
+    sh.all_written = true;
+    for (int f = 0; f < d.factor_count; f++) sh.all_written = sh.all_written && d.writer[f] != kNoWriter;
+    sh.products = d.product_count > 0;
+    sh.max_arity = d.max_arity;
+    sh.slots = d.slot_count;
+    return sh;
+}
+
+// Whether `route` can run a round of this shape.
+static bool route_valid(const RoundShape &sh, const RoundRoute &rt) {
+    switch (rt.kernel) {
+        case kRouteOneBlock: return sh.regs && sh.pairs <= size_t(kSmallPairs);
+        case kRoutePerPair: return sh.regs;
+        case kRouteSlot: return sh.products;
+        case kRouteSlotFused: return sh.products && sh.fold && sh.all_written;
+        case kRoutePp: return sh.products && sh.max_arity <= 3 && sh.slots <= kMaxSlotsV2;
+        case kRoutePpFused: return sh.products && sh.max_arity <= 3 && sh.slots <= kMaxSlotsV2 && sh.fold &&
+                                   sh.all_written;
+        default: return false;
+    }
+}
+
+// The built-in rules (sizes measured on GB300; the environment switches of
+// the run-time table in the design notes override them).
+static RoundRoute default_route(const RoundShape &sh) {
+    const bool small = sh.regs && sh.pairs <= size_t(kSmallPairs);
+    if (sh.products && sh.pairs >= pp_min_pairs() && sh.pairs > wide_max_pairs() && sh.max_arity <= 3 &&
+        sh.slots <= kMaxSlotsV2 && product_pair_rounds())
+        return RoundRoute{uint8_t(sh.fold && sh.all_written && fused_fold_pp() ? kRoutePpFused : kRoutePp),
+                          uint8_t(kPpBlocksPerSm)};
+    if (sh.products && !small) {
+        if (sh.pairs > wide_max_pairs()) {
+            if (big_slot_rounds() || !sh.regs) return RoundRoute{kRouteSlot, uint8_t(big_blocks_per_sm())};
+        } else if (sh.pairs >= wide_min_pairs() || !sh.regs) {
+            // the fused fold stores only factors some product reads; products
+            // of arity >= separate_fold_arity() (HP_SEPARATE_FOLD_ARITY,
+            // default 3) fold in a separate pass: one more launch, but each
+            // item's chain loses the 2m products of re-folding its factors
+            // (GB300, nv = 20: arity-4/5 middle rounds 56-60 -> 35-43 us)
+            const bool separate = !sh.all_written || sh.max_arity >= separate_fold_arity();
+            return RoundRoute{uint8_t(sh.fold && !separate ? kRouteSlotFused : kRouteSlot), 0};
+        }
+    }
+    if (small) return RoundRoute{kRouteOneBlock, 0};
+    return RoundRoute{kRoutePerPair, 0};
+}
+
+// The route of a round: the tuned entry for its shape when one exists and
+// fits, else the built-in rules.
+static RoundRoute chosen_route(const RoundShape &sh) {
+    RoundRoute rt;
+    if (sumcheck_route_lookup(RoundKey{ceil_log2_size(sh.pairs), sh.max_arity, sh.slots, sh.fold ? 1 : 0}, rt) &&
+        route_valid(sh, rt))
+        return rt;
+    return default_route(sh);
+}
+
+// k_sumcheck_fold of every table: dst_f[i] = src_f[2i] + r (src_f[2i+1] - src_f[2i]).
+static void fold_all(HpCudaContext *ctx, const SumcheckDesc &d, const FrPtrList &src, const FrMutPtrList &dst,
+                     size_t pairs, const Fr &r, cudaStream_t st) {
+    int log_half = 0;
+    while ((size_t(1) << log_half) < 2 * pairs) log_half++;
+    const size_t total = size_t(d.factor_count) << log_half;
+    const size_t sms = size_t(ctx->sm_count > 0 ? ctx->sm_count : 152);
+    const unsigned fgrid = unsigned(std::max<size_t>(1, std::min<size_t>((total + 255) / 256, sms * 8)));
+    k_sumcheck_fold<<<fgrid, 256, 0, st>>>(src, dst, d.factor_count, log_half, r);
+    check_launch();
+}
+
+// Enqueues one round of state s on stream st along `rt`: fold with r (rounds
+// > 1) and message into out_dev (degree + 1 canonical Fr, device).  Scratch
+// is ordered on st.  Does not advance the state.
+static void launch_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, const Fr &r, cudaStream_t st,
+                         Fr *out_dev, const RoundShape &sh, const RoundRoute &rt) {
+    const SumcheckDesc &d = s->desc;
+    const bool fold = sh.fold;
     const int src_which = s->current;
     const int dst_which = fold ? (src_which == 1 ? 2 : 1) : src_which;
-    size_t pairs = table_len(s->num_vars - s->round - 1);
+    const size_t pairs = sh.pairs;
     FrPtrList src{}, rd{};
     FrMutPtrList dst{};
     for (int f = 0; f < d.factor_count; f++) {
@@ -725,142 +815,118 @@ static void enqueue_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, cons
         dst.p[f] = const_cast<Fr *>(state_table(s, dst_which, f));
         rd.p[f] = fold ? dst.p[f] : src.p[f];
     }
-    // the per-pair kernels take arity <= 8 and at most 48 slots (per-thread
-    // slot tables); the (slot, pair) kernel takes any shape with products
-    const bool regs = d.max_arity <= 8 && d.slot_count <= kMaxSlotsV2;
-    const bool small = regs && pairs <= size_t(kSmallPairs);
-    bool all_written = true;
-    for (int f = 0; f < d.factor_count; f++) all_written = all_written && d.writer[f] != kNoWriter;
-    bool use_slots = false, separate_fold = false;
-    if (d.product_count > 0 && !small) {
-        if (pairs > wide_max_pairs()) {
-            use_slots = big_slot_rounds() || !regs;
-            separate_fold = true;
-        } else if (pairs >= wide_min_pairs() || !regs) {
-            use_slots = true;
-            // the fused fold stores only factors some product reads; products
-            // of arity >= separate_fold_arity() (HP_SEPARATE_FOLD_ARITY,
-            // default 3) fold in a separate pass: one more launch, but each
-            // item's chain loses the 2m products of re-folding its factors
-            // (GB300, nv = 20: arity-4/5 middle rounds 56-60 -> 35-43 us)
-            separate_fold = !all_written || d.max_arity >= separate_fold_arity();
-        }
-    }
-    if (d.product_count > 0 && pairs >= pp_min_pairs() && pairs > wide_max_pairs() && d.max_arity <= 3 &&
-        d.slot_count <= kMaxSlotsV2 && product_pair_rounds()) {
-        int tok = ctx->prof_begin("sumcheck_round", st);
-        FrPtrList tables = src;
-        bool fused_fold = fold;
-        if (fold && (!all_written || !fused_fold_pp())) {
-            // fold every table first (a factor no product reads has no writer)
-            int log_half = 0;
-            while ((size_t(1) << log_half) < 2 * pairs) log_half++;
-            const size_t total = size_t(d.factor_count) << log_half;
-            const size_t sms = size_t(ctx->sm_count > 0 ? ctx->sm_count : 152);
-            const unsigned fgrid = unsigned(std::max<size_t>(1, std::min<size_t>((total + 255) / 256, sms * 8)));
-            k_sumcheck_fold<<<fgrid, 256, 0, st>>>(src, dst, d.factor_count, log_half, r);
-            check_launch();
-            tables = rd;
-            fused_fold = false;
-        }
-        const size_t P = size_t(d.product_count);
-        const size_t tiles = (pairs + kPpThreads - 1) / kPpThreads;
-        const size_t target = size_t(ctx->sm_count > 0 ? ctx->sm_count : 152) * kPpBlocksPerSm;
-        const int bpp = int(std::max<size_t>(1, std::min(tiles, (target + P - 1) / P)));
-        const unsigned grid = unsigned(P) * unsigned(bpp);
-        Scratch spill;
-        Fr *partials = round_partials(ctx, s, size_t(d.slot_count) * size_t(bpp) * sizeof(Fr), spill, st);
-        const size_t smem = size_t(d.slot_count) * sizeof(Fr);
-        auto launch = [&](auto kernel) {
-            kernel<<<grid, kPpThreads, smem, st>>>(d, tables, dst, fused_fold, r, pairs, bpp, partials,
-                                                   round_counter(s), state_weights(s), int(s->max_degree), out_dev);
-        };
-        if (d.max_arity <= 2) launch(k_sumcheck_round_pp<2>);
-        else launch(k_sumcheck_round_pp<3>);
-        check_launch();
-        ctx->prof_end(tok, st);
-        return;
-    }
-    if (use_slots) {
-        int tok = ctx->prof_begin("sumcheck_round", st);
-        const size_t tiles = (pairs + kWideThreads - 1) / kWideThreads;
-        int bps = int(std::min(tiles, size_t(1) << 20));
-        FrPtrList tables = src;
-        bool fused_fold = fold;
-        if (fold && separate_fold) {
-            // fold every table first, then one pass over the folded tables
-            int log_half = 0;
-            while ((size_t(1) << log_half) < 2 * pairs) log_half++;
-            const size_t total = size_t(d.factor_count) << log_half;
-            const size_t sms = size_t(ctx->sm_count > 0 ? ctx->sm_count : 152);
-            const unsigned fgrid = unsigned(std::max<size_t>(1, std::min<size_t>((total + 255) / 256, sms * 8)));
-            k_sumcheck_fold<<<fgrid, 256, 0, st>>>(src, dst, d.factor_count, log_half, r);
-            check_launch();
-            tables = rd;
-            fused_fold = false;
-        }
-        if (pairs > wide_max_pairs()) {
-            // about big_blocks_per_sm() blocks per SM over all slots
-            const size_t target = size_t(ctx->sm_count > 0 ? ctx->sm_count : 152) * big_blocks_per_sm();
-            bps = int(std::max<size_t>(1, std::min(tiles, (target + d.slot_count - 1) / d.slot_count)));
-        }
-        const unsigned grid = unsigned(d.slot_count) * unsigned(bps);
-        Scratch spill;
-        Fr *partials = round_partials(ctx, s, size_t(grid) * sizeof(Fr), spill, st);
-        const size_t smem = size_t(d.slot_count) * sizeof(Fr);
-        auto launch = [&](auto kernel) {
-            if (smem > 32 * 1024)
-                check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-            kernel<<<grid, kWideThreads, smem, st>>>(d, tables, dst, fused_fold, r, pairs, bps, partials,
-                                                     round_counter(s), state_weights(s), int(s->max_degree),
-                                                     out_dev);
-        };
-        if (d.max_arity <= 2) launch(k_sumcheck_round_wide<2>);
-        else if (d.max_arity <= 4) launch(k_sumcheck_round_wide<4>);
-        else if (d.max_arity <= 6) launch(k_sumcheck_round_wide<6>);
-        else if (d.max_arity <= 8) launch(k_sumcheck_round_wide<8>);
-        else launch(k_sumcheck_round_wide<0>);  // any arity, loop not unrolled
-        check_launch();
-        ctx->prof_end(tok, st);
-        return;
-    }
-    if (regs && pairs <= size_t(kSmallPairs)) {
-        int tok = ctx->prof_begin("sumcheck_round", st);
-        const size_t smem = size_t(d.slot_count) * (kSmallPairs + 1) * sizeof(Fr);
-        auto launch = [&](auto kernel) {
-            if (smem > 32 * 1024)
-                check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-            kernel<<<1, kSmallThreads, smem, st>>>(d, src, dst, rd, fold, r, int(pairs),
-                                                   state_weights(s), int(s->max_degree), out_dev);
-        };
-        if (d.max_arity <= 2) launch(k_sumcheck_round_small<2>);
-        else if (d.max_arity <= 4) launch(k_sumcheck_round_small<4>);
-        else if (d.max_arity <= 6) launch(k_sumcheck_round_small<6>);
-        else launch(k_sumcheck_round_small<8>);
-        check_launch();
-        ctx->prof_end(tok, st);
-        return;
-    }
-    if (!regs) fail(HP_CUDA_STATUS_NOT_IMPLEMENTED);  // unreachable: !regs implies products, hence slots
-    const unsigned grid = grid_for(ctx, pairs, kRoundThreads, HP_ROUND_BLOCKS_PER_SM);
-    Scratch spill;
-    Fr *partials = round_partials(ctx, s, size_t(grid) * d.slot_count * sizeof(Fr), spill, st);
+    const size_t sms = size_t(ctx->sm_count > 0 ? ctx->sm_count : 152);
     int tok = ctx->prof_begin("sumcheck_round", st);
-    const size_t smem = size_t(d.slot_count) * kRoundThreads * sizeof(Fr);
-    auto launch = [&](auto kernel) {
-        // the kernel's own static shared memory counts against the same
-        // 48 KiB default, so opt in well before the dynamic size reaches it
-        if (smem > 32 * 1024)
-            check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-        kernel<<<grid, kRoundThreads, smem, st>>>(d, src, dst, rd, fold, r, pairs, partials, round_counter(s),
-                                                  state_weights(s), int(s->max_degree), out_dev);
-    };
-    if (d.max_arity <= 2) launch(k_sumcheck_round_regs<2>);
-    else if (d.max_arity <= 4) launch(k_sumcheck_round_regs<4>);
-    else if (d.max_arity <= 6) launch(k_sumcheck_round_regs<6>);
-    else launch(k_sumcheck_round_regs<8>);
-    check_launch();
+    switch (rt.kernel) {
+        case kRoutePp:
+        case kRoutePpFused: {
+            FrPtrList tables = src;
+            bool fused_fold = fold && rt.kernel == kRoutePpFused;
+            if (fold && !fused_fold) {
+                fold_all(ctx, d, src, dst, pairs, r, st);
+                tables = rd;
+            }
+            const size_t P = size_t(d.product_count);
+            const size_t tiles = (pairs + kPpThreads - 1) / kPpThreads;
+            const size_t target = sms * std::max<size_t>(1, rt.per_sm);
+            const int bpp = int(std::max<size_t>(1, std::min(tiles, (target + P - 1) / P)));
+            const unsigned grid = unsigned(P) * unsigned(bpp);
+            Scratch spill;
+            Fr *partials = round_partials(ctx, s, size_t(d.slot_count) * size_t(bpp) * sizeof(Fr), spill, st);
+            const size_t smem = size_t(d.slot_count) * sizeof(Fr);
+            auto launch = [&](auto kernel) {
+                kernel<<<grid, kPpThreads, smem, st>>>(d, tables, dst, fused_fold, r, pairs, bpp, partials,
+                                                       round_counter(s), state_weights(s), int(s->max_degree),
+                                                       out_dev);
+            };
+            if (d.max_arity <= 2) launch(k_sumcheck_round_pp<2>);
+            else launch(k_sumcheck_round_pp<3>);
+            check_launch();
+            break;
+        }
+        case kRouteSlot:
+        case kRouteSlotFused: {
+            const size_t tiles = (pairs + kWideThreads - 1) / kWideThreads;
+            int bps = int(std::min(tiles, size_t(1) << 20));
+            FrPtrList tables = src;
+            bool fused_fold = fold && rt.kernel == kRouteSlotFused;
+            if (fold && !fused_fold) {
+                // fold every table first, then one pass over the folded tables
+                fold_all(ctx, d, src, dst, pairs, r, st);
+                tables = rd;
+            }
+            if (rt.per_sm > 0) {
+                // about per_sm blocks per SM over all slots
+                const size_t target = sms * rt.per_sm;
+                bps = int(std::max<size_t>(1, std::min(tiles, (target + d.slot_count - 1) / d.slot_count)));
+            }
+            const unsigned grid = unsigned(d.slot_count) * unsigned(bps);
+            Scratch spill;
+            Fr *partials = round_partials(ctx, s, size_t(grid) * sizeof(Fr), spill, st);
+            const size_t smem = size_t(d.slot_count) * sizeof(Fr);
+            auto launch = [&](auto kernel) {
+                if (smem > 32 * 1024)
+                    check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+                kernel<<<grid, kWideThreads, smem, st>>>(d, tables, dst, fused_fold, r, pairs, bps, partials,
+                                                         round_counter(s), state_weights(s), int(s->max_degree),
+                                                         out_dev);
+            };
+            if (d.max_arity <= 2) launch(k_sumcheck_round_wide<2>);
+            else if (d.max_arity <= 4) launch(k_sumcheck_round_wide<4>);
+            else if (d.max_arity <= 6) launch(k_sumcheck_round_wide<6>);
+            else if (d.max_arity <= 8) launch(k_sumcheck_round_wide<8>);
+            else launch(k_sumcheck_round_wide<0>);  // any arity, loop not unrolled
+            check_launch();
+            break;
+        }
+        case kRouteOneBlock: {
+            const size_t smem = size_t(d.slot_count) * (kSmallPairs + 1) * sizeof(Fr);
+            auto launch = [&](auto kernel) {
+                if (smem > 32 * 1024)
+                    check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+                kernel<<<1, kSmallThreads, smem, st>>>(d, src, dst, rd, fold, r, int(pairs), state_weights(s),
+                                                       int(s->max_degree), out_dev);
+            };
+            if (d.max_arity <= 2) launch(k_sumcheck_round_small<2>);
+            else if (d.max_arity <= 4) launch(k_sumcheck_round_small<4>);
+            else if (d.max_arity <= 6) launch(k_sumcheck_round_small<6>);
+            else launch(k_sumcheck_round_small<8>);
+            check_launch();
+            break;
+        }
+        case kRoutePerPair: {
+            const unsigned grid = grid_for(ctx, pairs, kRoundThreads, HP_ROUND_BLOCKS_PER_SM);
+            Scratch spill;
+            Fr *partials = round_partials(ctx, s, size_t(grid) * d.slot_count * sizeof(Fr), spill, st);
+            const size_t smem = size_t(d.slot_count) * kRoundThreads * sizeof(Fr);
+            auto launch = [&](auto kernel) {
+                // the kernel's own static shared memory counts against the same
+                // 48 KiB default, so opt in well before the dynamic size reaches it
+                if (smem > 32 * 1024)
+                    check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+                kernel<<<grid, kRoundThreads, smem, st>>>(d, src, dst, rd, fold, r, pairs, partials,
+                                                          round_counter(s), state_weights(s), int(s->max_degree),
+                                                          out_dev);
+            };
+            if (d.max_arity <= 2) launch(k_sumcheck_round_regs<2>);
+            else if (d.max_arity <= 4) launch(k_sumcheck_round_regs<4>);
+            else if (d.max_arity <= 6) launch(k_sumcheck_round_regs<6>);
+            else launch(k_sumcheck_round_regs<8>);
+            check_launch();
+            break;
+        }
+        default: fail(HP_CUDA_STATUS_INVALID_STATE);
+    }
     ctx->prof_end(tok, st);
+}
+
+// Enqueues one round of state s on stream st along its chosen route.
+static void enqueue_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, const Fr &r, cudaStream_t st,
+                          Fr *out_dev) {
+    const RoundShape sh = round_shape(s);
+    const RoundRoute rt = chosen_route(sh);
+    if (!route_valid(sh, rt)) fail(HP_CUDA_STATUS_NOT_IMPLEMENTED);
+    launch_round(ctx, s, r, st, out_dev, sh, rt);
 }
 
 // Rounds of wide_min_pairs() .. wide_max_pairs() pairs use the (slot, pair)
@@ -1052,6 +1118,136 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prove_rounds(HpCudaContext *ctx, HpC
             std::memcpy(out_challenges + 32 * k, canon, 32);
             std::memcpy(r.v, c.v, 32);
         }
+    });
+}
+
+// Sumcheck round autotuner: runs every round of `s` (a fresh state, which it
+// consumes) once per candidate route -- each kernel family that can run the
+// round, at a few grid sizes -- times each as the median of a few runs with
+// CUDA events on the context stream, checks that every candidate's message
+// equals the built-in rule's, and stores the fastest route for the round's
+// key (ceil log2 pairs, largest arity, slot count) in the process-wide
+// tuning table; then runs the round along it and advances.  Challenges are
+// fixed small values (the route does not depend on them).
+namespace hp {
+namespace {
+
+const RoundRoute kRouteCandidates[] = {
+    {kRouteOneBlock, 0}, {kRoutePerPair, 0}, {kRouteSlot, 0},      {kRouteSlot, 4},  {kRouteSlot, 8},
+    {kRouteSlot, 16},    {kRouteSlot, 32},   {kRouteSlotFused, 0}, {kRouteSlotFused, 16},
+    {kRoutePp, 2},       {kRoutePp, 3},      {kRoutePp, 6},        {kRoutePpFused, 3},
+};
+
+bool same_route(const RoundRoute &a, const RoundRoute &b) { return a.kernel == b.kernel && a.per_sm == b.per_sm; }
+
+}  // namespace
+}  // namespace hp
+
+extern "C" HpCudaStatus hp_cuda_v1_sumcheck_autotune(HpCudaContext *ctx, HpCudaSumCheckProverState *s,
+                                                     HpCudaRoundTuning *out, size_t capacity, size_t *out_count) {
+    if (out_count) *out_count = 0;
+    return guard([&] {
+        using namespace hp;
+        require_ctx(ctx);
+        require(s != nullptr && out != nullptr && out_count != nullptr);
+        if (s->poisoned || s->round != 0) fail(HP_CUDA_STATUS_INVALID_STATE);
+        require(capacity >= s->num_vars);
+        const size_t d1 = s->max_degree + 1;
+        void *box_dev = nullptr;
+        const uint8_t *box = ctx->mailbox(d1 * sizeof(Fr), &box_dev);
+        Fr *msg_dev = static_cast<Fr *>(box_dev);
+        cudaEvent_t a = nullptr, b = nullptr;
+        check_cuda(cudaEventCreate(&a));
+        check_cuda(cudaEventCreate(&b));
+        struct Events {
+            cudaEvent_t &a, &b;
+            ~Events() {
+                cudaEventDestroy(a);
+                cudaEventDestroy(b);
+            }
+        } events{a, b};
+        try {
+            for (size_t k = 0; k < s->num_vars; k++) {
+                uint8_t cb[32] = {0};
+                cb[0] = uint8_t(k + 2);
+                const Fr r = k == 0 ? Fr::zero() : host_scalar(cb);
+                const RoundShape sh = round_shape(s);
+                const RoundRoute dflt = default_route(sh);
+                if (!route_valid(sh, dflt)) fail(HP_CUDA_STATUS_NOT_IMPLEMENTED);
+                auto run_once = [&](const RoundRoute &rt) {
+                    launch_round(ctx, s, r, ctx->stream, msg_dev, sh, rt);
+                };
+                auto timed = [&](const RoundRoute &rt) {
+                    const int reps = sh.pairs >= (size_t(1) << 16) ? 5 : 9;
+                    std::vector<float> ms;
+                    for (int i = 0; i < reps; i++) {
+                        check_cuda(cudaEventRecord(a, ctx->stream));
+                        run_once(rt);
+                        check_cuda(cudaEventRecord(b, ctx->stream));
+                        check_cuda(cudaEventSynchronize(b));
+                        float t = 0.f;
+                        check_cuda(cudaEventElapsedTime(&t, a, b));
+                        ms.push_back(t);
+                    }
+                    std::sort(ms.begin(), ms.end());
+                    return double(ms[ms.size() / 2]) * 1e3;  // us
+                };
+                // the built-in rule's message is the one every candidate must give
+                run_once(dflt);
+                ctx->sync();
+                std::vector<uint8_t> want(box, box + d1 * sizeof(Fr));
+                const double dflt_us = timed(dflt);
+                RoundRoute best = dflt;
+                double best_us = dflt_us;
+                for (const RoundRoute &cand : kRouteCandidates) {
+                    if (same_route(cand, dflt) || !route_valid(sh, cand)) continue;
+                    run_once(cand);
+                    ctx->sync();
+                    if (std::memcmp(box, want.data(), want.size()) != 0) fail(HP_CUDA_STATUS_INVALID_STATE);
+                    const double us = timed(cand);
+                    if (us < best_us * 0.98) {
+                        best = cand;
+                        best_us = us;
+                    }
+                }
+                sumcheck_route_store(RoundKey{ceil_log2_size(sh.pairs), sh.max_arity, sh.slots, sh.fold ? 1 : 0},
+                                     best, best_us);
+                run_once(best);
+                ctx->sync();
+                advance(s);
+                HpCudaRoundTuning &o = out[k];
+                o.pairs = uint64_t(sh.pairs);
+                o.kernel = best.kernel;
+                o.blocks_per_sm = best.per_sm;
+                o.default_kernel = dflt.kernel;
+                o.default_blocks_per_sm = dflt.per_sm;
+                o.default_us = dflt_us;
+                o.tuned_us = best_us;
+                *out_count = k + 1;
+            }
+        } catch (const Failure &f) {
+            if (f.kind == HP_CUDA_STATUS_INVALID_STATE) s->poisoned = true;
+            throw;
+        }
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_sumcheck_route_query(size_t pairs, int32_t max_arity, int32_t slots,
+                                                        int32_t fold, uint32_t *out2) {
+    return guard([&] {
+        using namespace hp;
+        require(out2 != nullptr && pairs >= 1 && max_arity >= 1 && slots >= 1);
+        RoundShape sh;
+        sh.pairs = pairs;
+        sh.fold = fold != 0;
+        sh.regs = max_arity <= 8 && slots <= kMaxSlotsV2;
+        sh.all_written = true;
+        sh.products = true;
+        sh.max_arity = max_arity;
+        sh.slots = slots;
+        const RoundRoute rt = chosen_route(sh);
+        out2[0] = rt.kernel;
+        out2[1] = rt.per_sm;
     });
 }
 

@@ -30,4 +30,45 @@ struct SumcheckDesc {
 
 constexpr uint16_t kNoWriter = 0xffff;
 
+// How a round is run (sumcheck.cu): the kernel family and, where it has one,
+// its grid in blocks per SM (0: one thread per item of the round).
+enum RouteKernel : uint8_t {
+    kRouteNone = 0,
+    kRouteOneBlock = 1,   // one block, (factor, pair) then (product, pair) items (<= 64 pairs)
+    kRoutePerPair = 2,    // one pair per thread, per-thread slot sums in shared memory
+    kRouteSlot = 3,       // (slot, pair) items, separate fold pass
+    kRouteSlotFused = 4,  // (slot, pair) items folding their own factors
+    kRoutePp = 5,         // (product, pair) items, separate fold pass
+    kRoutePpFused = 6,    // (product, pair) items folding their own factors
+    kRouteKinds = 7
+};
+struct RoundRoute {
+    uint8_t kernel;
+    uint8_t per_sm;
+};
+// Tuning key of a round: ceil(log2 pairs), the largest product arity, the
+// slot count (sum over products of arity + 1) and whether the round folds
+// the previous challenge in (every round but the first).
+struct RoundKey {
+    int log2_pairs;
+    int max_arity;
+    int slots;
+    int fold;
+    bool operator<(const RoundKey &o) const {
+        if (log2_pairs != o.log2_pairs) return log2_pairs < o.log2_pairs;
+        if (max_arity != o.max_arity) return max_arity < o.max_arity;
+        if (slots != o.slots) return slots < o.slots;
+        return fold < o.fold;
+    }
+};
+inline int ceil_log2_size(size_t x) {
+    int k = 0;
+    while ((size_t(1) << k) < x) k++;
+    return k;
+}
+// The process-wide table of measured round routes (tune.cu: it shares the
+// MSM tuning table's file, built-in GB300 entries and environment override).
+bool sumcheck_route_lookup(const RoundKey &key, RoundRoute &out);
+void sumcheck_route_store(const RoundKey &key, const RoundRoute &route, double us);
+
 }  // namespace hp

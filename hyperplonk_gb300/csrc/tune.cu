@@ -35,6 +35,11 @@
 //     device <name, spaces as _>
 //     alone <log2 n> <c> <seg> <chunk> <ms>
 //     many <log2 records> <chunk> <ms>
+//     round <log2 pairs> <max arity> <slots> <fold 0/1> <kernel> <blocks per SM> <us>
+//
+// The last kind holds the sumcheck round routes that
+// hp_cuda_v1_sumcheck_autotune measures (sumcheck.cu): which round kernel
+// and grid run a round of that many pairs and that product shape.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -51,6 +56,7 @@
 #include "kzg.cuh"
 #include "msm.cuh"
 #include "runtime.cuh"
+#include "sumcheck.cuh"
 
 namespace hp {
 namespace {
@@ -64,12 +70,25 @@ struct ManyEntry {
     double ms;
 };
 
+struct RouteEntry {
+    RoundRoute route;
+    double us;
+};
+
 struct TuningTable {
     std::mutex mu;
     std::map<int, AloneEntry> alone;  // ceil(log2 n)
     std::map<int, ManyEntry> many;    // ceil(log2 records)
+    std::map<RoundKey, RouteEntry> rounds;
     std::string device = "any";
     bool env_checked = false;
+};
+
+struct Parsed {
+    std::map<int, AloneEntry> alone;
+    std::map<int, ManyEntry> many;
+    std::map<RoundKey, RouteEntry> rounds;
+    std::string device = "any";
 };
 
 TuningTable &table() {
@@ -93,20 +112,19 @@ std::string device_token(const char *name) {
 bool valid_seg(long v) { return v >= 1 && v <= 64 && (v & (v - 1)) == 0; }
 bool valid_chunk(long v) { return v >= 2 && v <= 1024; }
 
-// Parse a tuning table into `alone` / `many` / `device`; false on any
-// malformed line (nothing is applied then).
-bool parse_table(std::istream &in, std::map<int, AloneEntry> &alone, std::map<int, ManyEntry> &many,
-                 std::string &device) {
+// Parse a tuning table; false on any malformed line (nothing is applied
+// then).
+bool parse_table(std::istream &in, Parsed &out) {
     std::string line;
     if (!std::getline(in, line) || line != "hp_cuda msm tuning 1") return false;
-    device = "any";
+    out = Parsed();
     while (std::getline(in, line)) {
         if (line.empty()) continue;
         std::istringstream ls(line);
         std::string kind;
         ls >> kind;
         if (kind == "device") {
-            if (!(ls >> device)) return false;
+            if (!(ls >> out.device)) return false;
         } else if (kind == "alone") {
             long k, c, seg, chunk;
             double ms;
@@ -118,13 +136,24 @@ bool parse_table(std::istream &in, std::map<int, AloneEntry> &alone, std::map<in
             t.c = int(c);
             t.seg = uint32_t(seg);
             t.chunk = uint32_t(chunk);
-            alone[int(k)] = AloneEntry{t, ms};
+            out.alone[int(k)] = AloneEntry{t, ms};
         } else if (kind == "many") {
             long k, chunk;
             double ms;
             if (!(ls >> k >> chunk >> ms)) return false;
             if (k < 0 || k > 40 || !valid_chunk(chunk) || !std::isfinite(ms) || ms < 0) return false;
-            many[int(k)] = ManyEntry{uint32_t(chunk), ms};
+            out.many[int(k)] = ManyEntry{uint32_t(chunk), ms};
+        } else if (kind == "round") {
+            // round <ceil log2 pairs> <max arity> <slots> <fold> <kernel> <blocks per SM> <us>
+            long k, arity, slots, fold, kernel, per_sm;
+            double us;
+            if (!(ls >> k >> arity >> slots >> fold >> kernel >> per_sm >> us)) return false;
+            if (k < 0 || k > 40 || arity < 1 || arity > kMaxDegree || slots < 1 || slots > 4096 ||
+                (fold != 0 && fold != 1) || kernel <= kRouteNone || kernel >= kRouteKinds || per_sm < 0 ||
+                per_sm > 64 || !std::isfinite(us) || us < 0)
+                return false;
+            out.rounds[RoundKey{int(k), int(arity), int(slots), int(fold)}] =
+                RouteEntry{RoundRoute{uint8_t(kernel), uint8_t(per_sm)}, us};
         } else {
             return false;
         }
@@ -134,10 +163,16 @@ bool parse_table(std::istream &in, std::map<int, AloneEntry> &alone, std::map<in
     return true;
 }
 
-bool parse_file(const char *path, std::map<int, AloneEntry> &alone, std::map<int, ManyEntry> &many,
-                std::string &device) {
+bool parse_file(const char *path, Parsed &out) {
     std::ifstream in(path);
-    return in && parse_table(in, alone, many, device);
+    return in && parse_table(in, out);
+}
+
+void merge_into(TuningTable &t, const Parsed &p) {
+    for (auto &kv : p.alone) t.alone[kv.first] = kv.second;
+    for (auto &kv : p.many) t.many[kv.first] = kv.second;
+    for (auto &kv : p.rounds) t.rounds[kv.first] = kv.second;
+    t.device = p.device;
 }
 
 // The table measured on a GB300 (msm_tuning_gb300.inc), the default on
@@ -166,22 +201,12 @@ void load_env_locked(TuningTable &t) {
     t.env_checked = true;
     const char *path = std::getenv("HP_CUDA_MSM_TUNING");
     if (path && std::strcmp(path, "off") == 0) return;
-    std::map<int, AloneEntry> alone;
-    std::map<int, ManyEntry> many;
-    std::string device;
+    Parsed parsed;
     std::istringstream builtin(kBuiltinGb300);
-    if (parse_table(builtin, alone, many, device) && device == current_device_token()) {
-        t.alone = alone;
-        t.many = many;
-        t.device = device;
-    }
+    if (parse_table(builtin, parsed) && parsed.device == current_device_token()) merge_into(t, parsed);
     if (!path || !path[0]) return;
-    alone.clear();
-    many.clear();
-    if (!parse_file(path, alone, many, device)) return;
-    for (auto &kv : alone) t.alone[kv.first] = kv.second;
-    for (auto &kv : many) t.many[kv.first] = kv.second;
-    t.device = device;
+    if (!parse_file(path, parsed)) return;
+    merge_into(t, parsed);
 }
 
 bool geometry_env_set() {
@@ -483,6 +508,27 @@ extern "C" HpCudaStatus hp_cuda_v1_msm_tuning_query(int32_t mode, size_t size, u
     });
 }
 
+namespace hp {
+
+bool sumcheck_route_lookup(const RoundKey &key, RoundRoute &out) {
+    TuningTable &t = table();
+    std::lock_guard<std::mutex> lock(t.mu);
+    load_env_locked(t);
+    auto it = t.rounds.find(key);
+    if (it == t.rounds.end()) return false;
+    out = it->second.route;
+    return true;
+}
+
+void sumcheck_route_store(const RoundKey &key, const RoundRoute &route, double us) {
+    TuningTable &t = table();
+    std::lock_guard<std::mutex> lock(t.mu);
+    load_env_locked(t);
+    t.rounds[key] = RouteEntry{route, us};
+}
+
+}  // namespace hp
+
 extern "C" HpCudaStatus hp_cuda_v1_msm_tuning_save(const char *path) {
     return guard([&] {
         require(path != nullptr);
@@ -503,6 +549,12 @@ extern "C" HpCudaStatus hp_cuda_v1_msm_tuning_save(const char *path) {
             std::snprintf(line, sizeof line, "many %d %u %.4f\n", kv.first, kv.second.chunk, kv.second.ms);
             f << line;
         }
+        for (const auto &kv : t.rounds) {
+            std::snprintf(line, sizeof line, "round %d %d %d %d %u %u %.2f\n", kv.first.log2_pairs,
+                          kv.first.max_arity, kv.first.slots, kv.first.fold, unsigned(kv.second.route.kernel),
+                          unsigned(kv.second.route.per_sm), kv.second.us);
+            f << line;
+        }
         f.flush();
         require(bool(f));
     });
@@ -511,18 +563,14 @@ extern "C" HpCudaStatus hp_cuda_v1_msm_tuning_save(const char *path) {
 extern "C" HpCudaStatus hp_cuda_v1_msm_tuning_load(const char *path, const char *device) {
     return guard([&] {
         require(path != nullptr);
-        std::map<int, hp::AloneEntry> alone;
-        std::map<int, hp::ManyEntry> many;
-        std::string file_device;
-        if (!hp::parse_file(path, alone, many, file_device)) fail(HP_CUDA_STATUS_INVALID_PARAMETERS);
-        if (device && file_device != "any" && file_device != hp::device_token(device))
+        hp::Parsed parsed;
+        if (!hp::parse_file(path, parsed)) fail(HP_CUDA_STATUS_INVALID_PARAMETERS);
+        if (device && parsed.device != "any" && parsed.device != hp::device_token(device))
             fail(HP_CUDA_STATUS_INVALID_PARAMETERS);
         hp::TuningTable &t = hp::table();
         std::lock_guard<std::mutex> lock(t.mu);
         hp::load_env_locked(t);
-        for (auto &kv : alone) t.alone[kv.first] = kv.second;
-        for (auto &kv : many) t.many[kv.first] = kv.second;
-        t.device = file_device;
+        hp::merge_into(t, parsed);
     });
 }
 
@@ -532,6 +580,7 @@ extern "C" HpCudaStatus hp_cuda_v1_msm_tuning_clear(void) {
         std::lock_guard<std::mutex> lock(t.mu);
         t.alone.clear();
         t.many.clear();
+        t.rounds.clear();
         t.device = "any";
         t.env_checked = true;  // a cleared table stays empty
     });

@@ -1,5 +1,14 @@
-"""MSM autotuner: the Python face of hp_cuda_v1_msm_autotune and the tuning
-table entries of include/hp_cuda.h (csrc/tune.cu).
+"""Autotuners: the Python face of hp_cuda_v1_msm_autotune,
+hp_cuda_v1_sumcheck_autotune and the tuning table entries of
+include/hp_cuda.h (csrc/tune.cu, csrc/sumcheck.cu).
+
+Sumcheck rounds: every round can run on several kernel families, each with
+its own grid; `autotune_sumcheck` measures them for the rounds of one
+virtual polynomial's shape (keyed by ceil(log2 pairs), the largest product
+arity and the slot count) and records the fastest in the same table (saved
+and loaded with the MSM entries).  A route never changes a round message:
+the tuner compares every candidate's message with the built-in rule's.
+
 
 The MSM's window width c, reduction segment length and accumulation chunk
 length come from a process-wide table of measured entries, else from the size
@@ -54,6 +63,68 @@ def autotune(backend, prover_param, num_vars: Sequence[int], mode: int = ALONE) 
                  "msm_autotune")
     return [Tuning(int(t.size), int(t.mode), int(t.window_bits), int(t.segment), int(t.chunk),
                    float(t.model_ms), float(t.tuned_ms)) for t in out]
+
+
+ROUTE_KERNELS = {1: "one block", 2: "pair per thread", 3: "(slot, pair)", 4: "(slot, pair), fused fold",
+                 5: "(product, pair)", 6: "(product, pair), fused fold"}
+
+
+@dataclasses.dataclass(frozen=True)
+class RoundTuning:
+    pairs: int
+    kernel: int
+    blocks_per_sm: int
+    default_kernel: int
+    default_blocks_per_sm: int
+    default_us: float   # median device time of the built-in rule's route
+    tuned_us: float     # median device time of the chosen route
+
+
+def autotune_sumcheck(backend, polynomial) -> list[RoundTuning]:
+    """Measure the round routes of `polynomial`'s shape on a throwaway prover
+    state (the polynomial's MLEs are read, never changed) and record the
+    fastest route of every round size in the tuning table."""
+    lib = _native.load()
+    state = backend.prover_init(polynomial)
+    nv = polynomial.aux_info.num_variables
+    out = (_native.RoundTuning * max(1, nv))()
+    count = ctypes.c_size_t()
+    check_status(lib.hp_cuda_v1_sumcheck_autotune(backend.ctx.raw, state.raw, out, nv, ctypes.byref(count)),
+                 "sumcheck_autotune")
+    return [RoundTuning(int(t.pairs), int(t.kernel), int(t.blocks_per_sm), int(t.default_kernel),
+                        int(t.default_blocks_per_sm), float(t.default_us), float(t.tuned_us))
+            for t in out[:count.value]]
+
+
+class SumcheckTuningBackend:
+    """A backend view that tunes the round routes of every new sumcheck shape
+    it sees (autotune_sumcheck on a throwaway state) before the prover state
+    is created; everything else goes to `backend` unchanged.  Running one
+    proof through it tunes all of the proof's sumcheck shapes."""
+
+    def __init__(self, backend):
+        self._backend = backend
+        self.tuned: dict = {}
+
+    def __getattr__(self, name):
+        return getattr(self._backend, name)
+
+    def prover_init(self, polynomial):
+        key = (polynomial.aux_info.num_variables,
+               max(len(ix) for _, ix in polynomial.products) if polynomial.products else 0,
+               sum(len(ix) + 1 for _, ix in polynomial.products))
+        if polynomial.products and key not in self.tuned:
+            self.tuned[key] = autotune_sumcheck(self._backend, polynomial)
+        return self._backend.prover_init(polynomial)
+
+
+def route(pairs: int, max_arity: int, slots: int, fold: bool = True) -> tuple[int, int]:
+    """(kernel, blocks per SM) a round of `pairs` pairs of this shape takes now
+    (fold: a round after the first, which folds the previous challenge in)."""
+    out = (ctypes.c_uint32 * 2)()
+    check_status(_native.load().hp_cuda_v1_sumcheck_route_query(pairs, max_arity, slots, 1 if fold else 0, out),
+                 "sumcheck_route_query")
+    return int(out[0]), int(out[1])
 
 
 def query(mode: int, size: int) -> tuple[int, int, int]:
@@ -115,11 +186,22 @@ def main(argv=None) -> None:
     ap.add_argument("--alone", default="4:22")
     ap.add_argument("--shared", action="append", default=[])
     ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--prove-num-vars", type=int, action="append", default=[],
+                    help="tune the sumcheck round routes of a proof of 2^NV gates (repeatable)")
     ap.add_argument("--out", required=True)
     args = ap.parse_args(argv)
     from .backend import CudaBackend
     be = CudaBackend(args.device)
     nv = args.srs_num_vars
+    for pnv in args.prove_num_vars:
+        from . import snark
+        sel, wit, perm, pub = snark.vanilla_fixture(pnv, 2)
+        view = SumcheckTuningBackend(be)
+        pk = snark.preprocess(be, pnv, min(16, 1 << pnv), sel, perm, be.generate_srs(pnv, 0), commit=False)
+        snark.prove(view, pk, pub, wit)
+        for key, recs in view.tuned.items():
+            for r in recs:
+                print(json.dumps({"shape": key} | dataclasses.asdict(r)), flush=True)
     params = be.prepare_prover_param(nv, be.generate_srs(nv, 0))
     alone = [k for k in _parse_range(args.alone) if k <= nv]
     for e in autotune(be, params, alone):

@@ -384,6 +384,37 @@ HpCudaStatus hp_cuda_v1_msm_tuning_save(const char *path);
 HpCudaStatus hp_cuda_v1_msm_tuning_load(const char *path, const char *device);
 HpCudaStatus hp_cuda_v1_msm_tuning_clear(void);
 
+/* Sumcheck round autotuner (no counterpart in the reference, which fixes its
+ * kernel geometry by plan).  A round can run on several kernel families --
+ * one block (<= 64 pairs), one pair per thread, (slot, pair) items with a
+ * separate or a fused fold, (product, pair) items with a separate or a fused
+ * fold -- each with its own grid (blocks per SM).  sumcheck_autotune runs
+ * every round of `state` (a fresh prover state, which it consumes: destroy
+ * it afterwards) once per candidate, times each as the median of a few runs,
+ * checks that every candidate's round message equals the built-in rule's
+ * (InvalidState otherwise, the state poisoned), stores the fastest route for
+ * the round's key -- ceil(log2 pairs), largest product arity, slot count,
+ * whether the round folds the previous challenge (every round but the first) --
+ * in the process-wide tuning table (saved and loaded with the MSM entries by
+ * msm_tuning_save / _load; msm_tuning_clear empties it), and writes one
+ * record per round (capacity >= num_vars).  Later rounds of any state with
+ * the same key take the stored route.  sumcheck_route_query: the route
+ * (out2 = kernel, blocks per SM) a round of `pairs` pairs of that shape
+ * (fold != 0: a round after the first) would take now (kernel codes: 1 one block, 2 one pair per thread, 3
+ * (slot, pair), 4 (slot, pair) with fused fold, 5 (product, pair), 6
+ * (product, pair) with fused fold). */
+typedef struct HpCudaRoundTuning {
+    uint64_t pairs;
+    uint32_t kernel, blocks_per_sm;
+    uint32_t default_kernel, default_blocks_per_sm;
+    double default_us; /* median device time of the built-in rule's route */
+    double tuned_us;   /* median device time of the chosen route */
+} HpCudaRoundTuning;
+HpCudaStatus hp_cuda_v1_sumcheck_autotune(HpCudaContext *ctx, HpCudaSumCheckProverState *state,
+                                          HpCudaRoundTuning *out, size_t capacity, size_t *out_count);
+HpCudaStatus hp_cuda_v1_sumcheck_route_query(size_t pairs, int32_t max_arity, int32_t slots, int32_t fold,
+                                             uint32_t *out2);
+
 /* Runtime audit and failure injection (test support; no counterpart in the
  * reference's bridge -- its native tests wrap the runtime's copy, sync and
  * allocation calls at link time, backend/src/ascend910b3/native/

@@ -182,8 +182,11 @@ def test_builtin_gb300_table_parses(tuning, tmp_path):
             c, seg, chunk = int(f[2]), int(f[3]), int(f[4])
             assert window_fits(n, c)
             assert tuning.query(tuning.ALONE, n) == (c, seg, chunk), line
-        else:
+        elif f[0] == "many":
             assert tuning.query(tuning.SHARED, 1 << int(f[1]))[2] == int(f[2]), line
+        else:
+            k, arity, slots, fold, kernel, per_sm = (int(x) for x in f[1:7])
+            assert tuning.route(1 << k, arity, slots, fold=bool(fold)) == (kernel, per_sm), line
     # the headline sizes keep the size rule's geometry
     assert tuning.query(tuning.ALONE, 1 << 20) == (20, 16, 32)
 
@@ -282,3 +285,95 @@ def test_autotune_refuses_geometry_overrides(gpu, oracle, tuning, monkeypatch):
     monkeypatch.setenv("HP_MSM_SEG", "4")
     with pytest.raises(InvalidState):
         tuning.autotune(gpu, pg, [6])
+
+
+# ---------------------------------------------------------------------------
+# sumcheck round routes (csrc/sumcheck.cu, same table and file)
+# ---------------------------------------------------------------------------
+
+ONE_BLOCK, PER_PAIR, SLOT, SLOT_FUSED, PP, PP_FUSED = 1, 2, 3, 4, 5, 6
+
+
+def test_round_routes_without_entries_are_the_built_in_rules(tuning):
+    # degree-2 products of arity 2, 12 slots (the sumcheck workload's shape)
+    assert tuning.route(1 << 19, 2, 12) == (PP, 4)
+    assert tuning.route(1 << 16, 2, 12) == (PP, 4)
+    assert tuning.route(1 << 15, 2, 12) == (SLOT, 16)
+    assert tuning.route(1 << 13, 2, 12) == (SLOT_FUSED, 0)
+    assert tuning.route(65, 2, 12) == (SLOT_FUSED, 0)
+    assert tuning.route(64, 2, 12) == (ONE_BLOCK, 0)
+    # arity 4 and 5 (the zero-checks): separate fold in the middle rounds
+    assert tuning.route(1 << 19, 5, 18) == (SLOT, 16)
+    assert tuning.route(1 << 10, 4, 20) == (SLOT, 0)
+    # products of arity above 8 keep the (slot, pair) kernel even when small
+    assert tuning.route(8, 34, 35) == (SLOT, 0)
+
+
+def test_round_route_file_round_trip_and_validity(tuning, tmp_path):
+    f = _write(tmp_path / "t.txt", ["hp_cuda msm tuning 1", "device any",
+                                    "round 19 2 12 1 3 8 120.5",
+                                    "round 10 2 12 1 2 0 30.0",
+                                    "round 12 5 18 1 5 3 40.0"])  # (product, pair) cannot run arity 5
+    tuning.load(f)
+    assert tuning.route(1 << 19, 2, 12) == (SLOT, 8)
+    assert tuning.route((1 << 18) + 1, 2, 12) == (SLOT, 8)  # ceil(log2 pairs) = 19
+    assert tuning.route(1 << 10, 2, 12) == (PER_PAIR, 0)
+    assert tuning.route(1 << 12, 5, 18) == (SLOT, 0)  # invalid entry: the built-in rule
+    assert tuning.route(1 << 10, 2, 13) == (SLOT_FUSED, 0)  # other key
+    assert tuning.route(1 << 19, 2, 12, fold=False) == (PP, 4)  # the first round is another key
+    out = tmp_path / "out.txt"
+    tuning.save(out)
+    lines = out.read_text().splitlines()
+    assert "round 19 2 12 1 3 8 120.50" in lines and "round 10 2 12 1 2 0 30.00" in lines
+    tuning.clear()
+    assert tuning.route(1 << 19, 2, 12) == (PP, 4)
+    tuning.load(out)
+    assert tuning.route(1 << 19, 2, 12) == (SLOT, 8)
+
+
+@pytest.mark.parametrize("bad", ["round 19 2 12 1 7 8 1.0", "round 19 2 12 1 0 8 1.0", "round 19 2 12 1 3 99 1.0",
+                                 "round 19 0 12 1 3 8 1.0", "round 19 2 12 2 3 8 1.0", "round 19 2 12 1 3 8",
+                                 "round 19 2 12 1 3 8 1.0 x"])
+def test_malformed_round_lines_are_rejected(tuning, tmp_path, bad):
+    from hyperplonk_gb300.errors import InvalidParameters
+    f = _write(tmp_path / "bad.txt", ["hp_cuda msm tuning 1", "device any", bad])
+    with pytest.raises(InvalidParameters):
+        tuning.load(f)
+    assert tuning.route(1 << 19, 2, 12) == (PP, 4)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("arities,nv", [((2, 2, 2, 2), 13), ((3, 4, 5, 2), 11)])
+def test_sumcheck_autotune_then_rounds_equal_oracle(gpu, cpu, oracle, tuning, arities, nv):
+    """Tune the routes of a shape on one state, then prove another state of
+    the same shape round by round: every message equals the oracle's, and the
+    rounds took the stored routes."""
+    from hyperplonk_gb300.virtual_polynomial import VirtualPolynomial
+    R = 0x73EDA753299D7D483339D80809A1D80553BDA402FFFE5BFEFFFFFFFF00000001
+    rng = random.Random(sum(arities) + nv)
+    nf = 6
+    tables = [oracle.random_fr(400 + nv, 1 << nv, first=j << nv) for j in range(nf)]
+    products = [(rng.randrange(1, R), [rng.randrange(nf) for _ in range(m)]) for m in arities]
+
+    def vp_for(be, mles):
+        vp = VirtualPolynomial(nv)
+        for c, ix in products:
+            vp.add_mle_list([mles[i] for i in ix], c)
+        return vp
+
+    gm = [gpu.mle_from_evaluations(nv, t) for t in tables]
+    cm = [cpu.mle_from_evaluations(nv, t) for t in tables]
+    records = tuning.autotune_sumcheck(gpu, vp_for(gpu, gm))
+    assert [r.pairs for r in records] == [1 << (nv - 1 - k) for k in range(nv)]
+    vg = vp_for(gpu, gm)
+    slots = sum(len(ix) + 1 for _, ix in vg.products)
+    max_arity = max(len(ix) for _, ix in vg.products)
+    for k, r in enumerate(records):
+        assert r.tuned_us <= r.default_us
+        assert tuning.route(r.pairs, max_arity, slots, fold=k > 0) == (r.kernel, r.blocks_per_sm)
+    sg, sc = gpu.prover_init(vg), cpu.prover_init(vp_for(cpu, cm))
+    ch = None
+    for k in range(nv):
+        assert gpu.prove_round_and_update_state(sg, ch) == cpu.prove_round_and_update_state(sc, ch), k
+        ch = rng.randrange(R)
+    assert gpu.final_evaluations(sg, ch) == cpu.final_evaluations(sc, ch)
