@@ -58,6 +58,8 @@ SIGNATURES: dict[str, list] = {
     "hp_cuda_v1_context_stream": [c_voidp, c_voidpp],
     "hp_cuda_v1_mle_upload": [c_voidp, c_size, c_u8p, c_size, c_voidpp],
     "hp_cuda_v1_mle_upload_many": [c_voidp, c_size, ctypes.POINTER(c_u8p), c_size, c_size, c_voidpp],
+    "hp_cuda_v1_mle_upload_async": [c_voidp, c_size, ctypes.POINTER(c_u8p), c_size, c_size, c_voidpp],
+    "hp_cuda_v1_mle_upload_wait": [c_voidp, c_voidpp, c_size],
     "hp_cuda_v1_mle_download": [c_voidp, c_voidp, c_size, c_u8p, c_size],
     "hp_cuda_v1_mle_linear_combination": [c_voidp, c_size, c_voidpp, c_u8p, c_size, c_voidpp],
     "hp_cuda_v1_mle_evaluate": [c_voidp, c_voidp, c_size, c_u8p, c_u8p],

@@ -202,6 +202,31 @@ class CudaSumCheckProverState:
             _destroy_or_abort("sumcheck_prover_state_destroy", status)
 
 
+class AsyncUpload:
+    """Tables of one hp_cuda_v1_mle_upload_async call: `mles` are usable at
+    once (device work waits for the copies); wait() blocks until the upload is
+    complete, checks the encoding (InvalidParameters on a non-canonical
+    element, the tables then released) and lets go of the host buffers."""
+
+    def __init__(self, backend: "CudaBackend", mles: list, host_buffers: list):
+        self.backend, self.mles, self._host = backend, mles, host_buffers
+
+    def wait(self) -> list:
+        if self._host is not None:
+            arr = _addr_array(self.mles)
+            try:
+                check_status(self.backend.lib.hp_cuda_v1_mle_upload_wait(self.backend.ctx.raw, arr, len(self.mles)),
+                             "mle_upload_wait")
+            except InvalidParameters:
+                for m in self.mles:  # the library released them
+                    m._addr = 0
+                self.mles = []
+                raise
+            finally:
+                self._host = None
+        return self.mles
+
+
 def _addr_array(mles: Sequence[CudaMle]):
     arr = (ctypes.c_void_p * max(1, len(mles)))()
     for i, m in enumerate(mles):
@@ -253,6 +278,25 @@ class CudaBackend:
         check_status(self.lib.hp_cuda_v1_mle_upload_many(self.ctx.raw, num_vars, ptrs, len(datas), 1 << num_vars,
                                                          out), "mle_upload_many")
         return [self._new(ctypes.c_void_p(a), num_vars) for a in out]
+
+    def mle_upload_async(self, num_vars: int, tables: Sequence) -> "AsyncUpload":
+        """Queue the upload of several tables of one size on the context's
+        ingress stream and return at once (hp_cuda_v1_mle_upload_async): work
+        queued later on the tables waits for the upload on the device, so the
+        copies overlap whatever the context is computing.  The tables should
+        be pinned host memory (else the copies are synchronous).  Call wait()
+        on the result before trusting results computed from the tables: it
+        checks the encoding and releases the host buffers."""
+        datas = [table_bytes(t) for t in tables]
+        for d in datas:
+            n = _nbytes(d)
+            if num_vars >= 64 or n % 32 or n // 32 != (1 << num_vars):
+                raise InvalidParameters(f"evaluation count {n // 32} does not match {num_vars} variables")
+        ptrs = (_native.c_u8p * max(1, len(datas)))(*[_native.buf(d) for d in datas])
+        out = (ctypes.c_void_p * max(1, len(datas)))()
+        check_status(self.lib.hp_cuda_v1_mle_upload_async(self.ctx.raw, num_vars, ptrs, len(datas), 1 << num_vars,
+                                                          out), "mle_upload_async")
+        return AsyncUpload(self, [self._new(ctypes.c_void_p(a), num_vars) for a in out[:len(datas)]], datas)
 
     def generate_srs(self, num_vars: int, seed: int) -> list:
         """Testing SRS of num_vars variables from fixture seed `seed`, computed

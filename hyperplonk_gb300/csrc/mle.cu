@@ -477,6 +477,95 @@ extern "C" HpCudaStatus hp_cuda_v1_mle_upload_many(HpCudaContext *ctx, size_t nu
     });
 }
 
+extern "C" HpCudaStatus hp_cuda_v1_mle_upload_async(HpCudaContext *ctx, size_t num_vars,
+                                                    const uint8_t *const *evaluations, size_t count,
+                                                    size_t evaluation_count, HpCudaDeviceAddress *out) {
+    if (out)
+        for (size_t i = 0; i < count; i++) out[i] = nullptr;
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(out != nullptr && (count == 0 || evaluations != nullptr) && num_vars <= hp::kMaxNumVars);
+        const size_t n = table_len(num_vars);
+        require(evaluation_count == n);
+        for (size_t i = 0; i < count; i++) require(evaluations[i] != nullptr);
+        if (count == 0) return;
+        // Everything of this call runs on the ingress stream, after what the
+        // context stream holds now (the new buffers' previous owners are
+        // done with them): allocation, copies, conversions, the flag copy
+        // into the call's pinned slot, then the event that work on these
+        // tables waits for.  The host returns at once.
+        std::shared_ptr<HpCudaIngress> in = ctx->new_ingress();
+        const cudaStream_t st = ctx->ingress_stream;
+        cudaEvent_t after_ctx = nullptr;
+        check_cuda(cudaEventCreateWithFlags(&after_ctx, cudaEventDisableTiming));
+        struct EventGuard {
+            cudaEvent_t e;
+            ~EventGuard() { cudaEventDestroy(e); }
+        } eg{after_ctx};
+        check_cuda(cudaEventRecord(after_ctx, ctx->stream));
+        check_cuda(cudaStreamWaitEvent(st, after_ctx, 0));
+        std::vector<void *> ptrs;
+        try {
+            void *dflag = ctx->scratch(16, st);
+            ptrs.reserve(count);
+            for (size_t i = 0; i < count; i++) ptrs.push_back(ctx->scratch(n * kFrBytes, st));
+            check_cuda(cudaMemsetAsync(dflag, 0, sizeof(uint32_t), st));
+            for (size_t i = 0; i < count; i++) {
+                check_cuda(cudaMemcpyAsync(ptrs[i], evaluations[i], n * kFrBytes, cudaMemcpyHostToDevice, st));
+                hp::k_to_mont_check<<<hp::grid_for(ctx, n, 256), 256, 0, st>>>(static_cast<Fr *>(ptrs[i]), n,
+                                                                                static_cast<uint32_t *>(dflag));
+                check_launch();
+            }
+            check_cuda(cudaMemcpyAsync(ctx->ingress_flags_h + in->slot, dflag, sizeof(uint32_t),
+                                       cudaMemcpyDeviceToHost, st));
+            ctx->scratch_free(dflag, st);
+            check_cuda(cudaEventRecord(in->ready, st));
+            for (void *p : ptrs) ctx->buffers.emplace(p, HpCudaContext::Buffer{n * kFrBytes, 1, true, in});
+        } catch (...) {
+            for (void *p : ptrs) {
+                ctx->buffers.erase(p);
+                cudaFreeAsync(p, st);
+            }
+            throw;
+        }
+        for (size_t i = 0; i < count; i++) out[i] = ptrs[i];
+    });
+}
+
+extern "C" HpCudaStatus hp_cuda_v1_mle_upload_wait(HpCudaContext *ctx, const HpCudaDeviceAddress *tables,
+                                                   size_t count) {
+    return guard([&] {
+        hp::require_ctx(ctx);
+        require(count == 0 || tables != nullptr);
+        for (size_t i = 0; i < count; i++) require(tables[i] != nullptr && ctx->owns(tables[i]));
+        // every distinct upload these tables came from: wait for it and read its flag
+        std::vector<std::shared_ptr<HpCudaIngress>> ins;
+        for (size_t i = 0; i < count; i++) {
+            auto &b = ctx->buffers.at(tables[i]);
+            if (b.ingress && std::find(ins.begin(), ins.end(), b.ingress) == ins.end()) ins.push_back(b.ingress);
+        }
+        std::vector<std::shared_ptr<HpCudaIngress>> bad;
+        for (auto &in : ins) {
+            check_cuda(cudaEventSynchronize(in->ready));
+            if (ctx->ingress_flags_h[in->slot] & hp::kFlagNonCanonical) bad.push_back(in);
+        }
+        if (!bad.empty()) {
+            // a non-canonical element: every table of the failing uploads is released
+            std::vector<void *> victims;
+            for (auto &kv : ctx->buffers)
+                if (kv.second.ingress && kv.second.public_handle &&
+                    std::find(bad.begin(), bad.end(), kv.second.ingress) != bad.end())
+                    victims.push_back(kv.first);
+            for (void *p : victims) ctx->retire(p);
+            fail(HP_CUDA_STATUS_INVALID_PARAMETERS);
+        }
+        // validated and written: later work need not wait for these uploads
+        for (auto &kv : ctx->buffers)
+            if (kv.second.ingress && std::find(ins.begin(), ins.end(), kv.second.ingress) != ins.end())
+                kv.second.ingress.reset();
+    });
+}
+
 extern "C" HpCudaStatus hp_cuda_v1_mle_download(HpCudaContext *ctx, HpCudaDeviceAddress polynomial,
                                                 size_t num_vars, uint8_t *out_evaluations,
                                                 size_t evaluation_count) {

@@ -89,9 +89,40 @@ void HpCudaContext::unref(void *p) {
     auto it = buffers.find(p);
     if (it == buffers.end()) fail(HP_CUDA_STATUS_INVALID_PARAMETERS);
     if (--it->second.refs == 0) {
+        // a buffer an asynchronous upload may still write is freed after it
+        if (it->second.ingress) check_cuda(cudaStreamWaitEvent(stream, it->second.ingress->ready, 0));
         buffers.erase(it);
         check_cuda(cudaFreeAsync(p, stream));
     }
+}
+
+void HpCudaContext::await_ingress(void *p) {
+    auto it = buffers.find(p);
+    if (it != buffers.end() && it->second.ingress)
+        check_cuda(cudaStreamWaitEvent(stream, it->second.ingress->ready, 0));
+}
+
+std::shared_ptr<HpCudaIngress> HpCudaContext::new_ingress() {
+    if (!ingress_stream) check_cuda(cudaStreamCreateWithFlags(&ingress_stream, cudaStreamNonBlocking));
+    if (!ingress_flags_h) {
+        void *h = nullptr;
+        check_cuda(cudaHostAlloc(&h, kIngressSlots * sizeof(uint32_t), cudaHostAllocDefault));
+        ingress_flags_h = static_cast<uint32_t *>(h);
+    }
+    int slot = -1;
+    for (int i = 0; i < kIngressSlots; i++)
+        if (!ingress_used[i]) {
+            slot = i;
+            break;
+        }
+    if (slot < 0) fail(HP_CUDA_STATUS_INVALID_STATE);  // too many uploads not yet waited for
+    auto in = std::make_shared<HpCudaIngress>();
+    check_cuda(cudaEventCreateWithFlags(&in->ready, cudaEventDisableTiming));
+    in->slot = slot;
+    in->slot_used = &ingress_used[slot];
+    ingress_used[slot] = true;
+    ingress_flags_h[slot] = 0;
+    return in;
 }
 
 void HpCudaContext::retire(void *p) {
@@ -207,6 +238,7 @@ extern "C" HpCudaStatus hp_cuda_v1_context_destroy(HpCudaContext *ctx) {
     return guard([&] {
         require(ctx != nullptr);
         cudaSetDevice(ctx->device);
+        if (ctx->ingress_stream) cudaStreamSynchronize(ctx->ingress_stream);
         cudaError_t first = cudaStreamSynchronize(ctx->stream);
         for (auto &kv : ctx->buffers) cudaFreeAsync(kv.first, ctx->stream);
         ctx->buffers.clear();
@@ -225,6 +257,8 @@ extern "C" HpCudaStatus hp_cuda_v1_context_destroy(HpCudaContext *ctx) {
         cudaFree(ctx->d_flags);
         cudaFreeHost(ctx->h_flags);
         if (ctx->h_mailbox) cudaFreeHost(ctx->h_mailbox);
+        if (ctx->ingress_flags_h) cudaFreeHost(ctx->ingress_flags_h);
+        if (ctx->ingress_stream) cudaStreamDestroy(ctx->ingress_stream);
         cudaStreamDestroy(ctx->stream);
         cudaMemPoolDestroy(ctx->pool);
         delete ctx;

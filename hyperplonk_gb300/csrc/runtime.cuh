@@ -17,6 +17,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <map>
+#include <memory>
 #include <new>
 #include <string>
 #include <unordered_map>
@@ -71,6 +72,22 @@ inline size_t table_len(size_t num_vars) { return size_t(1) << num_vars; }
 
 }  // namespace hp
 
+// One asynchronous upload call (hp_cuda_v1_mle_upload_async): the event its
+// copies and conversions end with on the ingress stream, and its slot in the
+// context's pinned flag words (non-canonical input seen).
+struct HpCudaIngress {
+    cudaEvent_t ready = nullptr;
+    int slot = -1;
+    bool *slot_used = nullptr;  // the context's slot flag, freed with this record
+    HpCudaIngress() = default;
+    HpCudaIngress(const HpCudaIngress &) = delete;
+    HpCudaIngress &operator=(const HpCudaIngress &) = delete;
+    ~HpCudaIngress() {
+        if (ready) cudaEventDestroy(ready);
+        if (slot_used) *slot_used = false;
+    }
+};
+
 struct HpCudaContext {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -82,8 +99,21 @@ struct HpCudaContext {
         size_t bytes;
         int refs;
         bool public_handle;  // still owned by the caller (not yet retired)
+        std::shared_ptr<HpCudaIngress> ingress;  // set while an asynchronous upload may still write it
     };
     std::unordered_map<void *, Buffer> buffers;
+    // Asynchronous uploads: their own stream, and pinned host words that each
+    // upload's validation flag is copied into, one per upload call whose
+    // buffers are still pending (created on first use).
+    static constexpr int kIngressSlots = 256;
+    cudaStream_t ingress_stream = nullptr;
+    uint32_t *ingress_flags_h = nullptr;
+    bool ingress_used[kIngressSlots] = {};
+    // Make `stream` wait for the asynchronous upload that writes `p`, if any.
+    void await_ingress(void *p);
+    // Event and flag slot for a new asynchronous upload (both released when
+    // the last buffer holding the record lets go of it).
+    std::shared_ptr<HpCudaIngress> new_ingress();
 
     // Worker streams for independent work inside one call (fork from and
     // join back into `stream` with events; created on first use).
@@ -200,11 +230,14 @@ inline void require_ctx(HpCudaContext *ctx) {
     check_cuda(cudaSetDevice(ctx->device));
 }
 
-// A registered MLE buffer of exactly 2^num_vars Fr.
+// A registered MLE buffer of exactly 2^num_vars Fr.  When an asynchronous
+// upload may still be writing it, the context stream waits for that upload
+// (on the device): work queued after this call reads the uploaded values.
 inline Fr *mle_ptr(HpCudaContext *ctx, HpCudaDeviceAddress a, size_t num_vars) {
     require(a != nullptr && num_vars <= kMaxNumVars);
     require(ctx->owns(a));
     require(ctx->bytes_of(a) == table_len(num_vars) * kFrBytes);
+    ctx->await_ingress(a);
     return static_cast<Fr *>(a);
 }
 

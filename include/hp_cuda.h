@@ -215,6 +215,27 @@ HpCudaStatus hp_cuda_v1_batch_sumcheck_round(HpCudaContext *ctx, HpCudaSumCheckP
                                              uint8_t *const *out_evaluations, const size_t *evaluation_counts,
                                              size_t count);
 
+/* Asynchronous upload of `count` tables of 2^num_vars canonical Fr, for
+ * witness ingress that overlaps the context's computation (no counterpart in
+ * the reference, whose upload returns after its copy).  The copies from
+ * `evaluations` (pinned host memory, so the copies run asynchronously) and
+ * the conversions run on the context's ingress stream; the call returns at
+ * once with the device addresses.  Every later entry of this context that
+ * reads one of these tables first makes the context stream wait for its
+ * upload on the device (no host synchronisation), so a proof queued now
+ * reads the uploaded values; entries that take raw device pointers
+ * (mle_evaluate_noalloc) do not wait.  The host buffers are borrowed until
+ * upload_wait returns for the tables.  upload_wait blocks until the uploads
+ * of `tables` are complete and checks their encoding: a non-canonical
+ * element is InvalidParameters, and then every table of that upload call is
+ * released (its addresses become invalid); results computed from such tables
+ * before the wait are unspecified.  At most 256 upload calls may be pending
+ * (not yet waited for, with live tables) per context; beyond that
+ * upload_async is InvalidState. */
+HpCudaStatus hp_cuda_v1_mle_upload_async(HpCudaContext *ctx, size_t num_vars, const uint8_t *const *evaluations,
+                                         size_t count, size_t evaluation_count, HpCudaDeviceAddress *out_addresses);
+HpCudaStatus hp_cuda_v1_mle_upload_wait(HpCudaContext *ctx, const HpCudaDeviceAddress *tables, size_t count);
+
 /* Evaluations of `count` resident MLEs, polynomial k at the point of
  * num_vars[k] canonical Fr starting at points + 32 * (num_vars[0] + ... +
  * num_vars[k-1]); writes count canonical Fr.  Each value equals

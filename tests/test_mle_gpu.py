@@ -4,6 +4,8 @@ Mirrors backend/src/ascend910b3/integration_tests.rs (device vs CpuBackend on
 the same inputs) with sizes chosen around the kernels' tile edges."""
 import random
 
+import numpy as np
+
 import pytest
 
 from hyperplonk_gb300.errors import InvalidParameters
@@ -199,3 +201,68 @@ def test_upload_many_equals_single_uploads(gpu, oracle):
         gpu.mle_from_evaluations_many(nv, [tables[0], bytes(bad), tables[1]])
     with pytest.raises(InvalidParameters):
         gpu.mle_from_evaluations_many(nv, [tables[0], tables[1][:-32]])
+
+
+# ---------------------------------------------------------------------------
+# asynchronous upload (ingress stream): hp_cuda_v1_mle_upload_async / _wait
+# ---------------------------------------------------------------------------
+
+def _pinned(table):
+    import torch
+    t = torch.empty(len(table), dtype=torch.uint8, pin_memory=True)
+    t.numpy()[:] = np.frombuffer(table, dtype=np.uint8)
+    return t
+
+
+@pytest.mark.gpu
+def test_async_upload_is_waited_for_on_the_device(gpu, cpu, oracle):
+    nv = 14
+    tables = [oracle.random_fr(90 + j, 1 << nv) for j in range(3)]
+    pinned = [_pinned(t) for t in tables]
+    up = gpu.mle_upload_async(nv, [p.numpy() for p in pinned])
+    # queued before the wait: the linear combination waits for the copies on the device
+    lc = gpu.linear_combination(up.mles, [3, 5, 7])
+    mles = up.wait()
+    assert gpu.download(lc) == cpu.linear_combination([cpu.mle_from_evaluations(nv, t) for t in tables],
+                                                      [3, 5, 7]).evaluations
+    assert [gpu.download(m) for m in mles] == tables
+    assert up.wait() is mles  # a second wait is a no-op
+
+
+@pytest.mark.gpu
+def test_async_upload_rejects_non_canonical_at_wait(gpu, oracle):
+    from hyperplonk_gb300.errors import InvalidParameters
+    nv = 6
+    good = oracle.random_fr(95, 1 << nv)
+    bad = bytearray(good)
+    bad[32 * 7 + 31] = 0xff  # >= r
+    up = gpu.mle_upload_async(nv, [_pinned(good).numpy(), _pinned(bytes(bad)).numpy()])
+    with pytest.raises(InvalidParameters):
+        up.wait()
+    assert up.mles == []
+    # the context keeps working, and a later upload call is independent
+    ok = gpu.mle_upload_async(nv, [_pinned(good).numpy()]).wait()
+    assert gpu.download(ok[0]) == good
+
+
+@pytest.mark.gpu
+def test_pipelined_proofs_equal_proofs_from_blocking_uploads(gpu, oracle):
+    """Proof i+1's witness upload queued before proof i runs: every proof
+    equals the proof of the same witnesses uploaded the blocking way."""
+    from hyperplonk_gb300 import snark
+    nv = 9
+    layers = [oracle.affine_to_packets(l) for l in oracle.srs_layers(nv, 96)]
+    sel, wit, perm, pub = snark.vanilla_fixture(nv, 2)
+    pk = snark.preprocess(gpu, nv, 16, sel, perm, layers, commit=False)
+    witness_sets = [snark.vanilla_witness(nv, 2, (6 << 32) | i) for i in range(3)]
+    pubs = [[int.from_bytes(w[0][32 * j:32 * j + 32].tobytes(), "little") for j in range(16)] for w in witness_sets]
+    pinned = [[_pinned(t.tobytes()).numpy() for t in w] for w in witness_sets]
+    expect = [snark.prove(gpu, pk, p, w).to_bytes() for p, w in zip(pubs, witness_sets)]
+    got = []
+    nxt = gpu.mle_upload_async(nv, pinned[0])
+    for i in range(3):
+        cur = nxt
+        if i + 1 < 3:
+            nxt = gpu.mle_upload_async(nv, pinned[i + 1])
+        got.append(snark.prove(gpu, pk, pubs[i], None, witness_mles=cur.wait()).to_bytes())
+    assert got == expect
