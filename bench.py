@@ -4,7 +4,7 @@
 Workloads (--workload):
 
   prove  (default) -- full HyperPlonk prove of the vanilla-plonk circuit of
-         2^nv gates (configuration 3: q_L, q_R, q_M, q_C, w1, w2 uniform, q_O
+         2^nv gates (q_L, q_R, q_M, q_C, w1, w2 uniform, q_O
          = -1, w3 solving the gate, identity permutation over 3 columns, 16
          public inputs, fixture seed 2, testing SRS of nv variables).  One step
          = one proof through the reference-facing C ABI (witness commits,
@@ -12,8 +12,9 @@ Workloads (--workload):
          proof serialized to bytes.  Metric: HyperPlonk proofs/s, with p50/p99
          proof latency.  The MSM pts/s of a 2^nv commit on the same SRS is
          reported beside it ("msm").
-  commit -- one multilinear-KZG commit of a 2^nv-point MLE (configuration 1
-         shape; nv = 16 is configuration 1 itself).  Metric: MSM pts/s.
+  commit -- one multilinear-KZG commit of a 2^nv-point MLE (the nv = 16
+         commit of stream-0 scalars is the commit workload's stated size).
+         Metric: MSM pts/s.
 
   value : inputs already resident in HBM (witness MLEs uploaded before the
           timed loop);
@@ -896,8 +897,8 @@ def run_gb300(args, world, rank, local, pg):
 
 
 def other_workloads() -> dict:
-    """The batch plan (configuration 4) and the serving stream
-    (configuration 5) measured in the same run, each in a child process of
+    """The batch plan (64 MSMs + 32 sumchecks) and the serving stream
+    (prove requests of 2^16..2^22 gates) measured in the same run, each in a child process of
     this script with its own timed region and clock record; their summaries
     go into the prove line."""
     out = {}
@@ -990,7 +991,7 @@ def run_reference(args, world, rank):
         desc = f"oracle sumcheck prove of the degree-2 instance at 2^{nv} per step"
     else:
         sample, units, metric, unit = CpuProveSample(nv), 1, "HyperPlonk proofs/s", "proofs/s"
-        desc = f"one oracle proof of the configuration-3 circuit at 2^{nv} gates per step"
+        desc = f"one oracle proof of the vanilla-plonk circuit (seed 2) at 2^{nv} gates per step"
     setup_s = time.perf_counter() - t_setup
     for _ in range(args.warmup):
         sample.step()

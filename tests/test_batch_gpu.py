@@ -1,4 +1,4 @@
-"""Batched execution (BASELINE configuration 4 shape, small): many MSMs over
+"""Batched execution (the batch workload's shape, small): many MSMs over
 prefixes of one SRS layer in one call, and many sumcheck instances advanced
 one round per call -- every result must equal the per-instance oracle run."""
 import random
