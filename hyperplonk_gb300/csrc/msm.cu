@@ -674,7 +674,7 @@ __global__ void __launch_bounds__(128) k_msm_segments(const Xyzz *buckets, size_
 
 // Subset sums.  Subset y < bits: { run_j : bit y of j set } (segments/2
 // elements); subset y == bits: every acc_j.  Block (chunk, y) sums elements
-// [chunk * T * per, ...) of subset y into partial[y * chunks + chunk].
+// [chunk * kSubsetPerBlock, ...) of subset y into partial[y * chunks + chunk].
 constexpr int kSubsetThreads = 128;
 constexpr int kSubsetPerThread = 8;
 constexpr int kSubsetPerBlock = kSubsetThreads * kSubsetPerThread;
@@ -682,21 +682,8 @@ constexpr int kSubsetPerBlock = kSubsetThreads * kSubsetPerThread;
 // k_msm_rows sums at most 64 subset blocks per row
 size_t msm_max_segments() { return size_t(64) * kSubsetPerBlock; }
 
-// Elements per thread of the subset sums: the fewest whose chunks fit the
-// 64-column row sums.  Each level of these sums is a dependent XYZZ
-// addition of ~14 us in one thread's chain, so the depth per + log2(128) +
-// log2(chunks) is what a small MSM's tail costs: 2^16 points, 8192 segments:
-// 1 + 7 + 6 levels instead of 8 + 7 + 3 with 8 per thread.
-static int subset_per(size_t segments) {
-    int per = 1;
-    while (per < kSubsetPerThread && (segments + size_t(kSubsetThreads) * per - 1) / (size_t(kSubsetThreads) * per) > 64)
-        per *= 2;
-    return per;
-}
-
 // Blocks of T threads (a power of two <= kSubsetThreads), `per` elements per
-// thread: T = kSubsetThreads and per = subset_per(segments) when there are
-// several chunks; a single
+// thread: T * per = kSubsetPerBlock when there are several chunks; a single
 // chunk of few elements takes fewer threads and elements per thread (the
 // dependent-addition depth is per + log2 T).
 __global__ void __launch_bounds__(kSubsetThreads) k_msm_subsets(const Xyzz *run, const Xyzz *acc,
@@ -781,9 +768,7 @@ void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz 
     k_msm_segments<<<grid_for(ctx, sh.segments, 128, 16), 128, 0, st>>>(buckets.as<Xyzz>(), sh.segments, sh.seg,
                                                                        acc.as<Xyzz>(), run.as<Xyzz>());
     check_launch();
-    const int per_thread = subset_per(sh.segments);
-    const int chunks = int((sh.segments + size_t(kSubsetThreads) * per_thread - 1) /
-                           (size_t(kSubsetThreads) * per_thread));
+    const int chunks = int((sh.segments + kSubsetPerBlock - 1) / kSubsetPerBlock);
     if (chunks == 1) {
         // depth per + log2 T: T = the power of two >= segments, 32..128
         int T = 32;
@@ -797,7 +782,7 @@ void msm_run(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz 
         Scratch partial(ctx, size_t(chunks) * sh.partials * sizeof(Xyzz), st);
         k_msm_subsets<<<dim3(chunks, sh.partials), kSubsetThreads, 0, st>>>(run.as<Xyzz>(), acc.as<Xyzz>(),
                                                                             sh.segments, sh.seg_bits, chunks,
-                                                                            per_thread, partial.as<Xyzz>());
+                                                                            kSubsetPerThread, partial.as<Xyzz>());
         check_launch();
         k_msm_rows<<<sh.partials, 64, 0, st>>>(partial.as<Xyzz>(), chunks, out_partials);
         check_launch();
@@ -948,8 +933,8 @@ static void msm_run_group(HpCudaContext *ctx, const MsmTask *tasks, size_t count
         m.segments = uint32_t(sh.segments);
         m.seg_base = uint32_t(segs);
         m.seg_bits = sh.seg_bits;
-        m.per = subset_per(sh.segments);
-        m.chunks = int((sh.segments + size_t(kSubsetThreads) * m.per - 1) / (size_t(kSubsetThreads) * m.per));
+        m.per = kSubsetPerThread;
+        m.chunks = int((sh.segments + kSubsetPerBlock - 1) / kSubsetPerBlock);
         if (m.chunks > 64) fail(HP_CUDA_STATUS_NOT_IMPLEMENTED);
         m.block_base = uint32_t(blocks);
         m.row_base = uint32_t(rows);
