@@ -24,6 +24,7 @@
 // any slot count go through the (slot, pair) kernel; the per-pair kernel
 // with per-thread slot sums in shared memory remains for HP_BIG_SLOTS=0.
 #include <algorithm>
+#include <chrono>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -487,6 +488,139 @@ __global__ void __launch_bounds__(kSmallThreads) k_sumcheck_round_small(Sumcheck
     }
     __syncthreads();
     finalize_from_sums(desc, sums, weights, degree, out);
+}
+
+// The last rounds of a sumcheck (at most tail_pairs() pairs) in one launch
+// of one block that stays resident between rounds: the factor tables live in
+// shared memory, each round's message goes to pinned, device-mapped host
+// memory followed by a release of its sequence number, and the block waits
+// (bounded, see kTailSpinLimit) for the host's challenge before folding it
+// in and running the next round.  This removes a launch and a stream
+// synchronisation per round from hp_cuda_v1_sumcheck_prove_rounds, whose
+// host side polls the mapped sequence numbers instead; the messages are the
+// same field elements as the one-launch-per-round path's (same node sums,
+// same weight matrix).
+struct TailBox {
+    uint32_t msg_seq;  // messages ready (device writes)
+    uint32_t ch_seq;   // challenges written (host writes)
+    uint32_t error;    // the block gave up waiting for a challenge
+    uint32_t pad[5];
+    Fr challenges[10];  // Montgomery, one per tail round but the last (host writes)
+    Fr messages[10 * (kMaxDegree + 1)];  // canonical (device writes)
+};
+constexpr int kTailThreads = 256;
+constexpr int kTailMaxPairs = 256;  // at most 9 rounds
+constexpr uint32_t kTailSpinLimit = 1u << 24;  // polls of ~128 ns: gives up after about 2-4 s
+
+__device__ __forceinline__ uint32_t load_acquire_sys(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.acquire.sys.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void store_release_sys(uint32_t *p, uint32_t v) {
+    asm volatile("st.release.sys.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+template <int MAXM>
+__global__ void __launch_bounds__(kTailThreads) k_sumcheck_tail(SumcheckDesc desc, FrPtrList src, FrMutPtrList dst,
+                                                                bool fold_first, Fr r0, int pairs0, int rounds,
+                                                                const Fr *weights, int degree, TailBox *box) {
+    extern __shared__ Fr tsm[];
+    __shared__ int abort_round;
+    __shared__ Fr challenge;
+    const int F = desc.factor_count, S = desc.slot_count, P = desc.product_count;
+    const int row = 2 * pairs0;                     // table row stride
+    Fr *tab = tsm;                                  // F x 2 pairs0
+    Fr *tmp = tab + size_t(F) * row;                // F x pairs0 (fold staging)
+    Fr *vals = tmp + size_t(F) * pairs0;            // S x pairs0
+    Fr *sums = vals + size_t(S) * pairs0;           // S
+    int pairs = pairs0;
+    for (int idx = threadIdx.x; idx < F * 2 * pairs; idx += blockDim.x) {
+        const int f = idx / (2 * pairs), e = idx - f * 2 * pairs;
+        Fr v;
+        if (fold_first) {
+            const Fr a0 = load_fr(src.p[f] + 2 * e), a1 = load_fr(src.p[f] + 2 * e + 1);
+            v = a0 + r0 * (a1 - a0);
+        } else {
+            v = load_fr(src.p[f] + e);
+        }
+        tab[f * row + e] = v;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+    for (int j = 0; j < rounds; j++) {
+        for (int idx = threadIdx.x; idx < P * pairs; idx += blockDim.x) {
+            const int p = idx / pairs, b = idx - p * pairs;
+            const int begin = desc.offsets[p], m = desc.offsets[p + 1] - begin, slot = desc.slot_base[p];
+            Fr e[MAXM], st[MAXM];
+#pragma unroll
+            for (int q = 0; q < MAXM; q++) {
+                if (q < m) {
+                    const Fr *t = tab + desc.indices[begin + q] * row + 2 * b;
+                    e[q] = t[0];
+                    st[q] = t[1] - e[q];
+                }
+            }
+            for (int k = 0; k <= m; k++) {
+                if (k > 0) {
+#pragma unroll
+                    for (int q = 0; q < MAXM; q++)
+                        if (q < m) e[q] = e[q] + st[q];
+                }
+                Fr v = e[0];
+#pragma unroll
+                for (int q = 1; q < MAXM; q++)
+                    if (q < m) v = v * e[q];
+                vals[(slot + k) * pairs0 + b] = v;
+            }
+        }
+        __syncthreads();
+        for (int sl = warp; sl < S; sl += warps) {
+            Fr a = Fr::zero();
+            for (int b = lane; b < pairs; b += 32) a = a + vals[sl * pairs0 + b];
+            a = warp_sum(a);
+            if (lane == 0) sums[sl] = a;
+        }
+        __syncthreads();
+        finalize_from_sums(desc, sums, weights, degree, box->messages + size_t(j) * (degree + 1));
+        __threadfence_system();
+        __syncthreads();
+        if (threadIdx.x == 0) store_release_sys(&box->msg_seq, uint32_t(j + 1));
+        if (j + 1 == rounds) break;
+        if (threadIdx.x == 0) {
+            uint32_t it = 0;
+            while (load_acquire_sys(&box->ch_seq) < uint32_t(j + 1) && ++it < kTailSpinLimit) __nanosleep(128);
+            abort_round = it >= kTailSpinLimit;
+            if (abort_round) {
+                store_release_sys(&box->error, 1u);
+            } else {
+                const volatile uint32_t *c = reinterpret_cast<const volatile uint32_t *>(&box->challenges[j]);
+#pragma unroll
+                for (int w = 0; w < 8; w++) challenge.v[w] = c[w];
+            }
+        }
+        __syncthreads();
+        if (abort_round) return;
+        const Fr r = challenge;
+        for (int idx = threadIdx.x; idx < F * pairs; idx += blockDim.x) {
+            const int f = idx / pairs, b = idx - f * pairs;
+            const Fr lo = tab[f * row + 2 * b], hi = tab[f * row + 2 * b + 1];
+            tmp[f * pairs0 + b] = lo + r * (hi - lo);
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < F * pairs; idx += blockDim.x) {
+            const int f = idx / pairs, b = idx - f * pairs;
+            tab[f * row + b] = tmp[f * pairs0 + b];
+        }
+        __syncthreads();
+        pairs >>= 1;
+    }
+    // the state's tables after the last message (folded by every challenge but
+    // the last, which final_evaluations folds in)
+    for (int idx = threadIdx.x; idx < F * 2 * pairs; idx += blockDim.x) {
+        const int f = idx / (2 * pairs), e = idx - f * 2 * pairs;
+        store_fr(dst.p[f] + e, tab[f * row + e]);
+    }
 }
 
 __global__ void k_sumcheck_final_fold(FrPtrList tables, int count, Fr r, Fr *out) {
@@ -1081,6 +1215,118 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_final_evaluations(
     });
 }
 
+namespace hp {
+
+// HP_SUMCHECK_TAIL=0: no resident tail block (every round a launch of its own).
+static bool tail_enabled() {
+    static const bool v = env_size("HP_SUMCHECK_TAIL", 1) != 0;
+    return v;
+}
+
+// Shared memory of the tail block for a first tail round of `pairs` pairs.
+static size_t tail_smem(const SumcheckDesc &d, size_t pairs) {
+    return (size_t(3 * d.factor_count + d.slot_count) * pairs + size_t(d.slot_count)) * sizeof(Fr);
+}
+
+// Pairs of the tail's first round for this state: the largest power of two
+// <= kTailMaxPairs (or HP_SUMCHECK_TAIL_PAIRS) whose tables fit 200 KiB of
+// shared memory; 0 when the shape takes no tail (products of arity > 8, more
+// than kMaxSlotsV2 slots).
+static size_t tail_pairs(const HpCudaSumCheckProverState *s) {
+    static const size_t cap = std::min<size_t>(kTailMaxPairs, env_size("HP_SUMCHECK_TAIL_PAIRS", kTailMaxPairs));
+    const SumcheckDesc &d = s->desc;
+    if (!tail_enabled() || cap == 0 || d.product_count == 0 || d.max_arity > 8 || d.slot_count > kMaxSlotsV2)
+        return 0;
+    size_t p = size_t(1) << ceil_log2_size(cap);
+    if (p > cap) p >>= 1;
+    while (p > 1 && tail_smem(d, p) > size_t(200) * 1024) p >>= 1;
+    return tail_smem(d, p) <= size_t(200) * 1024 ? p : 0;
+}
+
+// Runs rounds k0.. of `s` in the resident tail block, with the Fiat-Shamir
+// step of each round on this thread, writing messages and challenges like
+// the per-round loop of hp_cuda_v1_sumcheck_prove_rounds; r_prev is the
+// previous round's challenge (k0 > 0).
+static void run_tail(HpCudaContext *ctx, HpCudaSumCheckProverState *s, size_t k0, const Fr &r_prev,
+                     HpMerlinTranscript *transcript, uint8_t *out_messages, uint8_t *out_challenges) {
+    const SumcheckDesc &d = s->desc;
+    const size_t nv = s->num_vars, d1 = s->max_degree + 1;
+    const int rounds = int(nv - k0);
+    const size_t pairs0 = table_len(nv - k0 - 1);
+    void *box_dev = nullptr;
+    TailBox *box = reinterpret_cast<TailBox *>(ctx->mailbox(sizeof(TailBox), &box_dev));
+    volatile uint32_t *seq = &box->msg_seq;
+    box->msg_seq = 0;
+    box->ch_seq = 0;
+    box->error = 0;
+    // where the per-round path would leave the tables: one buffer swap per
+    // round after the first of the state
+    HpCudaSumCheckProverState sim = HpCudaSumCheckProverState();
+    sim.round = s->round;
+    sim.current = s->current;
+    for (int j = 0; j < rounds; j++) advance(&sim);
+    FrPtrList src{};
+    FrMutPtrList dst{};
+    for (int f = 0; f < d.factor_count; f++) {
+        src.p[f] = state_table(s, s->current, f);
+        dst.p[f] = const_cast<Fr *>(state_table(s, sim.current, f));
+    }
+    const size_t smem = tail_smem(d, pairs0);
+    auto launch = [&](auto kernel) {
+        check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        kernel<<<1, kTailThreads, smem, ctx->stream>>>(d, src, dst, k0 > 0, r_prev, int(pairs0), rounds,
+                                                       state_weights(s), int(s->max_degree),
+                                                       static_cast<TailBox *>(box_dev));
+    };
+    int tok = ctx->prof_begin("sumcheck_round", ctx->stream);
+    if (d.max_arity <= 2) launch(k_sumcheck_tail<2>);
+    else if (d.max_arity <= 4) launch(k_sumcheck_tail<4>);
+    else if (d.max_arity <= 6) launch(k_sumcheck_tail<6>);
+    else launch(k_sumcheck_tail<8>);
+    check_launch();
+    std::vector<uint8_t> msg(8 + 32 * d1, 0);
+    for (int b = 0; b < 8; b++) msg[b] = uint8_t(uint64_t(d1) >> (8 * b));
+    for (int j = 0; j < rounds; j++) {
+        // the block's message j: poll the mapped sequence number; the block
+        // itself gives up after kTailSpinLimit polls, and a launch that ends
+        // without the message is an error
+        uint64_t polls = 0;
+        const auto t0 = std::chrono::steady_clock::now();
+        while (__atomic_load_n(seq, __ATOMIC_ACQUIRE) < uint32_t(j + 1)) {
+            if ((++polls & 1023) == 0) {
+                if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(60)) fail(HP_CUDA_STATUS_INVALID_STATE);
+                const cudaError_t e = cudaStreamQuery(ctx->stream);
+                if (e != cudaErrorNotReady) {
+                    if (__atomic_load_n(seq, __ATOMIC_ACQUIRE) >= uint32_t(j + 1)) break;
+                    check_cuda(e);
+                    fail(HP_CUDA_STATUS_INVALID_STATE);
+                }
+            }
+        }
+        const uint8_t *m = reinterpret_cast<const uint8_t *>(box->messages + size_t(j) * d1);
+        std::memcpy(msg.data() + 8, m, 32 * d1);
+        std::memcpy(out_messages + 32 * d1 * (k0 + j), m, 32 * d1);
+        merlin_append(transcript, "prover msg", msg.data(), msg.size());
+        uint8_t wide[64], canon[32];
+        merlin_challenge(transcript, "Internal round", wide, 64);
+        const host::Fr64 c = host::from_wide64(wide);
+        host::to_canonical(c, canon);
+        merlin_append(transcript, "Internal round", canon, 32);
+        std::memcpy(out_challenges + 32 * (k0 + j), canon, 32);
+        if (j + 1 < rounds) {
+            std::memcpy(&box->challenges[j], c.v, 32);
+            __atomic_store_n(&box->ch_seq, uint32_t(j + 1), __ATOMIC_RELEASE);
+        }
+    }
+    ctx->sync();
+    ctx->prof_end(tok, ctx->stream);
+    if (__atomic_load_n(&box->error, __ATOMIC_ACQUIRE)) fail(HP_CUDA_STATUS_INVALID_STATE);
+    s->round = sim.round;
+    s->current = sim.current;
+}
+
+}  // namespace hp
+
 extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prove_rounds(HpCudaContext *ctx, HpCudaSumCheckProverState *s,
                                                          HpMerlinTranscript *transcript, size_t rounds,
                                                          uint8_t *out_messages, uint8_t *out_challenges) {
@@ -1097,7 +1343,18 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prove_rounds(HpCudaContext *ctx, HpC
         std::vector<uint8_t> msg(8 + 32 * d1, 0);
         for (int b = 0; b < 8; b++) msg[b] = uint8_t(uint64_t(d1) >> (8 * b));
         Fr r = Fr::zero();
+        const size_t tail = hp::tail_pairs(s);
         for (size_t k = 0; k < rounds; k++) {
+            if (tail > 0 && hp::table_len(rounds - k - 1) <= tail) {
+                // this and every later round in the resident tail block
+                try {
+                    hp::run_tail(ctx, s, k, r, transcript, out_messages, out_challenges);
+                } catch (const hp::Failure &f) {
+                    if (f.kind == HP_CUDA_STATUS_INVALID_STATE) s->poisoned = true;
+                    throw;
+                }
+                break;
+            }
             try {
                 hp::enqueue_round(ctx, s, r, ctx->stream, static_cast<Fr *>(box_dev));
                 ctx->sync();

@@ -147,9 +147,14 @@ def test_execution_failure_poisons_the_round_state(gpu, cpu, oracle):
     assert gpu.final_evaluations(sg, ch) == cpu.final_evaluations(sc, ch)
 
 
-def test_execution_failure_poisons_prove_rounds(gpu, oracle):
+@pytest.mark.parametrize("nth", [2, 3])
+def test_execution_failure_poisons_prove_rounds(gpu, oracle, nth):
+    """nv = 11: rounds 1 and 2 run one launch each (one synchronisation per
+    round), rounds 3..11 (256 pairs and fewer) in the resident tail block (one
+    synchronisation at its end): the failure hits a per-round
+    synchronisation (nth = 2) or the tail's (nth = 3)."""
     from hyperplonk_gb300.transcript import IOPTranscript
-    nv = 8
+    nv = 11
     gm = [gpu.mle_from_evaluations(nv, t) for t in _tables(oracle, nv, 66)]
 
     def transcript():
@@ -157,16 +162,16 @@ def test_execution_failure_poisons_prove_rounds(gpu, oracle):
         t.append_message(b"x", b"y")
         return t.native_merlin()
 
+    expect = gpu.prove_rounds(gpu.prover_init(_degree2(gpu, gm)), transcript(), nv)  # also grows the mailbox
     s = gpu.prover_init(_degree2(gpu, gm))
-    _native.inject_failure(SYNC, 3)  # the third round's synchronisation
+    _native.inject_failure(SYNC, nth)
     with pytest.raises(InvalidState):
         gpu.prove_rounds(s, transcript(), nv)
     _native.inject_failure(NONE, 0)
     with pytest.raises(InvalidState):
         gpu.prove_rounds(s, transcript(), nv)
     fresh = gpu.prover_init(_degree2(gpu, gm))
-    msgs, point = gpu.prove_rounds(fresh, transcript(), nv)
-    assert len(msgs) == nv and len(point) == nv
+    assert gpu.prove_rounds(fresh, transcript(), nv) == expect
 
 
 def test_failed_destructor_aborts(tmp_path):
