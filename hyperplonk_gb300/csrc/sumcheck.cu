@@ -490,27 +490,20 @@ __global__ void __launch_bounds__(kSmallThreads) k_sumcheck_round_small(Sumcheck
     finalize_from_sums(desc, sums, weights, degree, out);
 }
 
-// The last rounds of a sumcheck (at most tail_pairs() pairs) in one launch
-// of one block that stays resident between rounds: the factor tables live in
-// shared memory, each round's message goes to pinned, device-mapped host
-// memory followed by a release of its sequence number, and the block waits
-// (bounded, see kTailSpinLimit) for the host's challenge before folding it
-// in and running the next round.  This removes a launch and a stream
-// synchronisation per round from hp_cuda_v1_sumcheck_prove_rounds, whose
-// host side polls the mapped sequence numbers instead; the messages are the
-// same field elements as the one-launch-per-round path's (same node sums,
-// same weight matrix).
-struct TailBox {
-    uint32_t msg_seq;  // messages ready (device writes)
-    uint32_t ch_seq;   // challenges written (host writes)
-    uint32_t error;    // the block gave up waiting for a challenge
-    uint32_t pad[5];
-    Fr challenges[10];  // Montgomery, one per tail round but the last (host writes)
-    Fr messages[10 * (kMaxDegree + 1)];  // canonical (device writes)
+// Host handshake of the resident rounds (the one-block tail below and the
+// cooperative grid after it), in pinned, device-mapped host memory: hdr[0]
+// counts the messages written (device), hdr[1] the challenges written (host),
+// hdr[2] is set when a block gave up waiting for a challenge; `challenges`
+// holds one Montgomery challenge per resident round but the last (host
+// writes), `messages` (degree + 1) canonical evaluations per round (device
+// writes).  A block waits for challenge j with at most kTailSpinLimit polls.
+struct Handshake {
+    uint32_t *hdr;
+    Fr *challenges;
+    Fr *messages;
 };
-constexpr int kTailThreads = 256;
-constexpr int kTailMaxPairs = 256;  // at most 9 rounds
-constexpr uint32_t kTailSpinLimit = 1u << 24;  // polls of ~128 ns: gives up after about 2-4 s
+constexpr uint32_t kTailSpinLimit = 1u << 22;  // polls of host memory (~1 us each): gives up after seconds
+constexpr uint32_t kRelaySpinLimit = 1u << 24;  // polls of the device relay (>= 256 ns each)
 
 __device__ __forceinline__ uint32_t load_acquire_sys(const uint32_t *p) {
     uint32_t v;
@@ -520,11 +513,54 @@ __device__ __forceinline__ uint32_t load_acquire_sys(const uint32_t *p) {
 __device__ __forceinline__ void store_release_sys(uint32_t *p, uint32_t v) {
     asm volatile("st.release.sys.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+__device__ __forceinline__ uint32_t load_acquire_gpu(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void store_release_gpu(uint32_t *p, uint32_t v) {
+    asm volatile("st.release.gpu.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Thread 0 of a block, after a barrier that follows every thread's writes of
+// message j: one system-scope fence (cumulative over the writes the barrier
+// ordered before it), then the release of the message count.
+__device__ __forceinline__ void release_message(const Handshake &hs, int j) {
+    __threadfence_system();
+    store_release_sys(&hs.hdr[0], uint32_t(j + 1));
+}
+
+// Thread 0 of a block: waits (bounded) until the host has written challenge
+// j and copies it to *out; false when the wait ran out (hdr[2] is then set).
+__device__ __forceinline__ bool wait_host_challenge(const Handshake &hs, int j, Fr *out) {
+    uint32_t it = 0;
+    while (load_acquire_sys(&hs.hdr[1]) < uint32_t(j + 1) && ++it < kTailSpinLimit) __nanosleep(32);
+    if (it >= kTailSpinLimit) {
+        store_release_sys(&hs.hdr[2], 1u);
+        return false;
+    }
+    const volatile uint32_t *c = reinterpret_cast<const volatile uint32_t *>(&hs.challenges[j]);
+#pragma unroll
+    for (int w = 0; w < 8; w++) out->v[w] = c[w];
+    return true;
+}
+
+// The last rounds of a sumcheck (at most tail_pairs() pairs) in one launch
+// of one block that stays resident between rounds: the factor tables live in
+// shared memory, each round's message goes to the handshake followed by a
+// release of its sequence number, and the block waits for the host's
+// challenge before folding it in and running the next round.  This removes
+// a launch and a stream synchronisation per round from
+// hp_cuda_v1_sumcheck_prove_rounds, whose host side polls the mapped
+// sequence numbers instead; the messages are the same field elements as the
+// one-launch-per-round path's (same node sums, same weight matrix).
+constexpr int kTailThreads = 256;
+constexpr int kTailMaxPairs = 256;  // at most 9 rounds
 
 template <int MAXM>
 __global__ void __launch_bounds__(kTailThreads) k_sumcheck_tail(SumcheckDesc desc, FrPtrList src, FrMutPtrList dst,
                                                                 bool fold_first, Fr r0, int pairs0, int rounds,
-                                                                const Fr *weights, int degree, TailBox *box) {
+                                                                const Fr *weights, int degree, Handshake hs) {
     extern __shared__ Fr tsm[];
     __shared__ int abort_round;
     __shared__ Fr challenge;
@@ -582,23 +618,11 @@ __global__ void __launch_bounds__(kTailThreads) k_sumcheck_tail(SumcheckDesc des
             if (lane == 0) sums[sl] = a;
         }
         __syncthreads();
-        finalize_from_sums(desc, sums, weights, degree, box->messages + size_t(j) * (degree + 1));
-        __threadfence_system();
+        finalize_from_sums(desc, sums, weights, degree, hs.messages + size_t(j) * (degree + 1));
         __syncthreads();
-        if (threadIdx.x == 0) store_release_sys(&box->msg_seq, uint32_t(j + 1));
+        if (threadIdx.x == 0) release_message(hs, j);
         if (j + 1 == rounds) break;
-        if (threadIdx.x == 0) {
-            uint32_t it = 0;
-            while (load_acquire_sys(&box->ch_seq) < uint32_t(j + 1) && ++it < kTailSpinLimit) __nanosleep(128);
-            abort_round = it >= kTailSpinLimit;
-            if (abort_round) {
-                store_release_sys(&box->error, 1u);
-            } else {
-                const volatile uint32_t *c = reinterpret_cast<const volatile uint32_t *>(&box->challenges[j]);
-#pragma unroll
-                for (int w = 0; w < 8; w++) challenge.v[w] = c[w];
-            }
-        }
+        if (threadIdx.x == 0) abort_round = !wait_host_challenge(hs, j, &challenge);
         __syncthreads();
         if (abort_round) return;
         const Fr r = challenge;
@@ -623,6 +647,212 @@ __global__ void __launch_bounds__(kTailThreads) k_sumcheck_tail(SumcheckDesc des
     }
 }
 
+// The middle and last rounds of a sumcheck (from resident_pairs() pairs
+// down) in one cooperative launch whose blocks stay resident between rounds.
+// Round j (pairs_j = pairs0 >> j): the first `active` blocks (at least
+// kResMinPairs pairs each; a block past that count returns, since ranges only
+// shrink) each take a contiguous range of pairs and, tile by tile, fold the
+// previous challenge into the factor rows of the range (reading the previous
+// round's tables through L2, since other blocks wrote them; writing the
+// folded rows to the state's next fold buffer and to shared memory), then
+// accumulate their (slot, pair) items from shared memory with one thread
+// group per slot (unreduced 17-limb sums).  Each block adds its slot sums
+// limb by limb into 64-bit counters of the round (double-buffered by round
+// parity, cleared by their reader); the last block to arrive (a counter
+// ticket) reads them, writes the message into the handshake and releases its
+// sequence number (a round of one active block skips the counters).  Block 0 then waits
+// for the host's challenge and relays it through device memory (relay[0]:
+// rounds relayed, relay[1]: abort, relay + 8: the challenge) to the other
+// blocks, which wait for it with a bounded spin as well.  Every round's
+// writes precede its ticket, and the next round starts only after the host
+// has answered that round's message, so a block can read rows that any other
+// block wrote in the previous round.  The fold buffers follow the per-round
+// path's ping-pong (inputs -> fold_a -> fold_b -> fold_a ...), so the state
+// after the launch is the one the per-round calls leave.
+constexpr int kResThreads = 256;
+constexpr size_t kResMinPairs = 32;
+
+// sum_i l[i] 2^(32 i) mod r: block partial sums (Montgomery values < r)
+// accumulated limb by limb in 64-bit counters (at most 2^31 terms), carried
+// into 256 bits plus a top word w (< 2^32), then reduced: the 256-bit part is
+// < 3r (two conditional subtractions), and w 2^256 = to_mont(w) mod r.
+__device__ Fr fr_from_limb_sums(const uint64_t *l) {
+    Fr r;
+    uint64_t c = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const uint64_t t = l[i] + c;
+        r.v[i] = uint32_t(t);
+        c = t >> 32;
+    }
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        uint32_t u[8];
+        u[0] = sub_cc(r.v[0], FrParams::p(0));
+#pragma unroll
+        for (int i = 1; i < 8; i++) u[i] = subc_cc(r.v[i], FrParams::p(i));
+        const uint32_t borrow = subc(0, 0);
+#pragma unroll
+        for (int i = 0; i < 8; i++) r.v[i] = borrow ? r.v[i] : u[i];
+    }
+    Fr w = Fr::zero();
+    w.v[0] = uint32_t(c);
+    return r + to_mont(w);
+}
+
+struct FoldBuffers {
+    FrPtrList inputs;
+    Fr *a, *b;
+    size_t a_stride, b_stride;
+    __device__ __forceinline__ Fr *table(int which, int f) const {
+        return which == 0 ? const_cast<Fr *>(inputs.p[f]) : which == 1 ? a + f * a_stride : b + f * b_stride;
+    }
+};
+
+template <int MAXM>
+__global__ void __launch_bounds__(kResThreads) k_sumcheck_resident(SumcheckDesc desc, FoldBuffers buf, int which0,
+                                                                   bool fold_first, Fr r0, size_t pairs0,
+                                                                   int rounds, int tile, const Fr *weights,
+                                                                   int degree, uint64_t *limb_sums,
+                                                                   unsigned *counter, uint32_t *relay, Handshake hs) {
+    extern __shared__ Fr rsm[];  // tile rows: F x 2 tile; then kResThreads reduced sums
+    __shared__ Fr challenge;
+    __shared__ Fr sums[kMaxSlotsV2];
+    __shared__ int stop;
+    __shared__ bool last;
+    const int F = desc.factor_count, S = desc.slot_count;
+    const int row = 2 * tile;
+    Fr *tab = rsm;
+    Fr *red = rsm + size_t(F) * row;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = kResThreads / 32;
+    // thread group of slot s: tps threads, each over pairs g, g + tps, ...
+    const int tps = kResThreads / S;
+    const int s = int(threadIdx.x) / tps, g = int(threadIdx.x) - s * tps;
+    int begin = 0, m = 1, k = 0;
+    if (s < S) {
+        int p = 0;
+        while (p + 1 < desc.product_count && desc.slot_base[p + 1] <= s) p++;
+        begin = desc.offsets[p];
+        m = desc.offsets[p + 1] - begin;
+        k = s - desc.slot_base[p];
+    }
+    int which = which0;
+    bool fold = fold_first;
+    Fr r = r0;
+    for (int j = 0; j < rounds; j++) {
+        const size_t pairs = pairs0 >> j;
+        const unsigned active = unsigned(min(size_t(gridDim.x), (pairs + kResMinPairs - 1) / kResMinPairs));
+        const size_t b0 = pairs * blockIdx.x / active, b1 = pairs * (blockIdx.x + 1) / active;
+        const int dst = fold ? (which == 1 ? 2 : 1) : which;
+        FrAcc X;
+        acc_zero(X);
+        for (size_t pb = b0; pb < b1; pb += size_t(tile)) {
+            const int np = int(min(size_t(tile), b1 - pb));
+            for (int idx = threadIdx.x; idx < F * 2 * np; idx += kResThreads) {
+                const int f = idx / (2 * np), e = idx - f * 2 * np;
+                const size_t ge = 2 * pb + size_t(e);
+                Fr v;
+                if (fold) {
+                    const Fr *q = buf.table(which, f) + 2 * ge;
+                    const Fr a0 = load_fr_cg(q), a1 = load_fr_cg(q + 1);
+                    v = a0 + r * (a1 - a0);
+                    store_fr(buf.table(dst, f) + ge, v);
+                } else {
+                    v = load_fr(buf.table(which, f) + ge);
+                }
+                tab[f * row + e] = v;
+            }
+            __syncthreads();
+            if (s < S) {
+                for (int b = g; b < np; b += tps) {
+                    Fr v;
+                    auto factor = [&](int q) {
+                        const Fr *t = tab + desc.indices[begin + q] * row + 2 * b;
+                        slot_step(X, v, t[0], t[1], q, m, k);
+                    };
+#pragma unroll
+                    for (int q = 0; q < MAXM; q++)
+                        if (q < m) factor(q);
+                }
+            }
+            __syncthreads();
+        }
+        red[threadIdx.x] = s < S ? acc_reduce(X) : Fr::zero();
+        __syncthreads();
+        for (int sl = warp; sl < S; sl += warps) {
+            Fr a = Fr::zero();
+            for (int i = lane; i < tps; i += 32) a = a + red[sl * tps + i];
+            a = warp_sum(a);
+            if (lane == 0) sums[sl] = a;
+        }
+        __syncthreads();
+        bool finish = active == 1;  // one block: its slot sums are the round's
+        if (!finish) {
+            // add the block's slot sums limb by limb into this round's 64-bit
+            // counters, then the ticket: thread 0 fences once for the block
+            // (cumulative over the additions the barrier ordered before it)
+            uint64_t *acc = limb_sums + size_t(j & 1) * 8 * kMaxSlotsV2;
+            for (int i = threadIdx.x; i < 8 * S; i += kResThreads)
+                atomicAdd(reinterpret_cast<unsigned long long *>(&acc[i]),
+                          (unsigned long long)sums[i >> 3].v[i & 7]);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                __threadfence();
+                last = atomicAdd(counter, 1u) == active - 1;
+            }
+            __syncthreads();
+            if (last) {
+                // read and clear the counters (their next use is two rounds on)
+                uint64_t *lim = reinterpret_cast<uint64_t *>(red);
+                for (int i = threadIdx.x; i < 8 * S; i += kResThreads)
+                    lim[i] = atomicExch(reinterpret_cast<unsigned long long *>(&acc[i]), 0ull);
+                __syncthreads();
+                if (threadIdx.x < S) sums[threadIdx.x] = fr_from_limb_sums(lim + 8 * threadIdx.x);
+                __syncthreads();
+                finish = true;
+            }
+        }
+        if (finish) {
+            finalize_from_sums(desc, sums, weights, degree, hs.messages + size_t(j) * (degree + 1));
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                *counter = 0u;
+                release_message(hs, j);
+            }
+        }
+        if (j + 1 == rounds) break;
+        const size_t next = pairs >> 1;
+        if (blockIdx.x >= unsigned(min(size_t(gridDim.x), (next + kResMinPairs - 1) / kResMinPairs))) return;
+        if (threadIdx.x == 0) {
+            bool ok;
+            if (blockIdx.x == 0) {
+                ok = wait_host_challenge(hs, j, &challenge);
+                if (ok) {
+                    Fr *slot = reinterpret_cast<Fr *>(relay + 8);
+                    store_fr(slot, challenge);
+                    store_release_gpu(&relay[0], uint32_t(j + 1));
+                } else {
+                    store_release_gpu(&relay[1], 1u);
+                }
+            } else {
+                uint32_t it = 0;
+                while (load_acquire_gpu(&relay[0]) < uint32_t(j + 1) && load_acquire_gpu(&relay[1]) == 0u &&
+                       ++it < kRelaySpinLimit)
+                    __nanosleep(256);
+                ok = it < kRelaySpinLimit && load_acquire_gpu(&relay[0]) >= uint32_t(j + 1);
+                if (ok) challenge = load_fr_cg(reinterpret_cast<const Fr *>(relay + 8));
+                else store_release_sys(&hs.hdr[2], 1u);
+            }
+            stop = ok ? 0 : 1;
+        }
+        __syncthreads();
+        if (stop) return;
+        r = challenge;
+        which = dst;
+        fold = true;
+    }
+}
+
 __global__ void k_sumcheck_final_fold(FrPtrList tables, int count, Fr r, Fr *out) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= count) return;
@@ -643,8 +873,9 @@ struct HpCudaSumCheckProverState {
     std::vector<void *> inputs;  // referenced input factor buffers
     void *fold_a = nullptr;      // F x 2^(nv-1) Fr
     void *fold_b = nullptr;      // F x 2^(nv-2) Fr
-    // device: one zeroed Fr slot whose first word is the round kernels'
-    // last-block counter, then the (max_degree + 1) x slot_count extrapolation
+    // device: three zeroed Fr slots -- the round kernels' last-block counter
+    // (first word), the resident grid's relay words and its relayed
+    // challenge -- then the (max_degree + 1) x slot_count extrapolation
     // weights (Montgomery) of finalize_from_sums
     void *weights = nullptr;
     void *partials = nullptr;  // block partials of a round, reused every round
@@ -667,7 +898,7 @@ static unsigned *round_counter(HpCudaSumCheckProverState *s) {
     return reinterpret_cast<unsigned *>(s->weights);
 }
 
-static const Fr *state_weights(HpCudaSumCheckProverState *s) { return static_cast<const Fr *>(s->weights) + 1; }
+static const Fr *state_weights(HpCudaSumCheckProverState *s) { return static_cast<const Fr *>(s->weights) + 3; }
 
 static size_t big_blocks_per_sm();
 
@@ -680,6 +911,8 @@ static size_t partials_capacity(const SumcheckDesc &d, int sm_count) {
     n = std::max(n, sms * 2 * S);
     n = std::max(n, size_t(64) * S);
     n = std::max(n, sms * big_blocks_per_sm() + S);
+    // the resident grid's limb counters: 2 rounds x 8 limbs x kMaxSlotsV2 slots
+    n = std::max(n, size_t(2 * 8 * kMaxSlotsV2) * sizeof(uint64_t) / sizeof(Fr));
     return n * sizeof(Fr);
 }
 
@@ -798,9 +1031,9 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_create(
                 s->inputs.push_back(factors[f]);
             }
             std::vector<hp::host::Fr64> w = hp::extrapolation_weights(d, coefficients, max_degree);
-            s->weights = ctx->scratch((w.size() + 1) * sizeof(Fr));
-            check_cuda(cudaMemsetAsync(s->weights, 0, sizeof(Fr), ctx->stream));
-            check_cuda(cudaMemcpyAsync(static_cast<Fr *>(s->weights) + 1, w.data(), w.size() * sizeof(Fr),
+            s->weights = ctx->scratch((w.size() + 3) * sizeof(Fr));
+            check_cuda(cudaMemsetAsync(s->weights, 0, 3 * sizeof(Fr), ctx->stream));
+            check_cuda(cudaMemcpyAsync(static_cast<Fr *>(s->weights) + 3, w.data(), w.size() * sizeof(Fr),
                                        cudaMemcpyHostToDevice, ctx->stream));
             s->partials_bytes = hp::partials_capacity(d, ctx->sm_count);
             s->partials = ctx->scratch(s->partials_bytes);
@@ -1243,53 +1476,130 @@ static size_t tail_pairs(const HpCudaSumCheckProverState *s) {
     return tail_smem(d, p) <= size_t(200) * 1024 ? p : 0;
 }
 
-// Runs rounds k0.. of `s` in the resident tail block, with the Fiat-Shamir
-// step of each round on this thread, writing messages and challenges like
-// the per-round loop of hp_cuda_v1_sumcheck_prove_rounds; r_prev is the
-// previous round's challenge (k0 > 0).
-static void run_tail(HpCudaContext *ctx, HpCudaSumCheckProverState *s, size_t k0, const Fr &r_prev,
-                     HpMerlinTranscript *transcript, uint8_t *out_messages, uint8_t *out_challenges) {
+// Rows of a resident-grid tile: the largest power of two <= 128 whose F x 2
+// tile rows and the block's reduced sums fit 96 KiB of shared memory.
+static int resident_tile(const SumcheckDesc &d) {
+    int tile = 128;
+    while (tile > 16 && (size_t(d.factor_count) * 2 * tile + kResThreads) * sizeof(Fr) > size_t(96) * 1024)
+        tile >>= 1;
+    return tile;
+}
+
+// First round (in pairs) of the cooperative resident grid for this state
+// (HP_SUMCHECK_RESIDENT_PAIRS overrides the rule below; HP_SUMCHECK_RESIDENT=0:
+// none); 0 when the shape takes none (products of arity > 8, more than
+// kMaxSlotsV2 slots, no products).
+static size_t resident_pairs(const HpCudaSumCheckProverState *s) {
+    static const bool on = env_size("HP_SUMCHECK_RESIDENT", 1) != 0;
+    static const size_t first = env_size("HP_SUMCHECK_RESIDENT_PAIRS", 0);
+    const SumcheckDesc &d = s->desc;
+    if (!on || d.product_count == 0 || d.max_arity > 8 || d.slot_count > kMaxSlotsV2) return 0;
+    if (first > 0) return first;
+    // measured on GB300 (nv = 20): 6 tables in 4 arity-2 products (12 slots)
+    // gain from 2^17 pairs on (0.935 ms per prove against 0.977 from 2^15);
+    // the proof's wider shapes lose from 2^17 (47.09 against 46.85 ms)
+    return d.max_arity <= 2 && d.slot_count <= 12 ? size_t(1) << 17 : size_t(1) << 15;
+}
+
+// The state's relay words for the resident grid (zeroed at prover_init).
+static uint32_t *state_relay(HpCudaSumCheckProverState *s) {
+    return reinterpret_cast<uint32_t *>(static_cast<Fr *>(s->weights) + 1);
+}
+
+// Runs rounds k0.. of `s` in one resident launch -- the cooperative grid
+// (`grid`) or the one-block tail -- with the Fiat-Shamir step of each round
+// on this thread, writing messages and challenges like the per-round loop of
+// hp_cuda_v1_sumcheck_prove_rounds; r_prev is the previous round's
+// challenge (k0 > 0).
+static void run_resident(HpCudaContext *ctx, HpCudaSumCheckProverState *s, size_t k0, const Fr &r_prev,
+                         HpMerlinTranscript *transcript, uint8_t *out_messages, uint8_t *out_challenges,
+                         bool grid) {
     const SumcheckDesc &d = s->desc;
     const size_t nv = s->num_vars, d1 = s->max_degree + 1;
     const int rounds = int(nv - k0);
     const size_t pairs0 = table_len(nv - k0 - 1);
+    // handshake: 32-byte header, the challenges, the messages
+    const size_t box_bytes = 32 + size_t(rounds) * sizeof(Fr) * (1 + d1);
     void *box_dev = nullptr;
-    TailBox *box = reinterpret_cast<TailBox *>(ctx->mailbox(sizeof(TailBox), &box_dev));
-    volatile uint32_t *seq = &box->msg_seq;
-    box->msg_seq = 0;
-    box->ch_seq = 0;
-    box->error = 0;
+    uint8_t *box = ctx->mailbox(box_bytes, &box_dev);
+    uint32_t *hdr = reinterpret_cast<uint32_t *>(box);
+    Fr *challenges = reinterpret_cast<Fr *>(box + 32);
+    const Fr *messages = challenges + rounds;
+    Handshake hs;
+    hs.hdr = static_cast<uint32_t *>(box_dev);
+    hs.challenges = reinterpret_cast<Fr *>(static_cast<uint8_t *>(box_dev) + 32);
+    hs.messages = hs.challenges + rounds;
+    volatile uint32_t *seq = &hdr[0];
+    hdr[0] = hdr[1] = hdr[2] = 0;
     // where the per-round path would leave the tables: one buffer swap per
     // round after the first of the state
     HpCudaSumCheckProverState sim = HpCudaSumCheckProverState();
     sim.round = s->round;
     sim.current = s->current;
     for (int j = 0; j < rounds; j++) advance(&sim);
-    FrPtrList src{};
-    FrMutPtrList dst{};
-    for (int f = 0; f < d.factor_count; f++) {
-        src.p[f] = state_table(s, s->current, f);
-        dst.p[f] = const_cast<Fr *>(state_table(s, sim.current, f));
-    }
-    const size_t smem = tail_smem(d, pairs0);
-    auto launch = [&](auto kernel) {
-        check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-        kernel<<<1, kTailThreads, smem, ctx->stream>>>(d, src, dst, k0 > 0, r_prev, int(pairs0), rounds,
-                                                       state_weights(s), int(s->max_degree),
-                                                       static_cast<TailBox *>(box_dev));
-    };
     int tok = ctx->prof_begin("sumcheck_round", ctx->stream);
-    if (d.max_arity <= 2) launch(k_sumcheck_tail<2>);
-    else if (d.max_arity <= 4) launch(k_sumcheck_tail<4>);
-    else if (d.max_arity <= 6) launch(k_sumcheck_tail<6>);
-    else launch(k_sumcheck_tail<8>);
+    if (grid) {
+        FoldBuffers fb;
+        for (int f = 0; f < d.factor_count; f++) fb.inputs.p[f] = state_table(s, 0, f);
+        fb.a = static_cast<Fr *>(s->fold_a);
+        fb.b = static_cast<Fr *>(s->fold_b);
+        fb.a_stride = nv >= 1 ? table_len(nv - 1) : 1;
+        fb.b_stride = nv >= 2 ? table_len(nv - 2) : 1;
+        int which0 = s->current;
+        bool fold_first = k0 > 0;
+        Fr r0 = r_prev;
+        int tile = resident_tile(d);
+        const Fr *w = state_weights(s);
+        int degree = int(s->max_degree);
+        uint64_t *limb_sums = static_cast<uint64_t *>(s->partials);  // 2 x 8 x kMaxSlotsV2 counters
+        check_cuda(cudaMemsetAsync(limb_sums, 0, 2 * 8 * kMaxSlotsV2 * sizeof(uint64_t), ctx->stream));
+        unsigned *counter = round_counter(s);
+        uint32_t *relay = state_relay(s);
+        size_t p0 = pairs0;
+        int nrounds = rounds;
+        const size_t smem = (size_t(d.factor_count) * 2 * tile + kResThreads) * sizeof(Fr);
+        const size_t sms = size_t(ctx->sm_count > 0 ? ctx->sm_count : 152);
+        auto launch = [&](auto kernel) {
+            check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+            int per_sm = 0;
+            check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kResThreads, smem));
+            if (per_sm < 1) fail(HP_CUDA_STATUS_NOT_IMPLEMENTED);
+            size_t blocks = sms * size_t(std::min(per_sm, 2));
+            blocks = std::max<size_t>(1, std::min(blocks, (pairs0 + kResMinPairs - 1) / kResMinPairs));
+            void *args[] = {const_cast<SumcheckDesc *>(&d), &fb, &which0, &fold_first, &r0, &p0, &nrounds,
+                            &tile, &w, &degree, &limb_sums, &counter, &relay, &hs};
+            check_cuda(cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(kernel), dim3(unsigned(blocks)),
+                                                   dim3(kResThreads), args, smem, ctx->stream));
+        };
+        if (d.max_arity <= 2) launch(k_sumcheck_resident<2>);
+        else if (d.max_arity <= 4) launch(k_sumcheck_resident<4>);
+        else if (d.max_arity <= 6) launch(k_sumcheck_resident<6>);
+        else launch(k_sumcheck_resident<8>);
+    } else {
+        FrPtrList src{};
+        FrMutPtrList dst{};
+        for (int f = 0; f < d.factor_count; f++) {
+            src.p[f] = state_table(s, s->current, f);
+            dst.p[f] = const_cast<Fr *>(state_table(s, sim.current, f));
+        }
+        const size_t smem = tail_smem(d, pairs0);
+        auto launch = [&](auto kernel) {
+            check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+            kernel<<<1, kTailThreads, smem, ctx->stream>>>(d, src, dst, k0 > 0, r_prev, int(pairs0), rounds,
+                                                           state_weights(s), int(s->max_degree), hs);
+        };
+        if (d.max_arity <= 2) launch(k_sumcheck_tail<2>);
+        else if (d.max_arity <= 4) launch(k_sumcheck_tail<4>);
+        else if (d.max_arity <= 6) launch(k_sumcheck_tail<6>);
+        else launch(k_sumcheck_tail<8>);
+    }
     check_launch();
     std::vector<uint8_t> msg(8 + 32 * d1, 0);
     for (int b = 0; b < 8; b++) msg[b] = uint8_t(uint64_t(d1) >> (8 * b));
     for (int j = 0; j < rounds; j++) {
-        // the block's message j: poll the mapped sequence number; the block
-        // itself gives up after kTailSpinLimit polls, and a launch that ends
-        // without the message is an error
+        // the launch's message j: poll the mapped sequence number; the blocks
+        // themselves give up after kTailSpinLimit polls, and a launch that
+        // ends without the message is an error
         uint64_t polls = 0;
         const auto t0 = std::chrono::steady_clock::now();
         while (__atomic_load_n(seq, __ATOMIC_ACQUIRE) < uint32_t(j + 1)) {
@@ -1303,7 +1613,7 @@ static void run_tail(HpCudaContext *ctx, HpCudaSumCheckProverState *s, size_t k0
                 }
             }
         }
-        const uint8_t *m = reinterpret_cast<const uint8_t *>(box->messages + size_t(j) * d1);
+        const uint8_t *m = reinterpret_cast<const uint8_t *>(messages + size_t(j) * d1);
         std::memcpy(msg.data() + 8, m, 32 * d1);
         std::memcpy(out_messages + 32 * d1 * (k0 + j), m, 32 * d1);
         merlin_append(transcript, "prover msg", msg.data(), msg.size());
@@ -1314,13 +1624,13 @@ static void run_tail(HpCudaContext *ctx, HpCudaSumCheckProverState *s, size_t k0
         merlin_append(transcript, "Internal round", canon, 32);
         std::memcpy(out_challenges + 32 * (k0 + j), canon, 32);
         if (j + 1 < rounds) {
-            std::memcpy(&box->challenges[j], c.v, 32);
-            __atomic_store_n(&box->ch_seq, uint32_t(j + 1), __ATOMIC_RELEASE);
+            std::memcpy(&challenges[j], c.v, 32);
+            __atomic_store_n(&hdr[1], uint32_t(j + 1), __ATOMIC_RELEASE);
         }
     }
     ctx->sync();
     ctx->prof_end(tok, ctx->stream);
-    if (__atomic_load_n(&box->error, __ATOMIC_ACQUIRE)) fail(HP_CUDA_STATUS_INVALID_STATE);
+    if (__atomic_load_n(&hdr[2], __ATOMIC_ACQUIRE)) fail(HP_CUDA_STATUS_INVALID_STATE);
     s->round = sim.round;
     s->current = sim.current;
 }
@@ -1343,12 +1653,14 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prove_rounds(HpCudaContext *ctx, HpC
         std::vector<uint8_t> msg(8 + 32 * d1, 0);
         for (int b = 0; b < 8; b++) msg[b] = uint8_t(uint64_t(d1) >> (8 * b));
         Fr r = Fr::zero();
-        const size_t tail = hp::tail_pairs(s);
+        const size_t resident = hp::resident_pairs(s);
+        const size_t tail = resident ? 0 : hp::tail_pairs(s);
         for (size_t k = 0; k < rounds; k++) {
-            if (tail > 0 && hp::table_len(rounds - k - 1) <= tail) {
-                // this and every later round in the resident tail block
+            const size_t pairs = hp::table_len(rounds - k - 1);
+            if ((resident > 0 && pairs <= resident) || (tail > 0 && pairs <= tail)) {
+                // this and every later round in one resident launch
                 try {
-                    hp::run_tail(ctx, s, k, r, transcript, out_messages, out_challenges);
+                    hp::run_resident(ctx, s, k, r, transcript, out_messages, out_challenges, resident > 0);
                 } catch (const hp::Failure &f) {
                     if (f.kind == HP_CUDA_STATUS_INVALID_STATE) s->poisoned = true;
                     throw;

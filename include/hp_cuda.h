@@ -329,10 +329,10 @@ HpCudaStatus hp_host_v1_keccak_f1600(uint8_t *state200);
  * (rounds * (max_degree+1) * 32 bytes) and the challenges (rounds * 32).
  * Afterwards the state is where the last per-round call would leave it
  * (final_evaluations takes the last challenge).  InvalidState unless the
- * state is at round 0; an execution failure poisons the state.  The last
- * rounds (from the first of <= 256 pairs) run in one resident block that
- * exchanges messages and challenges with this call through the context's
- * mapped mailbox.  No counterpart in the reference (its caller drives the
+ * state is at round 0; an execution failure poisons the state.  The middle
+ * and last rounds (from the first of <= 2^15 or 2^17 pairs, by shape) run in
+ * one resident cooperative launch that exchanges messages and challenges
+ * with this call through the context's mapped mailbox.  No counterpart in the reference (its caller drives the
  * rounds one at a time through the transcript). */
 HpCudaStatus hp_cuda_v1_sumcheck_prove_rounds(HpCudaContext *ctx, HpCudaSumCheckProverState *state,
                                               HpMerlinTranscript *transcript, size_t rounds,

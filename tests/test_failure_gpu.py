@@ -149,12 +149,13 @@ def test_execution_failure_poisons_the_round_state(gpu, cpu, oracle):
 
 @pytest.mark.parametrize("nth", [2, 3])
 def test_execution_failure_poisons_prove_rounds(gpu, oracle, nth):
-    """nv = 11: rounds 1 and 2 run one launch each (one synchronisation per
-    round), rounds 3..11 (256 pairs and fewer) in the resident tail block (one
-    synchronisation at its end): the failure hits a per-round
-    synchronisation (nth = 2) or the tail's (nth = 3)."""
+    """nv = 20, a degree-2 shape with 5 slots: rounds 1 and 2 (2^19, 2^18
+    pairs) run one launch each (one synchronisation per round), rounds 3..20
+    (2^17 pairs and fewer) in one resident launch (one synchronisation at its
+    end): the failure hits a per-round synchronisation (nth = 2) or the
+    resident launch's (nth = 3)."""
     from hyperplonk_gb300.transcript import IOPTranscript
-    nv = 11
+    nv = 20
     gm = [gpu.mle_from_evaluations(nv, t) for t in _tables(oracle, nv, 66)]
 
     def transcript():
