@@ -73,7 +73,7 @@ __device__ __forceinline__ Fr warp_sum(Fr v) {
 }
 
 __device__ void finalize_from_sums(const SumcheckDesc &desc, const Fr *sums, const Fr *weights, int degree,
-                                   Fr *out);
+                                   Fr *out, const Fr *claim);
 
 __device__ __forceinline__ Fr load_fr_cg(const Fr *p) {  // L2 load: written by other blocks of this launch
     const uint4 *q = reinterpret_cast<const uint4 *>(p);
@@ -89,7 +89,7 @@ __device__ __forceinline__ Fr load_fr_cg(const Fr *p) {  // L2 load: written by 
 // them and writes the round message -- no separate finalize launch.
 __device__ __forceinline__ void finish_round_in_last_block(const SumcheckDesc &desc, const Fr *partials,
                                                            int per_slot, unsigned *counter, const Fr *weights,
-                                                           int degree, Fr *out, Fr *sums) {
+                                                           int degree, Fr *out, Fr *sums, const Fr *claim) {
     __shared__ bool last;
     __threadfence();
     __syncthreads();
@@ -105,7 +105,7 @@ __device__ __forceinline__ void finish_round_in_last_block(const SumcheckDesc &d
         if (lane == 0) sums[s] = a;
     }
     __syncthreads();
-    finalize_from_sums(desc, sums, weights, degree, out);
+    finalize_from_sums(desc, sums, weights, degree, out, claim);
     if (threadIdx.x == 0) *counter = 0u;
 }
 
@@ -114,7 +114,8 @@ __global__ void __launch_bounds__(kRoundThreads) k_sumcheck_round_regs(SumcheckD
                                                                        FrMutPtrList dst, FrPtrList rd, bool fold,
                                                                        Fr r, size_t pairs, Fr *partials,
                                                                        unsigned *counter, const Fr *weights,
-                                                                       int degree, Fr *out) {
+                                                                       int degree, Fr *out, Fr claim,
+                                                                       bool use_claim) {
     // acc[s * kRoundThreads + t]: thread t's running sum of slot s over its pairs
     extern __shared__ Fr acc[];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -132,6 +133,7 @@ __global__ void __launch_bounds__(kRoundThreads) k_sumcheck_round_regs(SumcheckD
         }
         for (int p = 0; p < desc.product_count; p++) {
             const int begin = desc.offsets[p], m = desc.offsets[p + 1] - begin, slot = desc.slot_base[p];
+            const int n0 = desc.node0[p];
             Fr e[MAXM], st[MAXM];
 #pragma unroll
             for (int j = 0; j < MAXM; j++) {
@@ -147,11 +149,12 @@ __global__ void __launch_bounds__(kRoundThreads) k_sumcheck_round_regs(SumcheckD
                     for (int j = 0; j < MAXM; j++)
                         if (j < m) e[j] = e[j] + st[j];
                 }
+                if (k < n0) continue;
                 Fr v = e[0];
 #pragma unroll
                 for (int j = 1; j < MAXM; j++)
                     if (j < m) v = v * e[j];
-                Fr &a = acc[(slot + k) * kRoundThreads + t];
+                Fr &a = acc[(slot + k - n0) * kRoundThreads + t];
                 a = a + v;
             }
         }
@@ -166,7 +169,8 @@ __global__ void __launch_bounds__(kRoundThreads) k_sumcheck_round_regs(SumcheckD
         if (lane == 0) partials[size_t(s) * gridDim.x + blockIdx.x] = v;  // slot-major
     }
     __syncthreads();  // acc is reused below as the last block's slot sums
-    finish_round_in_last_block(desc, partials, int(gridDim.x), counter, weights, degree, out, acc);
+    finish_round_in_last_block(desc, partials, int(gridDim.x), counter, weights, degree, out, acc,
+                               use_claim ? &claim : nullptr);
 }
 
 // dst_f[i] = src_f[2i] + r (src_f[2i+1] - src_f[2i]) for the `count` factor
@@ -231,14 +235,15 @@ __device__ __forceinline__ void slot_step(FrAcc &X, Fr &v, const Fr &lo, const F
 template <int MAXM>
 __global__ void HP_WIDE_BOUNDS k_sumcheck_round_wide(SumcheckDesc desc, FrPtrList src, FrMutPtrList dst, bool fold,
                                                      Fr r, size_t pairs, int blocks_per_slot, Fr *partials,
-                                                     unsigned *counter, const Fr *weights, int degree, Fr *out) {
+                                                     unsigned *counter, const Fr *weights, int degree, Fr *out,
+                                                     Fr claim, bool use_claim) {
     extern __shared__ Fr sums[];  // S slot sums, used by the last block
     __shared__ Fr wsum[kWideThreads / 32];
     const int S = desc.slot_count;
     const int s = int(blockIdx.x % unsigned(S)), blk = int(blockIdx.x / unsigned(S));
     int p = 0;
     while (p + 1 < desc.product_count && desc.slot_base[p + 1] <= s) p++;
-    const int begin = desc.offsets[p], m = desc.offsets[p + 1] - begin, k = s - desc.slot_base[p];
+    const int begin = desc.offsets[p], m = desc.offsets[p + 1] - begin, k = s - desc.slot_base[p] + desc.node0[p];
     FrAcc X;
     acc_zero(X);
     const size_t stride = size_t(blocks_per_slot) * kWideThreads;
@@ -252,7 +257,7 @@ __global__ void HP_WIDE_BOUNDS k_sumcheck_round_wide(SumcheckDesc desc, FrPtrLis
                 const Fr a0 = load_fr(q), a1 = load_fr(q + 1), a2 = load_fr(q + 2), a3 = load_fr(q + 3);
                 lo = a0 + r * (a1 - a0);
                 hi = a2 + r * (a3 - a2);
-                if (k == 0 && desc.writer[f] == begin + j) {
+                if (k == desc.node0[p] && desc.writer[f] == begin + j) {  // the product's first slot
                     Fr *d = dst.p[f] + 2 * b;
                     store_fr(d, lo);
                     store_fr(d + 1, hi);
@@ -283,7 +288,8 @@ __global__ void HP_WIDE_BOUNDS k_sumcheck_round_wide(SumcheckDesc desc, FrPtrLis
         for (int w = 1; w < kWideThreads / 32; w++) t = t + wsum[w];
         partials[size_t(s) * blocks_per_slot + blk] = t;
     }
-    finish_round_in_last_block(desc, partials, blocks_per_slot, counter, weights, degree, out, sums);
+    finish_round_in_last_block(desc, partials, blocks_per_slot, counter, weights, degree, out, sums,
+                               use_claim ? &claim : nullptr);
 }
 
 // One thread per (product, pair) item, for the large rounds (more than
@@ -314,18 +320,24 @@ constexpr int kPpBlocksPerSm = HP_ROUND_BLOCKS_PER_SM;
 #define HP_PP_BOUNDS __launch_bounds__(kPpThreads)
 #endif
 
-template <int MAXM>
+// kNode0: the first node of every product (SumcheckDesc::node0, the same for
+// all products of the launch's layout: 0 in the first round, 1 in later
+// rounds when every product's arity is the degree), a compile-time constant
+// so that the node loop keeps its fixed shape (a per-product run-time node
+// measured 100 us against 82 us for the full 12-slot form at 2^18 pairs).
+template <int MAXM, int kNode0>
 __global__ void HP_PP_BOUNDS k_sumcheck_round_pp(SumcheckDesc desc, FrPtrList src, FrMutPtrList dst,
                                                                   bool fold, Fr r, size_t pairs,
                                                                   int blocks_per_product, Fr *partials,
                                                                   unsigned *counter, const Fr *weights, int degree,
-                                                                  Fr *out) {
+                                                                  Fr *out, Fr claim, bool use_claim) {
     constexpr bool kUnreduced = MAXM <= 2;
     extern __shared__ Fr sums[];  // S slot sums, used by the last block
     __shared__ Fr wsum[kPpThreads / 32][MAXM + 1];
     const int P = desc.product_count;
     const int p = int(blockIdx.x % unsigned(P)), blk = int(blockIdx.x / unsigned(P));
     const int begin = desc.offsets[p], m = desc.offsets[p + 1] - begin, slot0 = desc.slot_base[p];
+    constexpr int n0 = kNode0;  // slot slot0 holds node n0
     FrAcc X[kUnreduced ? MAXM + 1 : 1];
     Fr A[kUnreduced ? 1 : MAXM + 1];
 #pragma unroll
@@ -368,6 +380,7 @@ __global__ void HP_PP_BOUNDS k_sumcheck_round_pp(SumcheckDesc desc, FrPtrList sr
                     for (int j = 0; j < MAXM; j++)
                         if (j < m) e[j] = e[j] + st[j];  // factor j at node t
                 }
+                if (t < n0) continue;
                 Fr v;
 #pragma unroll
                 for (int j = 0; j < MAXM; j++) {
@@ -388,7 +401,7 @@ __global__ void HP_PP_BOUNDS k_sumcheck_round_pp(SumcheckDesc desc, FrPtrList sr
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int t = 0; t <= MAXM; t++) {
-        if (t <= m) {
+        if (t <= m && t >= n0) {
             Fr a;
             if constexpr (kUnreduced) a = acc_reduce(X[t]);
             else a = A[t];
@@ -397,14 +410,15 @@ __global__ void HP_PP_BOUNDS k_sumcheck_round_pp(SumcheckDesc desc, FrPtrList sr
         }
     }
     __syncthreads();
-    if (threadIdx.x <= m) {
+    if (int(threadIdx.x) <= m && int(threadIdx.x) >= n0) {
         const int t = threadIdx.x;
         Fr a = wsum[0][t];
 #pragma unroll
         for (int w = 1; w < kPpThreads / 32; w++) a = a + wsum[w][t];
-        partials[size_t(slot0 + t) * blocks_per_product + blk] = a;
+        partials[size_t(slot0 + t - n0) * blocks_per_product + blk] = a;
     }
-    finish_round_in_last_block(desc, partials, blocks_per_product, counter, weights, degree, out, sums);
+    finish_round_in_last_block(desc, partials, blocks_per_product, counter, weights, degree, out, sums,
+                               use_claim ? &claim : nullptr);
 }
 
 // Given the slot sums (Montgomery, shared memory) of a round, writes the d+1
@@ -417,14 +431,15 @@ __global__ void HP_PP_BOUNDS k_sumcheck_round_pp(SumcheckDesc desc, FrPtrList sr
 // reference's barycentric extrapolation (backend/src/cpu/sum_check.rs:183-217)
 // beyond -- scaled and summed over products.
 __device__ void finalize_from_sums(const SumcheckDesc &desc, const Fr *sums, const Fr *weights, int degree,
-                                   Fr *out) {
+                                   Fr *out, const Fr *claim) {
     const int S = desc.slot_count;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
     for (int x = warp; x <= degree; x += warps) {
         Fr a = Fr::zero();
         for (int s = lane; s < S; s += 32) a = a + weights[size_t(x) * S + s] * sums[s];
         a = warp_sum(a);
-        if (lane == 0) out[x] = from_mont(a);
+        // with a claim, row 0 of W is minus row 1: p(0) = claim - p(1)
+        if (lane == 0) out[x] = from_mont(x == 0 && claim != nullptr ? a + *claim : a);
     }
 }
 
@@ -438,7 +453,8 @@ template <int MAXM>
 __global__ void __launch_bounds__(kSmallThreads) k_sumcheck_round_small(SumcheckDesc desc, FrPtrList src,
                                                                         FrMutPtrList dst, FrPtrList rd, bool fold,
                                                                         Fr r, int pairs, const Fr *weights,
-                                                                        int degree, Fr *out) {
+                                                                        int degree, Fr *out, Fr claim,
+                                                                        bool use_claim) {
     extern __shared__ Fr sm[];  // vals[S][kSmallPairs], then sums[S]
     const int S = desc.slot_count, F = desc.factor_count;
     Fr *vals = sm, *sums = sm + size_t(S) * kSmallPairs;
@@ -456,6 +472,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_sumcheck_round_small(Sumcheck
     for (int idx = threadIdx.x; idx < desc.product_count * pairs; idx += blockDim.x) {
         const int p = idx / pairs, b = idx % pairs;
         const int begin = desc.offsets[p], m = desc.offsets[p + 1] - begin, slot = desc.slot_base[p];
+        const int n0 = desc.node0[p];
         Fr e[MAXM], st[MAXM];
 #pragma unroll
         for (int j = 0; j < MAXM; j++) {
@@ -471,11 +488,12 @@ __global__ void __launch_bounds__(kSmallThreads) k_sumcheck_round_small(Sumcheck
                 for (int j = 0; j < MAXM; j++)
                     if (j < m) e[j] = e[j] + st[j];
             }
+            if (k < n0) continue;
             Fr v = e[0];
 #pragma unroll
             for (int j = 1; j < MAXM; j++)
                 if (j < m) v = v * e[j];
-            vals[(slot + k) * kSmallPairs + b] = v;
+            vals[(slot + k - n0) * kSmallPairs + b] = v;
         }
     }
     __syncthreads();
@@ -487,7 +505,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_sumcheck_round_small(Sumcheck
         if (lane == 0) sums[s] = v;
     }
     __syncthreads();
-    finalize_from_sums(desc, sums, weights, degree, out);
+    finalize_from_sums(desc, sums, weights, degree, out, use_claim ? &claim : nullptr);
 }
 
 // Host handshake of the resident rounds (the one-block tail below and the
@@ -496,10 +514,14 @@ __global__ void __launch_bounds__(kSmallThreads) k_sumcheck_round_small(Sumcheck
 // hdr[2] is set when a block gave up waiting for a challenge; `challenges`
 // holds one Montgomery challenge per resident round but the last (host
 // writes), `messages` (degree + 1) canonical evaluations per round (device
-// writes).  A block waits for challenge j with at most kTailSpinLimit polls.
+// writes), `claims` the claim p_prev(r_prev) of every resident round after
+// the first (Montgomery, written with the previous round's challenge), and
+// `messages` (degree + 1) canonical evaluations per round (device writes).
+// A block waits for challenge j with at most kTailSpinLimit polls.
 struct Handshake {
     uint32_t *hdr;
     Fr *challenges;
+    Fr *claims;
     Fr *messages;
 };
 constexpr uint32_t kTailSpinLimit = 1u << 22;  // polls of host memory (~1 us each): gives up after seconds
@@ -531,8 +553,9 @@ __device__ __forceinline__ void release_message(const Handshake &hs, int j) {
 }
 
 // Thread 0 of a block: waits (bounded) until the host has written challenge
-// j and copies it to *out; false when the wait ran out (hdr[2] is then set).
-__device__ __forceinline__ bool wait_host_challenge(const Handshake &hs, int j, Fr *out) {
+// j, copies it to *out and the claim of round j + 1 to *claim; false when the
+// wait ran out (hdr[2] is then set).
+__device__ __forceinline__ bool wait_host_challenge(const Handshake &hs, int j, Fr *out, Fr *claim) {
     uint32_t it = 0;
     while (load_acquire_sys(&hs.hdr[1]) < uint32_t(j + 1) && ++it < kTailSpinLimit) __nanosleep(32);
     if (it >= kTailSpinLimit) {
@@ -540,8 +563,12 @@ __device__ __forceinline__ bool wait_host_challenge(const Handshake &hs, int j, 
         return false;
     }
     const volatile uint32_t *c = reinterpret_cast<const volatile uint32_t *>(&hs.challenges[j]);
+    const volatile uint32_t *q = reinterpret_cast<const volatile uint32_t *>(&hs.claims[j + 1]);
 #pragma unroll
-    for (int w = 0; w < 8; w++) out->v[w] = c[w];
+    for (int w = 0; w < 8; w++) {
+        out->v[w] = c[w];
+        claim->v[w] = q[w];
+    }
     return true;
 }
 
@@ -560,10 +587,11 @@ constexpr int kTailMaxPairs = 256;  // at most 9 rounds
 template <int MAXM>
 __global__ void __launch_bounds__(kTailThreads) k_sumcheck_tail(SumcheckDesc desc, FrPtrList src, FrMutPtrList dst,
                                                                 bool fold_first, Fr r0, int pairs0, int rounds,
-                                                                const Fr *weights, int degree, Handshake hs) {
+                                                                const Fr *weights, int degree, Fr claim0,
+                                                                Handshake hs) {
     extern __shared__ Fr tsm[];
     __shared__ int abort_round;
-    __shared__ Fr challenge;
+    __shared__ Fr challenge, claim;
     const int F = desc.factor_count, S = desc.slot_count, P = desc.product_count;
     const int row = 2 * pairs0;                     // table row stride
     Fr *tab = tsm;                                  // F x 2 pairs0
@@ -582,12 +610,14 @@ __global__ void __launch_bounds__(kTailThreads) k_sumcheck_tail(SumcheckDesc des
         }
         tab[f * row + e] = v;
     }
+    if (threadIdx.x == 0) claim = claim0;
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
     for (int j = 0; j < rounds; j++) {
         for (int idx = threadIdx.x; idx < P * pairs; idx += blockDim.x) {
             const int p = idx / pairs, b = idx - p * pairs;
             const int begin = desc.offsets[p], m = desc.offsets[p + 1] - begin, slot = desc.slot_base[p];
+            const int n0 = desc.node0[p];
             Fr e[MAXM], st[MAXM];
 #pragma unroll
             for (int q = 0; q < MAXM; q++) {
@@ -603,11 +633,12 @@ __global__ void __launch_bounds__(kTailThreads) k_sumcheck_tail(SumcheckDesc des
                     for (int q = 0; q < MAXM; q++)
                         if (q < m) e[q] = e[q] + st[q];
                 }
+                if (k < n0) continue;
                 Fr v = e[0];
 #pragma unroll
                 for (int q = 1; q < MAXM; q++)
                     if (q < m) v = v * e[q];
-                vals[(slot + k) * pairs0 + b] = v;
+                vals[(slot + k - n0) * pairs0 + b] = v;
             }
         }
         __syncthreads();
@@ -618,11 +649,11 @@ __global__ void __launch_bounds__(kTailThreads) k_sumcheck_tail(SumcheckDesc des
             if (lane == 0) sums[sl] = a;
         }
         __syncthreads();
-        finalize_from_sums(desc, sums, weights, degree, hs.messages + size_t(j) * (degree + 1));
+        finalize_from_sums(desc, sums, weights, degree, hs.messages + size_t(j) * (degree + 1), &claim);
         __syncthreads();
         if (threadIdx.x == 0) release_message(hs, j);
         if (j + 1 == rounds) break;
-        if (threadIdx.x == 0) abort_round = !wait_host_challenge(hs, j, &challenge);
+        if (threadIdx.x == 0) abort_round = !wait_host_challenge(hs, j, &challenge, &claim);
         __syncthreads();
         if (abort_round) return;
         const Fr r = challenge;
@@ -662,7 +693,8 @@ __global__ void __launch_bounds__(kTailThreads) k_sumcheck_tail(SumcheckDesc des
 // ticket) reads them, writes the message into the handshake and releases its
 // sequence number (a round of one active block skips the counters).  Block 0 then waits
 // for the host's challenge and relays it through device memory (relay[0]:
-// rounds relayed, relay[1]: abort, relay + 8: the challenge) to the other
+// rounds relayed, relay[1]: abort, relay + 8: the challenge, relay + 16: the
+// next round's claim) to the other
 // blocks, which wait for it with a bounded spin as well.  Every round's
 // writes precede its ticket, and the next round starts only after the host
 // has answered that round's message, so a block can read rows that any other
@@ -713,10 +745,10 @@ template <int MAXM>
 __global__ void __launch_bounds__(kResThreads) k_sumcheck_resident(SumcheckDesc desc, FoldBuffers buf, int which0,
                                                                    bool fold_first, Fr r0, size_t pairs0,
                                                                    int rounds, int tile, const Fr *weights,
-                                                                   int degree, uint64_t *limb_sums,
+                                                                   int degree, Fr claim0, uint64_t *limb_sums,
                                                                    unsigned *counter, uint32_t *relay, Handshake hs) {
     extern __shared__ Fr rsm[];  // tile rows: F x 2 tile; then kResThreads reduced sums
-    __shared__ Fr challenge;
+    __shared__ Fr challenge, claim;
     __shared__ Fr sums[kMaxSlotsV2];
     __shared__ int stop;
     __shared__ bool last;
@@ -734,8 +766,9 @@ __global__ void __launch_bounds__(kResThreads) k_sumcheck_resident(SumcheckDesc 
         while (p + 1 < desc.product_count && desc.slot_base[p + 1] <= s) p++;
         begin = desc.offsets[p];
         m = desc.offsets[p + 1] - begin;
-        k = s - desc.slot_base[p];
+        k = s - desc.slot_base[p] + desc.node0[p];
     }
+    if (threadIdx.x == 0) claim = claim0;
     int which = which0;
     bool fold = fold_first;
     Fr r = r0;
@@ -813,7 +846,7 @@ __global__ void __launch_bounds__(kResThreads) k_sumcheck_resident(SumcheckDesc 
             }
         }
         if (finish) {
-            finalize_from_sums(desc, sums, weights, degree, hs.messages + size_t(j) * (degree + 1));
+            finalize_from_sums(desc, sums, weights, degree, hs.messages + size_t(j) * (degree + 1), &claim);
             __syncthreads();
             if (threadIdx.x == 0) {
                 *counter = 0u;
@@ -826,10 +859,10 @@ __global__ void __launch_bounds__(kResThreads) k_sumcheck_resident(SumcheckDesc 
         if (threadIdx.x == 0) {
             bool ok;
             if (blockIdx.x == 0) {
-                ok = wait_host_challenge(hs, j, &challenge);
+                ok = wait_host_challenge(hs, j, &challenge, &claim);
                 if (ok) {
-                    Fr *slot = reinterpret_cast<Fr *>(relay + 8);
-                    store_fr(slot, challenge);
+                    store_fr(reinterpret_cast<Fr *>(relay + 8), challenge);
+                    store_fr(reinterpret_cast<Fr *>(relay + 16), claim);
                     store_release_gpu(&relay[0], uint32_t(j + 1));
                 } else {
                     store_release_gpu(&relay[1], 1u);
@@ -840,7 +873,10 @@ __global__ void __launch_bounds__(kResThreads) k_sumcheck_resident(SumcheckDesc 
                        ++it < kRelaySpinLimit)
                     __nanosleep(256);
                 ok = it < kRelaySpinLimit && load_acquire_gpu(&relay[0]) >= uint32_t(j + 1);
-                if (ok) challenge = load_fr_cg(reinterpret_cast<const Fr *>(relay + 8));
+                if (ok) {
+                    challenge = load_fr_cg(reinterpret_cast<const Fr *>(relay + 8));
+                    claim = load_fr_cg(reinterpret_cast<const Fr *>(relay + 16));
+                }
                 else store_release_sys(&hs.hdr[2], 1u);
             }
             stop = ok ? 0 : 1;
@@ -881,6 +917,18 @@ struct HpCudaSumCheckProverState {
     void *partials = nullptr;  // block partials of a round, reused every round
     size_t partials_bytes = 0;
     int current = 0;             // 0: inputs, 1: fold_a, 2: fold_b
+    // Rounds after the first: products of arity = degree without their t = 0
+    // slot (SumcheckDesc::node0), with their own weight matrix after the
+    // first one in `weights` (row 0 = minus row 1, the claim added to it).
+    hp::SumcheckDesc desc_red{};
+    bool red_uniform = false;  // every product of desc_red starts at node 1
+    size_t weights_full = 0;   // Fr entries of the first round's matrix
+    // 1 / prod_{y != x} (x - y) for x = 0..max_degree: Lagrange weights of a
+    // round message over the nodes 0..max_degree
+    std::vector<hp::host::Fr64> lag_den;
+    // the latest round message (Montgomery) and the round that produced it
+    std::vector<hp::host::Fr64> last_msg;
+    size_t last_round = SIZE_MAX;
 };
 
 namespace hp {
@@ -898,7 +946,44 @@ static unsigned *round_counter(HpCudaSumCheckProverState *s) {
     return reinterpret_cast<unsigned *>(s->weights);
 }
 
-static const Fr *state_weights(HpCudaSumCheckProverState *s) { return static_cast<const Fr *>(s->weights) + 3; }
+static const Fr *state_weights(HpCudaSumCheckProverState *s) { return static_cast<const Fr *>(s->weights) + 4; }
+static const Fr *state_weights_red(HpCudaSumCheckProverState *s) {
+    return static_cast<const Fr *>(s->weights) + 4 + s->weights_full;
+}
+
+// Stores round `round`'s message (canonical bytes) for the next round's claim.
+static void record_message(HpCudaSumCheckProverState *s, size_t round, const uint8_t *bytes) {
+    s->last_msg.resize(s->max_degree + 1);
+    for (size_t x = 0; x <= s->max_degree; x++)
+        if (!host::from_canonical(bytes + 32 * x, s->last_msg[x])) fail(HP_CUDA_STATUS_INVALID_STATE);
+    s->last_round = round;
+}
+
+// The claim of the state's current round: the previous message's polynomial
+// at the previous challenge r, sum_x L_x(r) m[x] with the Lagrange basis of
+// the nodes 0..d (prefix and suffix products of r - y); false when the
+// previous message was not recorded.
+static host::Fr64 message_at(const std::vector<host::Fr64> &msg, const std::vector<host::Fr64> &lag_den,
+                             const host::Fr64 &r) {
+    const size_t D = lag_den.size() - 1;
+    std::vector<host::Fr64> diff(D + 1), pre(D + 1), suf(D + 1);
+    for (size_t y = 0; y <= D; y++) diff[y] = host::add(r, host::neg(host::from_u64(uint64_t(y))));
+    pre[0] = host::one();
+    for (size_t x = 1; x <= D; x++) pre[x] = host::mont_mul(pre[x - 1], diff[x - 1]);
+    suf[D] = host::one();
+    for (size_t x = D; x-- > 0;) suf[x] = host::mont_mul(suf[x + 1], diff[x + 1]);
+    host::Fr64 acc{{0, 0, 0, 0}};
+    for (size_t x = 0; x <= D; x++) {
+        const host::Fr64 l = host::mont_mul(host::mont_mul(pre[x], suf[x]), lag_den[x]);
+        acc = host::add(acc, host::mont_mul(l, msg[x]));
+    }
+    return acc;
+}
+static bool round_claim(const HpCudaSumCheckProverState *s, const host::Fr64 &r, host::Fr64 &out) {
+    if (s->round == 0 || s->last_round != s->round - 1) return false;
+    out = message_at(s->last_msg, s->lag_den, r);
+    return true;
+}
 
 static size_t big_blocks_per_sm();
 
@@ -929,6 +1014,20 @@ static Fr *round_partials(HpCudaContext *ctx, HpCudaSumCheckProverState *s, size
 // Lagrange basis polynomial of the nodes 0..m (m = arity of product p):
 // l_{m,i}(x) = [x == i] for x <= m, else
 // prod_{k != i} (x - k) / ((-1)^(m-i) i! (m-i)!).
+// 1 / prod_{y != x} (x - y) = (-1)^(D - x) / (x! (D - x)!) for x = 0..D
+static std::vector<host::Fr64> lagrange_denominators(size_t D) {
+    std::vector<host::Fr64> fact(D + 1), inv_fact(D + 1), out(D + 1);
+    fact[0] = host::one();
+    for (size_t k = 1; k <= D; k++) fact[k] = host::mont_mul(fact[k - 1], host::from_u64(uint64_t(k)));
+    inv_fact[D] = host::inverse(fact[D]);
+    for (size_t k = D; k >= 1; k--) inv_fact[k - 1] = host::mont_mul(inv_fact[k], host::from_u64(uint64_t(k)));
+    for (size_t x = 0; x <= D; x++) {
+        out[x] = host::mont_mul(inv_fact[x], inv_fact[D - x]);
+        if ((D - x) & 1) out[x] = host::neg(out[x]);
+    }
+    return out;
+}
+
 static std::vector<host::Fr64> extrapolation_weights(const SumcheckDesc &d, const uint8_t *coefficients,
                                                      size_t degree) {
     using host::Fr64;
@@ -1018,6 +1117,7 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_create(
                 max_arity = std::max(max_arity, m);
             }
             d.offsets[product_count] = uint16_t(index_count);
+            for (int p = 0; p < hp::kMaxProducts; p++) d.node0[p] = 0;
             for (int f = 0; f < hp::kMaxFactors; f++) d.writer[f] = hp::kNoWriter;
             for (size_t i = 0; i < index_count; i++) {
                 d.indices[i] = uint8_t(factor_indices[i]);
@@ -1031,10 +1131,39 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_create(
                 s->inputs.push_back(factors[f]);
             }
             std::vector<hp::host::Fr64> w = hp::extrapolation_weights(d, coefficients, max_degree);
-            s->weights = ctx->scratch((w.size() + 3) * sizeof(Fr));
-            check_cuda(cudaMemsetAsync(s->weights, 0, 3 * sizeof(Fr), ctx->stream));
-            check_cuda(cudaMemcpyAsync(static_cast<Fr *>(s->weights) + 3, w.data(), w.size() * sizeof(Fr),
+            // rounds 2..: products of arity = degree lose their t = 0 slot; the
+            // reduced matrix keeps rows 1..d of the remaining columns and takes
+            // minus row 1 as row 0 (the claim is added to it)
+            hp::SumcheckDesc &dr = s->desc_red;
+            dr = d;
+            int rslots = 0;
+            for (size_t p = 0; p < product_count; p++) {
+                const int m = int(product_offsets[p + 1] - product_offsets[p]);
+                dr.node0[p] = uint8_t(size_t(m) == max_degree ? 1 : 0);
+                dr.slot_base[p] = uint16_t(rslots);
+                rslots += m + 1 - dr.node0[p];
+            }
+            dr.slot_count = std::max(rslots, 1);
+            s->red_uniform = product_count > 0;
+            for (size_t p = 0; p < product_count; p++) s->red_uniform = s->red_uniform && dr.node0[p] == 1;
+            const size_t S = size_t(d.slot_count), SR = size_t(dr.slot_count), D = max_degree;
+            std::vector<hp::host::Fr64> wr((D + 1) * SR, hp::host::Fr64{{0, 0, 0, 0}});
+            for (size_t p = 0; p < product_count; p++) {
+                const int m = int(product_offsets[p + 1] - product_offsets[p]);
+                for (int t = dr.node0[p]; t <= m; t++)
+                    for (size_t x = 1; x <= D; x++)
+                        wr[x * SR + dr.slot_base[p] + size_t(t - dr.node0[p])] = w[x * S + d.slot_base[p] + size_t(t)];
+            }
+            if (D >= 1)
+                for (size_t c = 0; c < SR; c++) wr[c] = hp::host::neg(wr[SR + c]);
+            s->lag_den = hp::lagrange_denominators(D);
+            s->weights_full = w.size();
+            s->weights = ctx->scratch((w.size() + wr.size() + 4) * sizeof(Fr));
+            check_cuda(cudaMemsetAsync(s->weights, 0, 4 * sizeof(Fr), ctx->stream));
+            check_cuda(cudaMemcpyAsync(static_cast<Fr *>(s->weights) + 4, w.data(), w.size() * sizeof(Fr),
                                        cudaMemcpyHostToDevice, ctx->stream));
+            check_cuda(cudaMemcpyAsync(static_cast<Fr *>(s->weights) + 4 + w.size(), wr.data(),
+                                       wr.size() * sizeof(Fr), cudaMemcpyHostToDevice, ctx->stream));
             s->partials_bytes = hp::partials_capacity(d, ctx->sm_count);
             s->partials = ctx->scratch(s->partials_bytes);
             ctx->sync();  // w is a pageable host vector
@@ -1170,7 +1299,16 @@ static void fold_all(HpCudaContext *ctx, const SumcheckDesc &d, const FrPtrList 
 // is ordered on st.  Does not advance the state.
 static void launch_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, const Fr &r, cudaStream_t st,
                          Fr *out_dev, const RoundShape &sh, const RoundRoute &rt) {
-    const SumcheckDesc &d = s->desc;
+    // rounds after the first whose previous message was recorded take the
+    // reduced layout and the claim (same message bytes, fewer slot products)
+    host::Fr64 r64, claim64;
+    std::memcpy(r64.v, r.v, 32);
+    const bool pp_route = rt.kernel == kRoutePp || rt.kernel == kRoutePpFused;
+    const bool red = (!pp_route || s->red_uniform) && round_claim(s, r64, claim64);
+    const SumcheckDesc &d = red ? s->desc_red : s->desc;
+    const Fr *wts = red ? state_weights_red(s) : state_weights(s);
+    Fr claim = Fr::zero();
+    if (red) std::memcpy(claim.v, claim64.v, 32);
     const bool fold = sh.fold;
     const int src_which = s->current;
     const int dst_which = fold ? (src_which == 1 ? 2 : 1) : src_which;
@@ -1203,11 +1341,16 @@ static void launch_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, const
             const size_t smem = size_t(d.slot_count) * sizeof(Fr);
             auto launch = [&](auto kernel) {
                 kernel<<<grid, kPpThreads, smem, st>>>(d, tables, dst, fused_fold, r, pairs, bpp, partials,
-                                                       round_counter(s), state_weights(s), int(s->max_degree),
-                                                       out_dev);
+                                                       round_counter(s), wts, int(s->max_degree), out_dev, claim,
+                                                       red);
             };
-            if (d.max_arity <= 2) launch(k_sumcheck_round_pp<2>);
-            else launch(k_sumcheck_round_pp<3>);
+            if (red) {
+                if (d.max_arity <= 2) launch(k_sumcheck_round_pp<2, 1>);
+                else launch(k_sumcheck_round_pp<3, 1>);
+            } else {
+                if (d.max_arity <= 2) launch(k_sumcheck_round_pp<2, 0>);
+                else launch(k_sumcheck_round_pp<3, 0>);
+            }
             check_launch();
             break;
         }
@@ -1235,8 +1378,8 @@ static void launch_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, const
                 if (smem > 32 * 1024)
                     check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
                 kernel<<<grid, kWideThreads, smem, st>>>(d, tables, dst, fused_fold, r, pairs, bps, partials,
-                                                         round_counter(s), state_weights(s), int(s->max_degree),
-                                                         out_dev);
+                                                         round_counter(s), wts, int(s->max_degree), out_dev, claim,
+                                                         red);
             };
             if (d.max_arity <= 2) launch(k_sumcheck_round_wide<2>);
             else if (d.max_arity <= 4) launch(k_sumcheck_round_wide<4>);
@@ -1251,8 +1394,8 @@ static void launch_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, const
             auto launch = [&](auto kernel) {
                 if (smem > 32 * 1024)
                     check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-                kernel<<<1, kSmallThreads, smem, st>>>(d, src, dst, rd, fold, r, int(pairs), state_weights(s),
-                                                       int(s->max_degree), out_dev);
+                kernel<<<1, kSmallThreads, smem, st>>>(d, src, dst, rd, fold, r, int(pairs), wts,
+                                                       int(s->max_degree), out_dev, claim, red);
             };
             if (d.max_arity <= 2) launch(k_sumcheck_round_small<2>);
             else if (d.max_arity <= 4) launch(k_sumcheck_round_small<4>);
@@ -1272,8 +1415,8 @@ static void launch_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, const
                 if (smem > 32 * 1024)
                     check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
                 kernel<<<grid, kRoundThreads, smem, st>>>(d, src, dst, rd, fold, r, pairs, partials,
-                                                          round_counter(s), state_weights(s), int(s->max_degree),
-                                                          out_dev);
+                                                          round_counter(s), wts, int(s->max_degree), out_dev, claim,
+                                                          red);
             };
             if (d.max_arity <= 2) launch(k_sumcheck_round_regs<2>);
             else if (d.max_arity <= 4) launch(k_sumcheck_round_regs<4>);
@@ -1373,6 +1516,7 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_round(HpCudaContext *ct
             hp::enqueue_round(ctx, s, r, ctx->stream, static_cast<Fr *>(box_dev));
             ctx->sync();
             std::memcpy(out_evaluations, box, evaluation_count * sizeof(Fr));
+            hp::record_message(s, s->round, out_evaluations);
             hp::advance(s);
         } catch (const hp::Failure &f) {
             if (f.kind == HP_CUDA_STATUS_INVALID_STATE) s->poisoned = true;
@@ -1416,6 +1560,7 @@ extern "C" HpCudaStatus hp_cuda_v1_batch_sumcheck_round(HpCudaContext *ctx, HpCu
             for (size_t i = 0; i < count; i++) {
                 std::memcpy(out_evaluations[i], box + off * sizeof(Fr), evaluation_counts[i] * sizeof(Fr));
                 off += evaluation_counts[i];
+                hp::record_message(states[i], states[i]->round, out_evaluations[i]);
                 hp::advance(states[i]);
             }
         } catch (const hp::Failure &f) {
@@ -1514,21 +1659,30 @@ static uint32_t *state_relay(HpCudaSumCheckProverState *s) {
 static void run_resident(HpCudaContext *ctx, HpCudaSumCheckProverState *s, size_t k0, const Fr &r_prev,
                          HpMerlinTranscript *transcript, uint8_t *out_messages, uint8_t *out_challenges,
                          bool grid) {
-    const SumcheckDesc &d = s->desc;
+    // rounds k0 >= 1: the reduced layout, with the claim of round k0 from the
+    // recorded message of round k0 - 1 and the host's claims after it
+    const SumcheckDesc &d = s->desc_red;
     const size_t nv = s->num_vars, d1 = s->max_degree + 1;
     const int rounds = int(nv - k0);
     const size_t pairs0 = table_len(nv - k0 - 1);
-    // handshake: 32-byte header, the challenges, the messages
-    const size_t box_bytes = 32 + size_t(rounds) * sizeof(Fr) * (1 + d1);
+    host::Fr64 r64, claim64;
+    std::memcpy(r64.v, r_prev.v, 32);
+    if (k0 == 0 || !round_claim(s, r64, claim64)) fail(HP_CUDA_STATUS_INVALID_STATE);
+    Fr claim0;
+    std::memcpy(claim0.v, claim64.v, 32);
+    // handshake: 32-byte header, the challenges, the claims, the messages
+    const size_t box_bytes = 32 + size_t(rounds) * sizeof(Fr) * (2 + d1);
     void *box_dev = nullptr;
     uint8_t *box = ctx->mailbox(box_bytes, &box_dev);
     uint32_t *hdr = reinterpret_cast<uint32_t *>(box);
     Fr *challenges = reinterpret_cast<Fr *>(box + 32);
-    const Fr *messages = challenges + rounds;
+    Fr *claims = challenges + rounds;
+    const Fr *messages = claims + rounds;
     Handshake hs;
     hs.hdr = static_cast<uint32_t *>(box_dev);
     hs.challenges = reinterpret_cast<Fr *>(static_cast<uint8_t *>(box_dev) + 32);
-    hs.messages = hs.challenges + rounds;
+    hs.claims = hs.challenges + rounds;
+    hs.messages = hs.claims + rounds;
     volatile uint32_t *seq = &hdr[0];
     hdr[0] = hdr[1] = hdr[2] = 0;
     // where the per-round path would leave the tables: one buffer swap per
@@ -1549,7 +1703,7 @@ static void run_resident(HpCudaContext *ctx, HpCudaSumCheckProverState *s, size_
         bool fold_first = k0 > 0;
         Fr r0 = r_prev;
         int tile = resident_tile(d);
-        const Fr *w = state_weights(s);
+        const Fr *w = state_weights_red(s);
         int degree = int(s->max_degree);
         uint64_t *limb_sums = static_cast<uint64_t *>(s->partials);  // 2 x 8 x kMaxSlotsV2 counters
         check_cuda(cudaMemsetAsync(limb_sums, 0, 2 * 8 * kMaxSlotsV2 * sizeof(uint64_t), ctx->stream));
@@ -1567,7 +1721,7 @@ static void run_resident(HpCudaContext *ctx, HpCudaSumCheckProverState *s, size_
             size_t blocks = sms * size_t(std::min(per_sm, 2));
             blocks = std::max<size_t>(1, std::min(blocks, (pairs0 + kResMinPairs - 1) / kResMinPairs));
             void *args[] = {const_cast<SumcheckDesc *>(&d), &fb, &which0, &fold_first, &r0, &p0, &nrounds,
-                            &tile, &w, &degree, &limb_sums, &counter, &relay, &hs};
+                            &tile, &w, &degree, &claim0, &limb_sums, &counter, &relay, &hs};
             check_cuda(cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(kernel), dim3(unsigned(blocks)),
                                                    dim3(kResThreads), args, smem, ctx->stream));
         };
@@ -1586,7 +1740,7 @@ static void run_resident(HpCudaContext *ctx, HpCudaSumCheckProverState *s, size_
         auto launch = [&](auto kernel) {
             check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
             kernel<<<1, kTailThreads, smem, ctx->stream>>>(d, src, dst, k0 > 0, r_prev, int(pairs0), rounds,
-                                                           state_weights(s), int(s->max_degree), hs);
+                                                           state_weights_red(s), int(s->max_degree), claim0, hs);
         };
         if (d.max_arity <= 2) launch(k_sumcheck_tail<2>);
         else if (d.max_arity <= 4) launch(k_sumcheck_tail<4>);
@@ -1624,6 +1778,12 @@ static void run_resident(HpCudaContext *ctx, HpCudaSumCheckProverState *s, size_
         merlin_append(transcript, "Internal round", canon, 32);
         std::memcpy(out_challenges + 32 * (k0 + j), canon, 32);
         if (j + 1 < rounds) {
+            // the next round's claim: this message's polynomial at c
+            std::vector<host::Fr64> mv(d1);
+            for (size_t x = 0; x < d1; x++)
+                if (!host::from_canonical(m + 32 * x, mv[x])) fail(HP_CUDA_STATUS_INVALID_STATE);
+            const host::Fr64 nc = message_at(mv, s->lag_den, c);
+            std::memcpy(&claims[j + 1], nc.v, 32);
             std::memcpy(&challenges[j], c.v, 32);
             __atomic_store_n(&hdr[1], uint32_t(j + 1), __ATOMIC_RELEASE);
         }
@@ -1657,8 +1817,9 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prove_rounds(HpCudaContext *ctx, HpC
         const size_t tail = resident ? 0 : hp::tail_pairs(s);
         for (size_t k = 0; k < rounds; k++) {
             const size_t pairs = hp::table_len(rounds - k - 1);
-            if ((resident > 0 && pairs <= resident) || (tail > 0 && pairs <= tail)) {
-                // this and every later round in one resident launch
+            if (k > 0 && ((resident > 0 && pairs <= resident) || (tail > 0 && pairs <= tail))) {
+                // this and every later round in one resident launch (from the
+                // second round on: the resident kernels take the reduced layout)
                 try {
                     hp::run_resident(ctx, s, k, r, transcript, out_messages, out_challenges, resident > 0);
                 } catch (const hp::Failure &f) {
@@ -1670,6 +1831,7 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prove_rounds(HpCudaContext *ctx, HpC
             try {
                 hp::enqueue_round(ctx, s, r, ctx->stream, static_cast<Fr *>(box_dev));
                 ctx->sync();
+                hp::record_message(s, k, box);
                 hp::advance(s);
             } catch (const hp::Failure &f) {
                 if (f.kind == HP_CUDA_STATUS_INVALID_STATE) s->poisoned = true;
@@ -1783,6 +1945,7 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_autotune(HpCudaContext *ctx, HpCudaS
                                      best, best_us);
                 run_once(best);
                 ctx->sync();
+                record_message(s, k, box);
                 advance(s);
                 HpCudaRoundTuning &o = out[k];
                 o.pairs = uint64_t(sh.pairs);

@@ -26,6 +26,11 @@ struct SumcheckDesc {
     // (kNoWriter if f is in no product); the wide round kernel's item at that
     // position and t = 0 stores f's folded pair
     uint16_t writer[kMaxFactors];
+    // node0[p]: the first node t whose slot product p has (its slots are
+    // t = node0[p] .. arity).  0 in round 1; 1 from round 2 on for products
+    // of arity equal to the degree, whose t = 0 share of the message the
+    // round's claim supplies: p(0) = claim - p(1), claim = p_prev(r_prev).
+    uint8_t node0[kMaxProducts];
 };
 
 constexpr uint16_t kNoWriter = 0xffff;
