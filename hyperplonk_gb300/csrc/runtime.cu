@@ -3,7 +3,11 @@
 // (reference bridge.h:43-45, bridge_runtime.cpp).
 #include <algorithm>
 #include <atomic>
+#include <condition_variable>
 #include <cstring>
+#include <exception>
+#include <mutex>
+#include <thread>
 
 #include "runtime.cuh"
 
@@ -234,9 +238,75 @@ extern "C" HpCudaStatus hp_cuda_v1_context_create(int32_t device_id, HpCudaConte
     });
 }
 
+struct HpCudaContext::Responder {
+    std::thread thread;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::function<void()> job;
+    bool stop = false;
+    std::atomic<int> state{0};  // 0 idle, 1 queued or running, 2 finished
+    std::exception_ptr error;
+};
+
+void HpCudaContext::respond_start(std::function<void()> job) {
+    if (!responder) {
+        responder = std::make_unique<Responder>();
+        Responder *r = responder.get();
+        const int dev = device;
+        r->thread = std::thread([r, dev] {
+            cudaSetDevice(dev);
+            std::unique_lock<std::mutex> lk(r->mu);
+            for (;;) {
+                r->cv.wait(lk, [r] { return r->stop || bool(r->job); });
+                if (r->stop) return;
+                std::function<void()> j = std::move(r->job);
+                r->job = nullptr;
+                lk.unlock();
+                try {
+                    j();
+                } catch (...) {
+                    r->error = std::current_exception();
+                }
+                r->state.store(2, std::memory_order_release);
+                lk.lock();
+            }
+        });
+    }
+    {
+        std::lock_guard<std::mutex> lk(responder->mu);
+        responder->error = nullptr;
+        responder->state.store(1, std::memory_order_relaxed);
+        responder->job = std::move(job);
+    }
+    responder->cv.notify_one();
+}
+
+void HpCudaContext::respond_wait() {
+    if (!responder) return;
+    while (responder->state.load(std::memory_order_acquire) == 1) std::this_thread::yield();
+    responder->state.store(0, std::memory_order_relaxed);
+    if (responder->error) {
+        std::exception_ptr e = responder->error;
+        responder->error = nullptr;
+        std::rethrow_exception(e);
+    }
+}
+
+void HpCudaContext::respond_shutdown() {
+    if (!responder) return;
+    {
+        std::lock_guard<std::mutex> lk(responder->mu);
+        responder->stop = true;
+    }
+    responder->cv.notify_one();
+    if (responder->thread.joinable()) responder->thread.join();
+    responder.reset();
+}
+
 extern "C" HpCudaStatus hp_cuda_v1_context_destroy(HpCudaContext *ctx) {
     return guard([&] {
         require(ctx != nullptr);
+        ctx->respond_shutdown();
         cudaSetDevice(ctx->device);
         if (ctx->ingress_stream) cudaStreamSynchronize(ctx->ingress_stream);
         cudaError_t first = cudaStreamSynchronize(ctx->stream);

@@ -16,6 +16,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <functional>
 #include <map>
 #include <memory>
 #include <new>
@@ -166,6 +167,17 @@ struct HpCudaContext {
     size_t mailbox_bytes = 0;
     // Host pointer to >= `bytes` of the mailbox; *dev gets its device alias.
     uint8_t *mailbox(size_t bytes, void **dev);
+    // A host thread beside the calling one that runs one job at a time
+    // (created on first use, joined by context_destroy): the Fiat-Shamir loop
+    // of a resident sumcheck launch runs there, so the launch call may return
+    // only when the kernel has finished (CUDA_LAUNCH_BLOCKING, profilers that
+    // serialise launches) while the kernel waits for the loop's challenges.
+    struct Responder;
+    std::unique_ptr<Responder> responder;
+    void respond_start(std::function<void()> job);
+    // Waits for the job and rethrows its exception, if any.
+    void respond_wait();
+    void respond_shutdown();
     // Clear the device status word (stream ordered).
     void clear_flags();
     // Synchronize and return the status word.

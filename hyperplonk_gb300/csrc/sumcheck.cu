@@ -24,6 +24,7 @@
 // any slot count go through the (slot, pair) kernel; the per-pair kernel
 // with per-thread slot sums in shared memory remains for HP_BIG_SLOTS=0.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstdlib>
 #include <cstring>
@@ -1595,9 +1596,26 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_final_evaluations(
 
 namespace hp {
 
+// Whether a kernel profiler is attached (Nsight Compute's injection sets
+// these): the resident kernels exchange messages and challenges with the
+// host while they run, which a profiled launch does not allow, so under a
+// profiler they would wait until their bounded spins ran out; such runs take
+// one launch per round instead.
+static bool profiler_attached() {
+    static const bool v = [] {
+        for (const char *name : {"NV_COMPUTE_PROFILER_PERFWORKS_DIR", "NVIDIA_PROCESS_INJECTION_CRASH_REPORTING",
+                                 "CUDA_INJECTION64_PATH"}) {
+            const char *e = std::getenv(name);
+            if (e != nullptr && *e != '\0') return true;
+        }
+        return false;
+    }();
+    return v;
+}
+
 // HP_SUMCHECK_TAIL=0: no resident tail block (every round a launch of its own).
 static bool tail_enabled() {
-    static const bool v = env_size("HP_SUMCHECK_TAIL", 1) != 0;
+    static const bool v = env_size("HP_SUMCHECK_TAIL", 1) != 0 && !profiler_attached();
     return v;
 }
 
@@ -1635,7 +1653,7 @@ static int resident_tile(const SumcheckDesc &d) {
 // none); 0 when the shape takes none (products of arity > 8, more than
 // kMaxSlotsV2 slots, no products).
 static size_t resident_pairs(const HpCudaSumCheckProverState *s) {
-    static const bool on = env_size("HP_SUMCHECK_RESIDENT", 1) != 0;
+    static const bool on = env_size("HP_SUMCHECK_RESIDENT", 1) != 0 && !profiler_attached();
     static const size_t first = env_size("HP_SUMCHECK_RESIDENT_PAIRS", 0);
     const SumcheckDesc &d = s->desc;
     if (!on || d.product_count == 0 || d.max_arity > 8 || d.slot_count > kMaxSlotsV2) return 0;
@@ -1692,102 +1710,124 @@ static void run_resident(HpCudaContext *ctx, HpCudaSumCheckProverState *s, size_
     sim.current = s->current;
     for (int j = 0; j < rounds; j++) advance(&sim);
     int tok = ctx->prof_begin("sumcheck_round", ctx->stream);
-    if (grid) {
-        FoldBuffers fb;
-        for (int f = 0; f < d.factor_count; f++) fb.inputs.p[f] = state_table(s, 0, f);
-        fb.a = static_cast<Fr *>(s->fold_a);
-        fb.b = static_cast<Fr *>(s->fold_b);
-        fb.a_stride = nv >= 1 ? table_len(nv - 1) : 1;
-        fb.b_stride = nv >= 2 ? table_len(nv - 2) : 1;
-        int which0 = s->current;
-        bool fold_first = k0 > 0;
-        Fr r0 = r_prev;
-        int tile = resident_tile(d);
-        const Fr *w = state_weights_red(s);
-        int degree = int(s->max_degree);
-        uint64_t *limb_sums = static_cast<uint64_t *>(s->partials);  // 2 x 8 x kMaxSlotsV2 counters
-        check_cuda(cudaMemsetAsync(limb_sums, 0, 2 * 8 * kMaxSlotsV2 * sizeof(uint64_t), ctx->stream));
-        unsigned *counter = round_counter(s);
-        uint32_t *relay = state_relay(s);
-        size_t p0 = pairs0;
-        int nrounds = rounds;
-        const size_t smem = (size_t(d.factor_count) * 2 * tile + kResThreads) * sizeof(Fr);
-        const size_t sms = size_t(ctx->sm_count > 0 ? ctx->sm_count : 152);
-        auto launch = [&](auto kernel) {
-            check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-            int per_sm = 0;
-            check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kResThreads, smem));
-            if (per_sm < 1) fail(HP_CUDA_STATUS_NOT_IMPLEMENTED);
-            size_t blocks = sms * size_t(std::min(per_sm, 2));
-            blocks = std::max<size_t>(1, std::min(blocks, (pairs0 + kResMinPairs - 1) / kResMinPairs));
-            void *args[] = {const_cast<SumcheckDesc *>(&d), &fb, &which0, &fold_first, &r0, &p0, &nrounds,
-                            &tile, &w, &degree, &claim0, &limb_sums, &counter, &relay, &hs};
-            check_cuda(cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(kernel), dim3(unsigned(blocks)),
-                                                   dim3(kResThreads), args, smem, ctx->stream));
-        };
-        if (d.max_arity <= 2) launch(k_sumcheck_resident<2>);
-        else if (d.max_arity <= 4) launch(k_sumcheck_resident<4>);
-        else if (d.max_arity <= 6) launch(k_sumcheck_resident<6>);
-        else launch(k_sumcheck_resident<8>);
-    } else {
-        FrPtrList src{};
-        FrMutPtrList dst{};
-        for (int f = 0; f < d.factor_count; f++) {
-            src.p[f] = state_table(s, s->current, f);
-            dst.p[f] = const_cast<Fr *>(state_table(s, sim.current, f));
-        }
-        const size_t smem = tail_smem(d, pairs0);
-        auto launch = [&](auto kernel) {
-            check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-            kernel<<<1, kTailThreads, smem, ctx->stream>>>(d, src, dst, k0 > 0, r_prev, int(pairs0), rounds,
-                                                           state_weights_red(s), int(s->max_degree), claim0, hs);
-        };
-        if (d.max_arity <= 2) launch(k_sumcheck_tail<2>);
-        else if (d.max_arity <= 4) launch(k_sumcheck_tail<4>);
-        else if (d.max_arity <= 6) launch(k_sumcheck_tail<6>);
-        else launch(k_sumcheck_tail<8>);
-    }
-    check_launch();
-    std::vector<uint8_t> msg(8 + 32 * d1, 0);
-    for (int b = 0; b < 8; b++) msg[b] = uint8_t(uint64_t(d1) >> (8 * b));
-    for (int j = 0; j < rounds; j++) {
-        // the launch's message j: poll the mapped sequence number; the blocks
-        // themselves give up after kTailSpinLimit polls, and a launch that
-        // ends without the message is an error
-        uint64_t polls = 0;
-        const auto t0 = std::chrono::steady_clock::now();
-        while (__atomic_load_n(seq, __ATOMIC_ACQUIRE) < uint32_t(j + 1)) {
-            if ((++polls & 1023) == 0) {
-                if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(60)) fail(HP_CUDA_STATUS_INVALID_STATE);
-                const cudaError_t e = cudaStreamQuery(ctx->stream);
-                if (e != cudaErrorNotReady) {
-                    if (__atomic_load_n(seq, __ATOMIC_ACQUIRE) >= uint32_t(j + 1)) break;
-                    check_cuda(e);
-                    fail(HP_CUDA_STATUS_INVALID_STATE);
+    // the Fiat-Shamir loop runs on the context's responder thread, so the
+    // launch below may block until the kernel ends
+    std::atomic<bool> cancel{false};
+    ctx->respond_start([&] {
+        std::vector<uint8_t> msg(8 + 32 * d1, 0);
+        for (int b = 0; b < 8; b++) msg[b] = uint8_t(uint64_t(d1) >> (8 * b));
+        for (int j = 0; j < rounds; j++) {
+            // the launch's message j: poll the mapped sequence number; the blocks
+            // themselves give up after kTailSpinLimit polls, and a launch that
+            // ends without the message is an error
+            uint64_t polls = 0;
+            const auto t0 = std::chrono::steady_clock::now();
+            while (__atomic_load_n(seq, __ATOMIC_ACQUIRE) < uint32_t(j + 1)) {
+                if (cancel.load(std::memory_order_relaxed)) fail(HP_CUDA_STATUS_INVALID_STATE);
+                if ((++polls & 1023) == 0) {
+                    const auto waited = std::chrono::steady_clock::now() - t0;
+                    if (waited > std::chrono::seconds(60)) fail(HP_CUDA_STATUS_INVALID_STATE);
+                    // a launch that ended without the message (checked only after
+                    // 100 ms without one, so that no runtime call competes with a
+                    // launch that serialised tools hold open)
+                    if (waited > std::chrono::milliseconds(100)) {
+                        const cudaError_t e = cudaStreamQuery(ctx->stream);
+                        if (e != cudaErrorNotReady) {
+                            if (__atomic_load_n(seq, __ATOMIC_ACQUIRE) >= uint32_t(j + 1)) break;
+                            check_cuda(e);
+                            fail(HP_CUDA_STATUS_INVALID_STATE);
+                        }
+                    }
                 }
             }
+            const uint8_t *m = reinterpret_cast<const uint8_t *>(messages + size_t(j) * d1);
+            std::memcpy(msg.data() + 8, m, 32 * d1);
+            std::memcpy(out_messages + 32 * d1 * (k0 + j), m, 32 * d1);
+            merlin_append(transcript, "prover msg", msg.data(), msg.size());
+            uint8_t wide[64], canon[32];
+            merlin_challenge(transcript, "Internal round", wide, 64);
+            const host::Fr64 c = host::from_wide64(wide);
+            host::to_canonical(c, canon);
+            merlin_append(transcript, "Internal round", canon, 32);
+            std::memcpy(out_challenges + 32 * (k0 + j), canon, 32);
+            if (j + 1 < rounds) {
+                // the next round's claim: this message's polynomial at c
+                std::vector<host::Fr64> mv(d1);
+                for (size_t x = 0; x < d1; x++)
+                    if (!host::from_canonical(m + 32 * x, mv[x])) fail(HP_CUDA_STATUS_INVALID_STATE);
+                const host::Fr64 nc = message_at(mv, s->lag_den, c);
+                std::memcpy(&claims[j + 1], nc.v, 32);
+                std::memcpy(&challenges[j], c.v, 32);
+                __atomic_store_n(&hdr[1], uint32_t(j + 1), __ATOMIC_RELEASE);
+            }
         }
-        const uint8_t *m = reinterpret_cast<const uint8_t *>(messages + size_t(j) * d1);
-        std::memcpy(msg.data() + 8, m, 32 * d1);
-        std::memcpy(out_messages + 32 * d1 * (k0 + j), m, 32 * d1);
-        merlin_append(transcript, "prover msg", msg.data(), msg.size());
-        uint8_t wide[64], canon[32];
-        merlin_challenge(transcript, "Internal round", wide, 64);
-        const host::Fr64 c = host::from_wide64(wide);
-        host::to_canonical(c, canon);
-        merlin_append(transcript, "Internal round", canon, 32);
-        std::memcpy(out_challenges + 32 * (k0 + j), canon, 32);
-        if (j + 1 < rounds) {
-            // the next round's claim: this message's polynomial at c
-            std::vector<host::Fr64> mv(d1);
-            for (size_t x = 0; x < d1; x++)
-                if (!host::from_canonical(m + 32 * x, mv[x])) fail(HP_CUDA_STATUS_INVALID_STATE);
-            const host::Fr64 nc = message_at(mv, s->lag_den, c);
-            std::memcpy(&claims[j + 1], nc.v, 32);
-            std::memcpy(&challenges[j], c.v, 32);
-            __atomic_store_n(&hdr[1], uint32_t(j + 1), __ATOMIC_RELEASE);
+    });
+    try {
+        if (grid) {
+            FoldBuffers fb;
+            for (int f = 0; f < d.factor_count; f++) fb.inputs.p[f] = state_table(s, 0, f);
+            fb.a = static_cast<Fr *>(s->fold_a);
+            fb.b = static_cast<Fr *>(s->fold_b);
+            fb.a_stride = nv >= 1 ? table_len(nv - 1) : 1;
+            fb.b_stride = nv >= 2 ? table_len(nv - 2) : 1;
+            int which0 = s->current;
+            bool fold_first = k0 > 0;
+            Fr r0 = r_prev;
+            int tile = resident_tile(d);
+            const Fr *w = state_weights_red(s);
+            int degree = int(s->max_degree);
+            uint64_t *limb_sums = static_cast<uint64_t *>(s->partials);  // 2 x 8 x kMaxSlotsV2 counters
+            check_cuda(cudaMemsetAsync(limb_sums, 0, 2 * 8 * kMaxSlotsV2 * sizeof(uint64_t), ctx->stream));
+            unsigned *counter = round_counter(s);
+            uint32_t *relay = state_relay(s);
+            size_t p0 = pairs0;
+            int nrounds = rounds;
+            const size_t smem = (size_t(d.factor_count) * 2 * tile + kResThreads) * sizeof(Fr);
+            const size_t sms = size_t(ctx->sm_count > 0 ? ctx->sm_count : 152);
+            auto launch = [&](auto kernel) {
+                check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+                int per_sm = 0;
+                check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kResThreads, smem));
+                if (per_sm < 1) fail(HP_CUDA_STATUS_NOT_IMPLEMENTED);
+                size_t blocks = sms * size_t(std::min(per_sm, 2));
+                blocks = std::max<size_t>(1, std::min(blocks, (pairs0 + kResMinPairs - 1) / kResMinPairs));
+                void *args[] = {const_cast<SumcheckDesc *>(&d), &fb, &which0, &fold_first, &r0, &p0, &nrounds,
+                                &tile, &w, &degree, &claim0, &limb_sums, &counter, &relay, &hs};
+                check_cuda(cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(kernel), dim3(unsigned(blocks)),
+                                                       dim3(kResThreads), args, smem, ctx->stream));
+            };
+            if (d.max_arity <= 2) launch(k_sumcheck_resident<2>);
+            else if (d.max_arity <= 4) launch(k_sumcheck_resident<4>);
+            else if (d.max_arity <= 6) launch(k_sumcheck_resident<6>);
+            else launch(k_sumcheck_resident<8>);
+        } else {
+            FrPtrList src{};
+            FrMutPtrList dst{};
+            for (int f = 0; f < d.factor_count; f++) {
+                src.p[f] = state_table(s, s->current, f);
+                dst.p[f] = const_cast<Fr *>(state_table(s, sim.current, f));
+            }
+            const size_t smem = tail_smem(d, pairs0);
+            auto launch = [&](auto kernel) {
+                check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+                kernel<<<1, kTailThreads, smem, ctx->stream>>>(d, src, dst, k0 > 0, r_prev, int(pairs0), rounds,
+                                                               state_weights_red(s), int(s->max_degree), claim0, hs);
+            };
+            if (d.max_arity <= 2) launch(k_sumcheck_tail<2>);
+            else if (d.max_arity <= 4) launch(k_sumcheck_tail<4>);
+            else if (d.max_arity <= 6) launch(k_sumcheck_tail<6>);
+            else launch(k_sumcheck_tail<8>);
         }
+        check_launch();
+    } catch (...) {
+        cancel.store(true);
+        try {
+            ctx->respond_wait();
+        } catch (...) {
+        }
+        throw;
     }
+    ctx->respond_wait();
     ctx->sync();
     ctx->prof_end(tok, ctx->stream);
     if (__atomic_load_n(&hdr[2], __ATOMIC_ACQUIRE)) fail(HP_CUDA_STATUS_INVALID_STATE);

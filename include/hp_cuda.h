@@ -332,7 +332,10 @@ HpCudaStatus hp_host_v1_keccak_f1600(uint8_t *state200);
  * state is at round 0; an execution failure poisons the state.  The middle
  * and last rounds (from the first of <= 2^15 or 2^17 pairs, by shape) run in
  * one resident cooperative launch that exchanges messages and challenges
- * with this call through the context's mapped mailbox.  No counterpart in the reference (its caller drives the
+ * with this call through the context's mapped mailbox; the host side of that
+ * exchange runs on a thread the context creates on first use (joined by
+ * hp_cuda_v1_context_destroy).  While a kernel profiler is attached every
+ * round is a launch of its own.  No counterpart in the reference (its caller drives the
  * rounds one at a time through the transcript). */
 HpCudaStatus hp_cuda_v1_sumcheck_prove_rounds(HpCudaContext *ctx, HpCudaSumCheckProverState *state,
                                               HpMerlinTranscript *transcript, size_t rounds,
