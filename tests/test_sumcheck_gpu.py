@@ -87,6 +87,38 @@ def test_mixed_arity_large_rounds(gpu, cpu, oracle):
     run_both(gpu, cpu, vg, vc, 15)
 
 
+# Rounds after the first take p(0) from the previous round's claim, and
+# products whose arity equals the degree drop their t = 0 slot.  nv = 18
+# reaches the (product, pair) kernel (>= 2^16 pairs): arity 3 everywhere takes
+# its reduced form, arity 2 next to arity 3 keeps the full layout there and
+# per-product first nodes in the resident grid; the native transcript runs
+# prove_rounds (resident from 2^15 pairs), the oracle one round at a time.
+REDUCED_SHAPES = {
+    "arity3": [(3, [0, 1, 2]), (5, [3, 4, 5]), (R - 7, [0, 3, 5])],
+    "mixed23": [(3, [0, 1, 2]), (5, [3, 4]), (R - 7, [1, 5]), (11, [2, 4, 5])],
+}
+
+
+@pytest.mark.parametrize("shape", sorted(REDUCED_SHAPES))
+def test_reduced_layout_rounds_nv18(gpu, cpu, oracle, shape):
+    vg, vc, _, _ = build_pair(gpu, cpu, oracle, 18, 6, REDUCED_SHAPES[shape], 91)
+    run_both(gpu, cpu, vg, vc, 18)
+
+
+@pytest.mark.parametrize("shape", sorted(REDUCED_SHAPES))
+def test_prove_rounds_reduced_layout_nv18(gpu, cpu, oracle, shape):
+    import transcript_ref as tref
+    from hyperplonk_gb300 import protocol
+    from hyperplonk_gb300.transcript import IOPTranscript
+    vg, vc, _, _ = build_pair(gpu, cpu, oracle, 18, 6, REDUCED_SHAPES[shape], 92)
+    fg, fc = [], []
+    pg = protocol.sumcheck_prove(gpu, vg, IOPTranscript(b"reduced layout"), fg)
+    pc = protocol.sumcheck_prove(cpu, vc, tref.OracleIOPTranscript(b"reduced layout"), fc)
+    assert pg.proofs == pc.proofs
+    assert pg.point == pc.point
+    assert fg == fc
+
+
 def test_repeated_factors_max_degree_34(gpu, cpu, oracle):
     nv = 6
     prods = [(3, [0] * 34), (5, [1, 0, 1]), (R - 7, [2] * 17 + [1] * 10), (9, [2])]
