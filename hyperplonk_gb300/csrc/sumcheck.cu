@@ -890,6 +890,194 @@ __global__ void __launch_bounds__(kResThreads) k_sumcheck_resident(SumcheckDesc 
     }
 }
 
+// One round over shared-memory tiles staged by bulk asynchronous copies.
+// Block b takes a contiguous range of pairs, in tiles of `tile` pairs: thread
+// 0 issues, per factor, one cp.async.bulk of the tile's source rows (4 Fr per
+// pair when the previous challenge is folded in, 2 otherwise) into one of
+// kTileStages shared-memory stages, completing on that stage's mbarrier, up
+// to kTileStages - 1 tiles ahead of the one being computed.  Each tile: the
+// fold writes the folded rows to `dst` and to a shared tile (a factor folded
+// once, whatever the number of products reading it), then one thread group
+// per slot accumulates its (slot, pair) items from shared memory into an
+// unreduced 17-limb sum.  Block slot sums go into the state's 64-bit limb
+// counters; the last block (ticket) turns them into field elements, clears
+// them and writes the message.  A stage wait that runs out (kTileWaitLimit
+// polls) makes the block skip its remaining tiles, wait (bounded) for its
+// copies still in flight and flag the launch; the last block then writes a
+// message of non-canonical bytes, which the host rejects.
+constexpr int kTileThreads = 256;
+constexpr int kTileStages = 3;
+constexpr uint32_t kTileWaitLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return uint32_t(__cvta_generic_to_shared(p)); }
+__device__ __forceinline__ void mbar_init(uint64_t *bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+    uint32_t it = 0;
+    while (!mbar_try_wait(bar, parity))
+        if (++it >= kTileWaitLimit) return false;
+    return true;
+}
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Shared memory of the tiled kernel: the barriers, kTileStages stages of raw
+// rows, the folded tile, the per-thread reduced sums.
+static size_t tiled_smem(int factors, int tile, bool fold) {
+    const size_t row = fold ? 4 : 2;
+    return 128 + (size_t(kTileStages) * factors * row * tile + size_t(factors) * 2 * tile + kTileThreads) * sizeof(Fr);
+}
+
+template <int MAXM>
+__global__ void __launch_bounds__(kTileThreads) k_sumcheck_round_tiled(SumcheckDesc desc, FrPtrList src,
+                                                                       FrMutPtrList dst, bool fold, Fr r,
+                                                                       size_t pairs, int tile, const Fr *weights,
+                                                                       int degree, Fr *out, Fr claim, bool use_claim,
+                                                                       uint64_t *limb_sums, unsigned *counter,
+                                                                       uint32_t *err) {
+    extern __shared__ __align__(128) uint8_t tile_smem[];
+    __shared__ Fr sums[kMaxSlotsV2];
+    __shared__ bool last;
+    __shared__ int bad;
+    const int F = desc.factor_count, S = desc.slot_count;
+    const int rowlen = fold ? 4 : 2;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(tile_smem);
+    Fr *raw = reinterpret_cast<Fr *>(tile_smem + 128);
+    const size_t stage_fr = size_t(F) * rowlen * tile;
+    Fr *tab = raw + kTileStages * stage_fr;  // F x 2 tile folded rows
+    Fr *red = tab + size_t(F) * 2 * tile;    // kTileThreads
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = kTileThreads / 32;
+    const int tps = kTileThreads / S;
+    const int s = int(threadIdx.x) / tps, g = int(threadIdx.x) - s * tps;
+    int begin = 0, m = 1, k = 0;
+    if (s < S) {
+        int p = 0;
+        while (p + 1 < desc.product_count && desc.slot_base[p + 1] <= s) p++;
+        begin = desc.offsets[p];
+        m = desc.offsets[p + 1] - begin;
+        k = s - desc.slot_base[p] + desc.node0[p];
+    }
+    const size_t b0 = pairs * blockIdx.x / gridDim.x, b1 = pairs * (blockIdx.x + 1) / gridDim.x;
+    const int ntiles = int((b1 - b0 + size_t(tile) - 1) / size_t(tile));
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < kTileStages; i++) mbar_init(&bar[i]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        bad = 0;
+    }
+    __syncthreads();
+    auto issue = [&](int t) {  // thread 0: the copies of tile t
+        const size_t pb = b0 + size_t(t) * tile;
+        const int np = int(min(size_t(tile), b1 - pb));
+        const int st = t % kTileStages;
+        const uint32_t bytes = uint32_t(size_t(rowlen) * np * sizeof(Fr));
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(&bar[st], bytes * uint32_t(F));
+        for (int f = 0; f < F; f++)
+            bulk_load(raw + st * stage_fr + size_t(f) * rowlen * tile, src.p[f] + size_t(rowlen) * pb, bytes,
+                      &bar[st]);
+    };
+    int issued = 0;
+    if (threadIdx.x == 0)
+        for (; issued < kTileStages - 1 && issued < ntiles; issued++) issue(issued);
+    FrAcc X;
+    acc_zero(X);
+    int t = 0;
+    for (; t < ntiles; t++) {
+        const size_t pb = b0 + size_t(t) * tile;
+        const int np = int(min(size_t(tile), b1 - pb));
+        const int st = t % kTileStages;
+        // the stage of tile t + kTileStages - 1 was last read in tile t - 1,
+        // which every thread has finished (barrier at the end of the loop)
+        if (threadIdx.x == 0 && issued < ntiles) issue(issued++);
+        if (!mbar_wait_bounded(&bar[st], uint32_t(t / kTileStages) & 1u)) bad = 1;
+        __syncthreads();
+        if (bad) break;
+        const Fr *rows = raw + st * stage_fr;
+        const Fr *tb = rows;  // unfolded: the stage holds this round's rows, 2 tile apart
+        if (fold) {
+            for (int idx = threadIdx.x; idx < F * 2 * np; idx += kTileThreads) {
+                const int f = idx / (2 * np), e = idx - f * 2 * np;
+                const Fr a0 = rows[size_t(f) * 4 * tile + 2 * e], a1 = rows[size_t(f) * 4 * tile + 2 * e + 1];
+                const Fr v = a0 + r * (a1 - a0);
+                tab[f * 2 * tile + e] = v;
+                store_fr(dst.p[f] + 2 * pb + size_t(e), v);
+            }
+            __syncthreads();
+            tb = tab;
+        }
+        if (s < S) {
+            for (int b = g; b < np; b += tps) {
+                Fr v;
+                auto factor = [&](int q) {
+                    const Fr *row = tb + desc.indices[begin + q] * 2 * tile + 2 * b;
+                    slot_step(X, v, row[0], row[1], q, m, k);
+                };
+#pragma unroll
+                for (int q = 0; q < MAXM; q++)
+                    if (q < m) factor(q);
+            }
+        }
+        __syncthreads();
+    }
+    if (bad && threadIdx.x == 0) {
+        // the copies still in flight: the timed-out tile's and those issued after it
+        for (int u = t; u < issued; u++) mbar_wait_bounded(&bar[u % kTileStages], uint32_t(u / kTileStages) & 1u);
+        atomicOr(err, 1u);
+    }
+    red[threadIdx.x] = s < S ? acc_reduce(X) : Fr::zero();
+    __syncthreads();
+    for (int sl = warp; sl < S; sl += warps) {
+        Fr a = Fr::zero();
+        for (int i = lane; i < tps; i += 32) a = a + red[sl * tps + i];
+        a = warp_sum(a);
+        if (lane == 0) sums[sl] = a;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 8 * S; i += kTileThreads)
+        atomicAdd(reinterpret_cast<unsigned long long *>(&limb_sums[i]), (unsigned long long)sums[i >> 3].v[i & 7]);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    uint64_t *lim = reinterpret_cast<uint64_t *>(red);
+    for (int i = threadIdx.x; i < 8 * S; i += kTileThreads)
+        lim[i] = atomicExch(reinterpret_cast<unsigned long long *>(&limb_sums[i]), 0ull);
+    if (threadIdx.x == 0) bad = atomicExch(err, 0u) != 0u;
+    __syncthreads();
+    if (threadIdx.x < S) sums[threadIdx.x] = fr_from_limb_sums(lim + 8 * threadIdx.x);
+    __syncthreads();
+    if (!bad) {
+        finalize_from_sums(desc, sums, weights, degree, out, use_claim ? &claim : nullptr);
+    } else if (threadIdx.x <= degree) {
+        Fr poison;
+#pragma unroll
+        for (int w = 0; w < 8; w++) poison.v[w] = 0xffffffffu;
+        out[threadIdx.x] = poison;  // not canonical: the host reading the message fails
+    }
+    if (threadIdx.x == 0) *counter = 0u;
+}
+
 __global__ void k_sumcheck_final_fold(FrPtrList tables, int count, Fr r, Fr *out) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= count) return;
@@ -924,6 +1112,7 @@ struct HpCudaSumCheckProverState {
     hp::SumcheckDesc desc_red{};
     bool red_uniform = false;  // every product of desc_red starts at node 1
     size_t weights_full = 0;   // Fr entries of the first round's matrix
+    size_t weights_red = 0;    // Fr entries of the later rounds' matrix
     // 1 / prod_{y != x} (x - y) for x = 0..max_degree: Lagrange weights of a
     // round message over the nodes 0..max_degree
     std::vector<hp::host::Fr64> lag_den;
@@ -947,10 +1136,22 @@ static unsigned *round_counter(HpCudaSumCheckProverState *s) {
     return reinterpret_cast<unsigned *>(s->weights);
 }
 
+// The state's relay words (zeroed at prover_init): [0] rounds relayed and [1]
+// abort of the resident grid, [2] the tiled kernel's error flag; the
+// resident grid's relayed challenge and claim follow at words 8 and 16.
+static uint32_t *state_relay(HpCudaSumCheckProverState *s) {
+    return reinterpret_cast<uint32_t *>(static_cast<Fr *>(s->weights) + 1);
+}
 static const Fr *state_weights(HpCudaSumCheckProverState *s) { return static_cast<const Fr *>(s->weights) + 4; }
 static const Fr *state_weights_red(HpCudaSumCheckProverState *s) {
     return static_cast<const Fr *>(s->weights) + 4 + s->weights_full;
 }
+// The tiled kernel's 8 x kMaxSlotsV2 limb counters after both matrices
+// (zeroed at prover_init, cleared again by every launch's last block).
+static uint64_t *state_tile_limbs(HpCudaSumCheckProverState *s) {
+    return reinterpret_cast<uint64_t *>(static_cast<Fr *>(s->weights) + 4 + s->weights_full + s->weights_red);
+}
+constexpr size_t kTileLimbFr = 8 * kMaxSlotsV2 * sizeof(uint64_t) / sizeof(Fr);
 
 // Stores round `round`'s message (canonical bytes) for the next round's claim.
 static void record_message(HpCudaSumCheckProverState *s, size_t round, const uint8_t *bytes) {
@@ -1159,8 +1360,10 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_create(
                 for (size_t c = 0; c < SR; c++) wr[c] = hp::host::neg(wr[SR + c]);
             s->lag_den = hp::lagrange_denominators(D);
             s->weights_full = w.size();
-            s->weights = ctx->scratch((w.size() + wr.size() + 4) * sizeof(Fr));
+            s->weights_red = wr.size();
+            s->weights = ctx->scratch((w.size() + wr.size() + 4 + hp::kTileLimbFr) * sizeof(Fr));
             check_cuda(cudaMemsetAsync(s->weights, 0, 4 * sizeof(Fr), ctx->stream));
+            check_cuda(cudaMemsetAsync(hp::state_tile_limbs(s), 0, hp::kTileLimbFr * sizeof(Fr), ctx->stream));
             check_cuda(cudaMemcpyAsync(static_cast<Fr *>(s->weights) + 4, w.data(), w.size() * sizeof(Fr),
                                        cudaMemcpyHostToDevice, ctx->stream));
             check_cuda(cudaMemcpyAsync(static_cast<Fr *>(s->weights) + 4 + w.size(), wr.data(),
@@ -1198,6 +1401,8 @@ static void check_round(HpCudaSumCheckProverState *s, const uint8_t *challenge_o
 
 static size_t wide_max_pairs();
 static size_t wide_min_pairs();
+static size_t tiled_min_pairs();
+static size_t tiled_blocks_per_sm();
 static bool product_pair_rounds();
 static bool fused_fold_pp();
 static size_t pp_min_pairs();
@@ -1242,6 +1447,7 @@ static bool route_valid(const RoundShape &sh, const RoundRoute &rt) {
         case kRouteSlot: return sh.products;
         case kRouteSlotFused: return sh.products && sh.fold && sh.all_written;
         case kRoutePp: return sh.products && sh.max_arity <= 3 && sh.slots <= kMaxSlotsV2;
+        case kRouteTiled: return sh.products && sh.regs;
         case kRoutePpFused: return sh.products && sh.max_arity <= 3 && sh.slots <= kMaxSlotsV2 && sh.fold &&
                                    sh.all_written;
         default: return false;
@@ -1252,6 +1458,8 @@ static bool route_valid(const RoundShape &sh, const RoundRoute &rt) {
 // the run-time table in the design notes override them).
 static RoundRoute default_route(const RoundShape &sh) {
     const bool small = sh.regs && sh.pairs <= size_t(kSmallPairs);
+    if (sh.products && sh.regs && tiled_min_pairs() > 0 && sh.pairs >= tiled_min_pairs())
+        return RoundRoute{kRouteTiled, uint8_t(tiled_blocks_per_sm())};
     if (sh.products && sh.pairs >= pp_min_pairs() && sh.pairs > wide_max_pairs() && sh.max_arity <= 3 &&
         sh.slots <= kMaxSlotsV2 && product_pair_rounds())
         return RoundRoute{uint8_t(sh.fold && sh.all_written && fused_fold_pp() ? kRoutePpFused : kRoutePp),
@@ -1390,6 +1598,28 @@ static void launch_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, const
             check_launch();
             break;
         }
+        case kRouteTiled: {
+            int tile = 64;
+            while (tile > 8 && tiled_smem(d.factor_count, tile, fold) > size_t(110) * 1024) tile >>= 1;
+            const size_t smem = tiled_smem(d.factor_count, tile, fold);
+            const size_t per_sm = std::max<size_t>(1, rt.per_sm);
+            const unsigned grid =
+                unsigned(std::max<size_t>(1, std::min(sms * per_sm, (pairs + size_t(tile) - 1) / size_t(tile))));
+            FrPtrList tables = src;
+            auto launch = [&](auto kernel) {
+                check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+                kernel<<<grid, kTileThreads, smem, st>>>(d, tables, dst, fold, r, pairs, tile, wts,
+                                                         int(s->max_degree), out_dev, claim, red,
+                                                         state_tile_limbs(s), round_counter(s),
+                                                         state_relay(s) + 2);
+            };
+            if (d.max_arity <= 2) launch(k_sumcheck_round_tiled<2>);
+            else if (d.max_arity <= 4) launch(k_sumcheck_round_tiled<4>);
+            else if (d.max_arity <= 6) launch(k_sumcheck_round_tiled<6>);
+            else launch(k_sumcheck_round_tiled<8>);
+            check_launch();
+            break;
+        }
         case kRouteOneBlock: {
             const size_t smem = size_t(d.slot_count) * (kSmallPairs + 1) * sizeof(Fr);
             auto launch = [&](auto kernel) {
@@ -1480,6 +1710,16 @@ static size_t pp_min_pairs() {
 }
 static bool fused_fold_pp() {
     static const bool v = env_size("HP_SUMCHECK_PP_FOLD", 0) != 0;
+    return v;
+}
+// Rounds of at least HP_SUMCHECK_TILED pairs take the tiled kernel (0: none),
+// with HP_SUMCHECK_TILED_PER_SM blocks per SM.
+static size_t tiled_min_pairs() {
+    static const size_t v = env_size("HP_SUMCHECK_TILED", 0);
+    return v;
+}
+static size_t tiled_blocks_per_sm() {
+    static const size_t v = std::max<size_t>(1, env_size("HP_SUMCHECK_TILED_PER_SM", 2));
     return v;
 }
 // Rounds above wide_max_pairs(): k_sumcheck_fold + the (slot, pair) kernel
@@ -1664,10 +1904,6 @@ static size_t resident_pairs(const HpCudaSumCheckProverState *s) {
     return d.max_arity <= 2 && d.slot_count <= 12 ? size_t(1) << 17 : size_t(1) << 15;
 }
 
-// The state's relay words for the resident grid (zeroed at prover_init).
-static uint32_t *state_relay(HpCudaSumCheckProverState *s) {
-    return reinterpret_cast<uint32_t *>(static_cast<Fr *>(s->weights) + 1);
-}
 
 // Runs rounds k0.. of `s` in one resident launch -- the cooperative grid
 // (`grid`) or the one-block tail -- with the Fiat-Shamir step of each round
@@ -1907,6 +2143,7 @@ const RoundRoute kRouteCandidates[] = {
     {kRouteOneBlock, 0}, {kRoutePerPair, 0}, {kRouteSlot, 0},      {kRouteSlot, 4},  {kRouteSlot, 8},
     {kRouteSlot, 16},    {kRouteSlot, 32},   {kRouteSlotFused, 0}, {kRouteSlotFused, 16},
     {kRoutePp, 2},       {kRoutePp, 3},      {kRoutePp, 6},        {kRoutePpFused, 3},
+    {kRouteTiled, 1},    {kRouteTiled, 2},
 };
 
 bool same_route(const RoundRoute &a, const RoundRoute &b) { return a.kernel == b.kernel && a.per_sm == b.per_sm; }

@@ -45,7 +45,8 @@ enum RouteKernel : uint8_t {
     kRouteSlotFused = 4,  // (slot, pair) items folding their own factors
     kRoutePp = 5,         // (product, pair) items, separate fold pass
     kRoutePpFused = 6,    // (product, pair) items folding their own factors
-    kRouteKinds = 7
+    kRouteTiled = 7,      // shared-memory tiles staged by bulk copies, fold + (slot, pair) items
+    kRouteKinds = 8
 };
 struct RoundRoute {
     uint8_t kernel;

@@ -429,7 +429,8 @@ HpCudaStatus hp_cuda_v1_msm_tuning_clear(void);
  * (out2 = kernel, blocks per SM) a round of `pairs` pairs of that shape
  * (fold != 0: a round after the first) would take now (kernel codes: 1 one block, 2 one pair per thread, 3
  * (slot, pair), 4 (slot, pair) with fused fold, 5 (product, pair), 6
- * (product, pair) with fused fold). */
+ * (product, pair) with fused fold, 7 shared-memory tiles staged by bulk
+ * copies). */
 typedef struct HpCudaRoundTuning {
     uint64_t pairs;
     uint32_t kernel, blocks_per_sm;
