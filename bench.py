@@ -507,8 +507,9 @@ def run_sumcheck(args, world, rank, local, pg):
          "d2h_bytes_per_step": 32 * (3 * nv + 6)}, nl, clk)
     result["roofline"] = {
         "bound": "imad",
-        "kernel": "sumcheck rounds: k_sumcheck_fold + k_sumcheck_round_wide (large and middle rounds), "
-                  "k_sumcheck_round_small (<= 64 pairs)",
+        "kernel": "sumcheck rounds: k_sumcheck_round_pp (round 1) and k_sumcheck_fold + k_sumcheck_round_pp "
+                  "(round 2, p(0) from the claim), then one k_sumcheck_resident launch for rounds 3..20 (its "
+                  "duration includes the host Merlin step of each of those rounds)",
         "achieved": imad_work / kernel_s / 1e12, "peak": imad / 1e12, "unit": "TIMAD/s",
         "frac": imad_work / kernel_s / imad, "traffic": None,
         "peak_source": "measured live: mad.lo.u32 issue rate on this GPU (libhp_probe)",
