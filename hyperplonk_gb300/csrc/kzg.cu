@@ -61,11 +61,14 @@ static void run_msms(HpCudaContext *ctx, std::vector<MsmTask> tasks, Xyzz *parts
         t.out_row = o;
         o += size_t(msm_shape(*t.layer).partials);
     }
-    const std::vector<char> binary = msm_binary_tasks(ctx, tasks.data(), tasks.size());
+    std::vector<uint64_t> ones;
+    const std::vector<char> binary = msm_binary_tasks(ctx, tasks.data(), tasks.size(), &ones);
     std::vector<MsmTask> big, small, sums;
+    std::vector<char> mostly_ones;
     for (size_t i = 0; i < tasks.size(); i++) {
         const MsmTask &t = tasks[i];
         (binary[i] ? sums : msm_runs_alone(size_t(t.layer->windows) * t.n) ? big : small).push_back(t);
+        if (binary[i]) mostly_ones.push_back(char(2 * ones[i] > t.n));
     }
     std::stable_sort(big.begin(), big.end(), [](const MsmTask &a, const MsmTask &b) { return a.n > b.n; });
     const size_t lanes = big.size() + (small.empty() ? 0 : 1) + sums.size();
@@ -73,8 +76,11 @@ static void run_msms(HpCudaContext *ctx, std::vector<MsmTask> tasks, Xyzz *parts
     ctx->fork(k);
     size_t w = 0;
     // sums of bases end in a latency-bound tree: one worker stream each, so the tails overlap
-    for (const auto &t : sums)
-        msm_run_binary(ctx, *t.layer, t.scalars, t.n, parts + t.out_row, ctx->workers[w++ % size_t(k)]);
+    for (size_t i = 0; i < sums.size(); i++) {
+        const MsmTask &t = sums[i];
+        msm_run_binary(ctx, *t.layer, t.scalars, t.n, parts + t.out_row, ctx->workers[w++ % size_t(k)],
+                       mostly_ones[i] != 0);
+    }
     if (!small.empty()) msm_run_many(ctx, small.data(), small.size(), parts, ctx->workers[w++ % size_t(k)]);
     for (const auto &t : big) msm_run(ctx, *t.layer, t.scalars, parts + t.out_row, ctx->workers[w++ % size_t(k)], t.n);
     ctx->join(k);
@@ -84,7 +90,9 @@ static void run_msms(HpCudaContext *ctx, std::vector<MsmTask> tasks, Xyzz *parts
 // every scalar is 0 or 1, else msm_run.
 static void run_one_msm(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, Xyzz *parts) {
     const MsmTask task{&layer, scalars, layer.n, 0};
-    if (msm_binary_tasks(ctx, &task, 1)[0]) msm_run_binary(ctx, layer, scalars, layer.n, parts);
+    std::vector<uint64_t> ones;
+    if (msm_binary_tasks(ctx, &task, 1, &ones)[0])
+        msm_run_binary(ctx, layer, scalars, layer.n, parts, nullptr, 2 * ones[0] > layer.n);
     else msm_run(ctx, layer, scalars, parts);
 }
 

@@ -253,6 +253,9 @@ __global__ void k_msm_to_mont(Fr *data, size_t n) {
 
 // Windows 1..W-1 from window 0 (already in layer.bases), then the randomiser
 // d and D = sum d_i P_i.
+static void msm_sum_bases(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, uint32_t want,
+                          const Xyzz *total, Xyzz *out, int rows, cudaStream_t st, size_t n = 0,
+                          const Xyzz *d_sum = nullptr);
 static void msm_finish_layer(HpCudaContext *ctx, MsmLayer &layer) {
     const size_t n = layer.n;
     if (layer.windows > 1) {
@@ -291,6 +294,9 @@ static void msm_finish_layer(HpCudaContext *ctx, MsmLayer &layer) {
     ctx->sync();
     d.y = host::fq_sub(host::Fq64{{0, 0, 0, 0, 0, 0}}, d.y);
     layer.minus_d = d;
+    // the sum of all window-0 bases, for 0/1 tables that are mostly ones
+    layer.base_sum = static_cast<Xyzz *>(ctx->scratch(sizeof(Xyzz)));
+    msm_sum_bases(ctx, layer, nullptr, 1, nullptr, layer.base_sum, 1, ctx->stream);
 }
 
 void msm_apply_tuning(MsmLayer &layer) {
@@ -365,9 +371,11 @@ void msm_release_layer(HpCudaContext *ctx, MsmLayer &layer) {
     if (layer.bases) ctx->scratch_free(layer.bases);
     if (layer.delta) ctx->scratch_free(layer.delta);
     if (layer.d_sum) ctx->scratch_free(layer.d_sum);
+    if (layer.base_sum) ctx->scratch_free(layer.base_sum);
     layer.bases = nullptr;
     layer.delta = nullptr;
     layer.d_sum = nullptr;
+    layer.base_sum = nullptr;
 }
 
 // ---------------------------------------------------------------------------
@@ -1040,29 +1048,40 @@ struct ClassifyList {
 
 // flags[t] = 1 when table t (blockIdx.y) has a scalar outside {0, 1}
 // (canonical value).  flags is host-mapped memory zeroed by the host; blocks
-// only ever store 1 there, so no atomics cross the link.
-__global__ void k_msm_classify(ClassifyList list, uint32_t *flags) {
+// only ever store 1 there, so no atomics cross the link.  ones[t] (device,
+// zeroed by the host) counts the scalars equal to 1.
+__global__ void k_msm_classify(ClassifyList list, uint32_t *flags, unsigned long long *ones) {
     const Fr *scalars = list.scalars[blockIdx.y];
     const size_t n = list.n[blockIdx.y];
-    uint32_t other = 0;
+    uint32_t other = 0, count = 0;
     for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
         const Fr c = from_mont(load_fr(&scalars[i]));
         uint32_t high = c.v[0] >> 1;
 #pragma unroll
         for (int k = 1; k < 8; k++) high |= c.v[k];
         other |= high;
+        count += c.v[0] & 1u;
     }
     if (__syncthreads_or(other != 0) && threadIdx.x == 0) flags[blockIdx.y] = 1u;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) count += __shfl_down_sync(0xffffffffu, count, off);
+    if ((threadIdx.x & 31) == 0 && count) atomicAdd(&ones[blockIdx.y], (unsigned long long)count);
 }
 
-std::vector<char> msm_binary_tasks(HpCudaContext *ctx, const MsmTask *tasks, size_t count) {
+std::vector<char> msm_binary_tasks(HpCudaContext *ctx, const MsmTask *tasks, size_t count,
+                                   std::vector<uint64_t> *ones) {
     std::vector<char> binary(count, 0);
+    if (ones) ones->assign(count, 0);
     const char *env = std::getenv("HP_MSM_BINARY");
     if (count == 0 || (env && env[0] == '0')) return binary;
+    // mailbox: the flags, then (8-byte aligned) the ones counts copied back
+    const size_t flag_bytes = (count * sizeof(uint32_t) + 7) & ~size_t(7);
     void *dev = nullptr;
-    volatile uint32_t *host =
-        reinterpret_cast<volatile uint32_t *>(ctx->mailbox(count * sizeof(uint32_t), &dev));
+    uint8_t *box = ctx->mailbox(flag_bytes + count * sizeof(uint64_t), &dev);
+    volatile uint32_t *host = reinterpret_cast<volatile uint32_t *>(box);
     for (size_t i = 0; i < count; i++) host[i] = 0;
+    Scratch counts(ctx, count * sizeof(uint64_t));
+    check_cuda(cudaMemsetAsync(counts.ptr, 0, count * sizeof(uint64_t), ctx->stream));
     for (size_t first = 0; first < count; first += kClassifyList) {
         const size_t m = std::min<size_t>(kClassifyList, count - first);
         ClassifyList list{};
@@ -1075,11 +1094,16 @@ std::vector<char> msm_binary_tasks(HpCudaContext *ctx, const MsmTask *tasks, siz
         // a memory pass over every table: about two waves of 256-thread blocks
         const unsigned x = unsigned(std::max<size_t>(
             1, std::min<size_t>((max_n + 255) / 256, (size_t(2) * ctx->sm_count * 8 + m - 1) / m)));
-        k_msm_classify<<<dim3(x, unsigned(m)), 256, 0, ctx->stream>>>(list, static_cast<uint32_t *>(dev) + first);
+        k_msm_classify<<<dim3(x, unsigned(m)), 256, 0, ctx->stream>>>(list, static_cast<uint32_t *>(dev) + first,
+                                                                      counts.as<unsigned long long>() + first);
         check_launch();
     }
+    if (ones)
+        check_cuda(cudaMemcpyAsync(box + flag_bytes, counts.ptr, count * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                                   ctx->stream));
     ctx->sync();
     for (size_t i = 0; i < count; i++) binary[i] = host[i] == 0;
+    if (ones) std::memcpy(ones->data(), box + flag_bytes, count * sizeof(uint64_t));
     return binary;
 }
 
@@ -1093,12 +1117,14 @@ constexpr int kBinaryThreads = 128;
 constexpr int kBinaryPerThread = 8;  // indices per thread below the grid cap
 
 __global__ void __launch_bounds__(kBinaryThreads, 4) k_msm_binary_blocks(const Affine *bases, const Fr *scalars,
-                                                                          size_t n, Xyzz *block_sums) {
+                                                                          size_t n, uint32_t want,
+                                                                          Xyzz *block_sums) {
     __shared__ Xyzz sm[kBinaryThreads];
     Xyzz acc = xyzz_inf();
     for (size_t i = size_t(blockIdx.x) * kBinaryThreads + threadIdx.x; i < n;
          i += size_t(gridDim.x) * kBinaryThreads) {
-        if (from_mont(load_fr(&scalars[i])).v[0] == 0) continue;  // classified: 0 or 1
+        // classified 0 or 1: the bases whose scalar is `want` (every base without scalars)
+        if (scalars && from_mont(load_fr(&scalars[i])).v[0] != want) continue;
         const Affine a = load_affine(&bases[i]);
         if (affine_is_inf(a)) continue;
         acc = xyzz_add_affine(acc, a.x, a.y);
@@ -1112,10 +1138,12 @@ __global__ void __launch_bounds__(kBinaryThreads, 4) k_msm_binary_blocks(const A
     if (threadIdx.x == 0) store_xyzz(&block_sums[blockIdx.x], sm[0]);
 }
 
-// One block: the sum of the block sums (+ D when present) into the last of
-// `rows` partial rows, infinity into the others.
+// One block: the sum of the block sums, subtracted from *total_sum when
+// given, plus D when present, into the last of `rows` partial rows;
+// infinity into the others.
 __global__ void __launch_bounds__(kBinaryThreads) k_msm_binary_final(const Xyzz *block_sums, size_t blocks,
-                                                                      const Xyzz *d_sum, int rows, Xyzz *out) {
+                                                                      const Xyzz *total_sum, const Xyzz *d_sum,
+                                                                      int rows, Xyzz *out) {
     __shared__ Xyzz sm[kBinaryThreads];
     Xyzz acc = xyzz_inf();
     for (size_t b = threadIdx.x; b < blocks; b += kBinaryThreads) acc = xyzz_add(acc, load_xyzz(&block_sums[b]));
@@ -1128,25 +1156,41 @@ __global__ void __launch_bounds__(kBinaryThreads) k_msm_binary_final(const Xyzz 
     for (int r = threadIdx.x; r < rows - 1; r += kBinaryThreads) store_xyzz(&out[r], xyzz_inf());
     if (threadIdx.x == 0) {
         Xyzz total = sm[0];
+        if (total_sum) {
+            total.y = neg(total.y);
+            total = xyzz_add(load_xyzz(total_sum), total);
+        }
         if (d_sum) total = xyzz_add(total, load_xyzz(d_sum));
         store_xyzz(&out[rows - 1], total);
     }
 }
 
-void msm_run_binary(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, size_t n, Xyzz *out_partials,
-                    cudaStream_t stream) {
-    const cudaStream_t st = stream ? stream : ctx->stream;
-    require(n >= 1 && n <= layer.n);
-    const MsmShape sh = msm_shape(layer);
+// The sum of the first n window-0 bases whose scalar is `want` (scalars
+// null: all of them), subtracted from *total when given, plus *d_sum when
+// given, into the last of `rows` rows at `out` (infinity in the others).
+static void msm_sum_bases(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, uint32_t want,
+                          const Xyzz *total, Xyzz *out, int rows, cudaStream_t st, size_t n,
+                          const Xyzz *d_sum) {
+    if (n == 0) n = layer.n;
     const size_t per_block = size_t(kBinaryThreads) * kBinaryPerThread;
     const size_t blocks = std::min<size_t>((n + per_block - 1) / per_block, size_t(4) * ctx->sm_count);
     Scratch sums(ctx, blocks * sizeof(Xyzz), st);
+    k_msm_binary_blocks<<<unsigned(blocks), kBinaryThreads, 0, st>>>(layer.bases, scalars, n, want,
+                                                                     sums.as<Xyzz>());
+    check_launch();
+    k_msm_binary_final<<<1, kBinaryThreads, 0, st>>>(sums.as<Xyzz>(), blocks, total, d_sum, rows, out);
+    check_launch();
+}
+
+void msm_run_binary(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, size_t n, Xyzz *out_partials,
+                    cudaStream_t stream, bool complement) {
+    const cudaStream_t st = stream ? stream : ctx->stream;
+    require(n >= 1 && n <= layer.n);
+    complement = complement && n == layer.n && layer.base_sum != nullptr;
+    const MsmShape sh = msm_shape(layer);
     int tok = ctx->prof_begin("msm_binary", st);
-    k_msm_binary_blocks<<<unsigned(blocks), kBinaryThreads, 0, st>>>(layer.bases, scalars, n, sums.as<Xyzz>());
-    check_launch();
-    k_msm_binary_final<<<1, kBinaryThreads, 0, st>>>(sums.as<Xyzz>(), blocks, layer.delta ? layer.d_sum : nullptr,
-                                                    sh.partials, out_partials);
-    check_launch();
+    msm_sum_bases(ctx, layer, scalars, complement ? 0u : 1u, complement ? layer.base_sum : nullptr, out_partials,
+                  sh.partials, st, n, layer.delta ? layer.d_sum : nullptr);
     ctx->prof_end(tok, st);
 }
 

@@ -31,6 +31,7 @@ struct MsmLayer {
     Fr *delta = nullptr;      // n canonical Fr < 2^254 (device), or null
     host::Xyzz64 minus_d{};   // -sum d_i P_i, added by the host finish
     Xyzz *d_sum = nullptr;    // D = sum d_i P_i (device, one point), or null
+    Xyzz *base_sum = nullptr; // sum of the n window-0 bases (device, one point)
 };
 
 // Window width for a new layer of n points: HP_MSM_WINDOW_BITS, else the
@@ -134,9 +135,13 @@ uint32_t msm_effective_chunk(size_t records, uint32_t tuned);
 // msm_run_binary writes the same partial rows msm_run would combine to (all
 // but the last at infinity, the last = the sum + D so that the host finish,
 // which adds -D, is unchanged).
-std::vector<char> msm_binary_tasks(HpCudaContext *ctx, const MsmTask *tasks, size_t count);
+// `ones`, when given, receives each task's number of scalars equal to 1.
+// With `complement` (a whole layer, n = layer.n, most scalars 1) the sum is
+// formed as the layer's base_sum minus the bases of the zero scalars.
+std::vector<char> msm_binary_tasks(HpCudaContext *ctx, const MsmTask *tasks, size_t count,
+                                   std::vector<uint64_t> *ones = nullptr);
 void msm_run_binary(HpCudaContext *ctx, const MsmLayer &layer, const Fr *scalars, size_t n, Xyzz *out_partials,
-                    cudaStream_t stream = nullptr);
+                    cudaStream_t stream = nullptr, bool complement = false);
 
 // Host: combine the partials of one MSM into a point.
 host::Xyzz64 msm_combine_host(const MsmShape &shape, const host::Xyzz64 *partials);

@@ -28,6 +28,8 @@ def binary_table(pattern: str, nv: int, seed: int) -> bytes:
         bits = [0] * (n - 1) + [1]
     elif pattern == "prod":  # a product table of the identity permutation: ones, then 0 in the last slot
         bits = [1] * (n - 1) + [0]
+    elif pattern == "mostly":  # about 90% ones: the layer's base sum minus the zeros' bases
+        bits = [int(rng.random() < 0.9) for _ in range(n)]
     else:
         bits = [rng.randrange(2) for _ in range(n)]
     return b"".join(ONE if b else ZERO for b in bits)
@@ -66,7 +68,9 @@ def params(gpu, cpu, srs, oracle):
             cpu.prepare_prover_param(nv, layers))
 
 
-@pytest.mark.parametrize("pattern", ["ones", "zeros", "last", "prod", "bits"])
+# "ones", "prod" and "mostly" (more ones than zeros over a whole layer) are
+# formed as the layer's precomputed base sum minus the bases of the zeros
+@pytest.mark.parametrize("pattern", ["ones", "zeros", "last", "prod", "mostly", "bits"])
 def test_binary_commits_match_oracle_and_take_the_sum_path(gpu, cpu, params, pattern):
     pg, pc = params
     for nv in range(0, 12):
