@@ -9,8 +9,8 @@
 // challenge_bytes = meta-AD(label) + meta-AD(u32 LE length, more) + PRF.
 // Keccak-f[1600] follows FIPS 202; its round constants and rotation offsets
 // are derived here from the spec's LFSR and (t+1)(t+2)/2 rules.
-// Host only; the transcript never touches the device (spec: the
-// Fiat-Shamir transcript stays on the host).
+// Host only: the Fiat-Shamir transcript never touches the device, as at the
+// reference's boundary (32-byte challenge in, round message out).
 #include <cstdint>
 #include <cstring>
 #include <new>
