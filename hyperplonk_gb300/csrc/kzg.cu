@@ -106,13 +106,18 @@ static void finish_msms(HpCudaContext *ctx, const Xyzz *dev, const std::vector<c
     if (total)
         check_cuda(cudaMemcpyAsync(hostp.data(), dev, total * sizeof(Xyzz), cudaMemcpyDeviceToHost, ctx->stream));
     ctx->sync();
-    // every result's Horner chain, then one inversion for all affine conversions
+    // every result's Horner chain (spread over the context's host threads),
+    // then one inversion for all affine conversions
     std::vector<host::Xyzz64> results(shapes.size());
+    std::vector<size_t> offs(shapes.size());
     size_t off = 0;
     for (size_t i = 0; i < shapes.size(); i++) {
-        results[i] = msm_result_host(*layers[i], hostp.data() + off);
+        offs[i] = off;
         off += size_t(shapes[i].partials);
     }
+    ctx->host_parallel_for(shapes.size(), [&](size_t i) {
+        results[i] = msm_result_host(*layers[i], hostp.data() + offs[i]);
+    });
     host::xyzz_to_packets(results.data(), results.size(), out97);
 }
 

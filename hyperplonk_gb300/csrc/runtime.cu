@@ -303,10 +303,110 @@ void HpCudaContext::respond_shutdown() {
     responder.reset();
 }
 
+// Jobs are handed over under `mu`: a worker takes a job's function and size
+// and marks itself busy while holding the lock, and a new job is installed
+// only while the lock is held with no worker busy, so a worker never runs
+// items of a job other than the one it took.
+struct HpCudaContext::HostPool {
+    std::vector<std::thread> threads;
+    std::mutex mu;
+    std::condition_variable cv;
+    const std::function<void(size_t)> *fn = nullptr;
+    size_t n = 0;
+    uint64_t generation = 0;
+    bool stop = false;
+    int busy = 0;                 // workers inside a job (guarded by mu)
+    std::atomic<size_t> next{0};  // next item to take
+    std::atomic<size_t> done{0};  // items finished
+    std::exception_ptr error;     // first failure (guarded by error_mu)
+    std::mutex error_mu;
+
+    void run_items(const std::function<void(size_t)> *f, size_t count) {
+        for (size_t i; (i = next.fetch_add(1)) < count;) {
+            try {
+                (*f)(i);
+            } catch (...) {
+                std::lock_guard<std::mutex> lk(error_mu);
+                if (!error) error = std::current_exception();
+            }
+            done.fetch_add(1, std::memory_order_release);
+        }
+    }
+};
+
+void HpCudaContext::host_parallel_for(size_t n, const std::function<void(size_t)> &fn) {
+    if (n == 0) return;
+    if (n == 1) {
+        fn(0);
+        return;
+    }
+    if (!host_pool) {
+        host_pool = std::make_unique<HostPool>();
+        HostPool *p = host_pool.get();
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        const unsigned workers = std::min(7u, hw > 1 ? hw - 1 : 1u);
+        for (unsigned w = 0; w < workers; w++) {
+            p->threads.emplace_back([p] {
+                uint64_t seen = 0;
+                std::unique_lock<std::mutex> lk(p->mu);
+                for (;;) {
+                    p->cv.wait(lk, [&] { return p->stop || p->generation != seen; });
+                    if (p->stop) return;
+                    seen = p->generation;
+                    const std::function<void(size_t)> *f = p->fn;
+                    const size_t count = p->n;
+                    p->busy++;
+                    lk.unlock();
+                    p->run_items(f, count);
+                    lk.lock();
+                    p->busy--;
+                }
+            });
+        }
+    }
+    HostPool *p = host_pool.get();
+    {
+        std::unique_lock<std::mutex> lk(p->mu);
+        while (p->busy != 0) {  // a worker still leaving the previous job
+            lk.unlock();
+            std::this_thread::yield();
+            lk.lock();
+        }
+        p->fn = &fn;
+        p->n = n;
+        p->next.store(0);
+        p->done.store(0);
+        p->error = nullptr;
+        p->generation++;
+    }
+    p->cv.notify_all();
+    p->run_items(&fn, n);
+    while (p->done.load(std::memory_order_acquire) < n) std::this_thread::yield();
+    std::exception_ptr e;
+    {
+        std::lock_guard<std::mutex> lk(p->error_mu);
+        e = p->error;
+    }
+    if (e) std::rethrow_exception(e);
+}
+
+void HpCudaContext::host_pool_shutdown() {
+    if (!host_pool) return;
+    {
+        std::lock_guard<std::mutex> lk(host_pool->mu);
+        host_pool->stop = true;
+    }
+    host_pool->cv.notify_all();
+    for (auto &t : host_pool->threads)
+        if (t.joinable()) t.join();
+    host_pool.reset();
+}
+
 extern "C" HpCudaStatus hp_cuda_v1_context_destroy(HpCudaContext *ctx) {
     return guard([&] {
         require(ctx != nullptr);
         ctx->respond_shutdown();
+        ctx->host_pool_shutdown();
         cudaSetDevice(ctx->device);
         if (ctx->ingress_stream) cudaStreamSynchronize(ctx->ingress_stream);
         cudaError_t first = cudaStreamSynchronize(ctx->stream);

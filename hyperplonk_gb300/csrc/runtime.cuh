@@ -178,6 +178,13 @@ struct HpCudaContext {
     // Waits for the job and rethrows its exception, if any.
     void respond_wait();
     void respond_shutdown();
+    // Host worker threads (created on first use, joined by context_destroy)
+    // for independent host work of one call: fn(i) for every i < n, spread
+    // over the pool and the calling thread; rethrows the first exception.
+    struct HostPool;
+    std::unique_ptr<HostPool> host_pool;
+    void host_parallel_for(size_t n, const std::function<void(size_t)> &fn);
+    void host_pool_shutdown();
     // Clear the device status word (stream ordered).
     void clear_flags();
     // Synchronize and return the status word.
