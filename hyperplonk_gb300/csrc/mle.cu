@@ -57,7 +57,17 @@ __global__ void k_linear_combination(Fr *out, FrPtrList polys, FrScalarList coef
             FrAcc X;
             acc_zero(X);
             if (accumulate) acc_add_shifted(X, load_fr(&out[i]));
-            for (int j = 0; j < count; j++) acc_mul_add(X, load_fr(&polys.p[j][i]), coefs.s[j]);
+            // four tables' loads in flight before their products
+            int j = 0;
+            for (; j + 4 <= count; j += 4) {
+                const Fr v0 = load_fr(&polys.p[j][i]), v1 = load_fr(&polys.p[j + 1][i]);
+                const Fr v2 = load_fr(&polys.p[j + 2][i]), v3 = load_fr(&polys.p[j + 3][i]);
+                acc_mul_add(X, v0, coefs.s[j]);
+                acc_mul_add(X, v1, coefs.s[j + 1]);
+                acc_mul_add(X, v2, coefs.s[j + 2]);
+                acc_mul_add(X, v3, coefs.s[j + 3]);
+            }
+            for (; j < count; j++) acc_mul_add(X, load_fr(&polys.p[j][i]), coefs.s[j]);
             store_fr(&out[i], acc_reduce(X));
         } else {
             Fr acc = accumulate ? load_fr(&out[i]) : Fr::zero();
@@ -664,8 +674,15 @@ __device__ __forceinline__ Fr block_sum(Fr v) {  // blockDim.x = 256; result in 
 __global__ void __launch_bounds__(256) k_dot_partials(const Fr *a, const Fr *b, size_t n, Fr *partials) {
     FrAcc X;
     acc_zero(X);
-    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
-        acc_mul_add(X, load_fr(&a[i]), load_fr(&b[i]));
+    // two elements per iteration, their loads issued before either product
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    for (; i + stride < n; i += 2 * stride) {
+        const Fr a0 = load_fr(&a[i]), b0 = load_fr(&b[i]), a1 = load_fr(&a[i + stride]), b1 = load_fr(&b[i + stride]);
+        acc_mul_add(X, a0, b0);
+        acc_mul_add(X, a1, b1);
+    }
+    if (i < n) acc_mul_add(X, load_fr(&a[i]), load_fr(&b[i]));
     Fr acc = block_sum(acc_reduce(X));
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
