@@ -129,6 +129,27 @@ __global__ void k_eq_direct(Fr *out, const Fr *r, int m) {
     }
 }
 
+// Both halves of a split eq table in one launch: blocks [0, lo_blocks) write
+// lo = eq(r[0..m_lo)), the others hi = eq(r[m_lo..m_lo + m_hi)).
+__global__ void k_eq_direct2(Fr *lo, Fr *hi, const Fr *r, int m_lo, int m_hi, unsigned lo_blocks) {
+    const bool is_lo = blockIdx.x < lo_blocks;
+    Fr *out = is_lo ? lo : hi;
+    const Fr *rr = is_lo ? r : r + m_lo;
+    const int m = is_lo ? m_lo : m_hi;
+    const unsigned b = is_lo ? blockIdx.x : blockIdx.x - lo_blocks;
+    const unsigned nb = is_lo ? lo_blocks : gridDim.x - lo_blocks;
+    const size_t n = size_t(1) << m;
+    const Fr one = Fr::one();
+    for (size_t x = b * size_t(blockDim.x) + threadIdx.x; x < n; x += size_t(nb) * blockDim.x) {
+        Fr acc = one;
+        for (int j = 0; j < m; j++) {
+            const Fr rj = rr[j];
+            acc = acc * (((x >> j) & 1) ? rj : one - rj);
+        }
+        store_fr(&out[x], acc);
+    }
+}
+
 // out[x] = lo[x & mask] * hi[x >> low_bits]
 __global__ void k_eq_outer(Fr *out, const Fr *lo, const Fr *hi, int low_bits, size_t n) {
     size_t mask = (size_t(1) << low_bits) - 1;
@@ -374,11 +395,9 @@ void build_eq(HpCudaContext *ctx, const Fr *r_dev, size_t nv, Fr *out) {
     }
     size_t low = nv / 2, high = nv - low;
     Scratch lo(ctx, table_len(low) * sizeof(Fr)), hi(ctx, table_len(high) * sizeof(Fr));
-    k_eq_direct<<<grid_for(ctx, table_len(low), 256), 256, 0, ctx->stream>>>(lo.as<Fr>(), r_dev,
-                                                                            int(low));
-    check_launch();
-    k_eq_direct<<<grid_for(ctx, table_len(high), 256), 256, 0, ctx->stream>>>(
-        hi.as<Fr>(), r_dev + low, int(high));
+    const unsigned lo_blocks = grid_for(ctx, table_len(low), 256), hi_blocks = grid_for(ctx, table_len(high), 256);
+    k_eq_direct2<<<lo_blocks + hi_blocks, 256, 0, ctx->stream>>>(lo.as<Fr>(), hi.as<Fr>(), r_dev, int(low),
+                                                                 int(high), lo_blocks);
     check_launch();
     k_eq_outer<<<grid_for(ctx, n, 256), 256, 0, ctx->stream>>>(out, lo.as<Fr>(), hi.as<Fr>(),
                                                               int(low), n);
