@@ -353,6 +353,20 @@ void fold_to_scalar(HpCudaContext *ctx, const Fr *table, size_t nv, const Fr *po
     // Ten variables per pass: block b folds entries [b 2^10, (b+1) 2^10) in
     // shared memory (one launch per ten variables instead of one per variable).
     constexpr int kTail = 10;
+    // A last coordinate b in {0, 1} fixes the top variable: the value is the
+    // MLE of the 2^(nv-1) entries from b 2^(nv-1) on at the other coordinates
+    // (folding by 0 or 1 keeps one half exactly), so those coordinates only
+    // move the table's start; one variable is left for the fold below.
+    static const Fr one = [] {
+        uint8_t c[32] = {1};
+        return host_scalar(c);
+    }();
+    while (nv > 1) {
+        const Fr &c = point[nv - 1];
+        if (std::memcmp(c.v, one.v, sizeof(Fr)) == 0) table += table_len(nv - 1);
+        else if (!c.is_zero()) break;
+        nv--;
+    }
     if (nv == 0) {
         check_cuda(cudaMemcpyAsync(dst, table, sizeof(Fr), cudaMemcpyDeviceToDevice, ctx->stream));
         return;
@@ -663,6 +677,10 @@ extern "C" HpCudaStatus hp_cuda_v1_mle_evaluate(HpCudaContext *ctx, HpCudaDevice
 
 namespace hp {
 
+struct DotRows {
+    uint32_t index[kMaxList];
+};
+
 // sum_i a[i] * b[i]: block partials (thread sums, shuffle and shared-memory
 // reduction), then one block sums the partials into out.
 __device__ __forceinline__ Fr fr_warp_sum(Fr v) {
@@ -689,8 +707,12 @@ __device__ __forceinline__ Fr block_sum(Fr v) {  // blockDim.x = 256; result in 
 }
 
 // Block partials of sum_i a[i] b[i]: each thread's products summed unreduced
-// (FrAcc), one reduction per thread.
-__global__ void __launch_bounds__(256) k_dot_partials(const Fr *a, const Fr *b, size_t n, Fr *partials) {
+// (FrAcc), one reduction per thread.  Row y of the grid takes table a.p[y]
+// against the shared b (the polynomials of one point against its eq table)
+// and writes partials[y * gridDim.x + blockIdx.x].
+__global__ void __launch_bounds__(256) k_dot_partials(FrPtrList tables, const Fr *b, size_t n, Fr *partials) {
+    const Fr *a = tables.p[blockIdx.y];
+    partials += size_t(blockIdx.y) * gridDim.x;
     FrAcc X;
     acc_zero(X);
     // two elements per iteration, their loads issued before either product
@@ -706,7 +728,10 @@ __global__ void __launch_bounds__(256) k_dot_partials(const Fr *a, const Fr *b, 
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
 
-__global__ void __launch_bounds__(256) k_sum_partials(const Fr *partials, int count, Fr *out) {
+// Block y sums row y of a [rows][count] partial matrix into out[index[y]].
+__global__ void __launch_bounds__(256) k_sum_partials(const Fr *partials, int count, Fr *out, DotRows rows) {
+    partials += size_t(blockIdx.x) * count;
+    out += rows.index[blockIdx.x];
     Fr acc = Fr::zero();
     for (int i = threadIdx.x; i < count; i += blockDim.x) acc = acc + partials[i];
     acc = block_sum(acc);
@@ -758,14 +783,23 @@ extern "C" HpCudaStatus hp_cuda_v1_mle_evaluate_many(HpCudaContext *ctx, size_t 
             check_cuda(cudaMemcpyAsync(rd.ptr, pts[k].data(), nv * sizeof(Fr), cudaMemcpyHostToDevice, ctx->stream));
             hp::build_eq(ctx, rd.as<Fr>(), nv, eq.as<Fr>());
             // a few blocks per SM: long per-thread runs amortise the reduction
+            // the group's dot products in one launch (up to 32 tables per launch)
             const unsigned grid = hp::grid_for(ctx, n, 256, 2);
-            Scratch part(ctx, size_t(grid) * sizeof(Fr));
-            for (size_t j : group) {
-                hp::k_dot_partials<<<grid, 256, 0, ctx->stream>>>(tables[j], eq.as<Fr>(), n, part.as<Fr>());
+            const size_t rows = std::min(group.size(), size_t(hp::kMaxList));
+            Scratch part(ctx, rows * grid * sizeof(Fr));
+            for (size_t g0 = 0; g0 < group.size(); g0 += hp::kMaxList) {
+                const unsigned m = unsigned(std::min(group.size() - g0, size_t(hp::kMaxList)));
+                hp::FrPtrList tl{};
+                hp::DotRows dr{};
+                for (unsigned y = 0; y < m; y++) {
+                    tl.p[y] = tables[group[g0 + y]];
+                    dr.index[y] = uint32_t(group[g0 + y]);
+                    done[group[g0 + y]] = true;
+                }
+                hp::k_dot_partials<<<dim3(grid, m), 256, 0, ctx->stream>>>(tl, eq.as<Fr>(), n, part.as<Fr>());
                 check_launch();
-                hp::k_sum_partials<<<1, 256, 0, ctx->stream>>>(part.as<Fr>(), int(grid), res.as<Fr>() + j);
+                hp::k_sum_partials<<<m, 256, 0, ctx->stream>>>(part.as<Fr>(), int(grid), res.as<Fr>(), dr);
                 check_launch();
-                done[j] = true;
             }
         }
         for (size_t k = 0; k < count; k++)

@@ -72,6 +72,22 @@ def test_evaluate(gpu, cpu, oracle, nv):
         gpu.evaluate_mle(g, pt + [1])
 
 
+@pytest.mark.parametrize("nv", [1, 2, 11, 14])
+def test_evaluate_with_boolean_last_coordinates(gpu, cpu, oracle, nv):
+    """Points whose last coordinates are 0 or 1 (the proof's (0, 1, .., 1) and
+    (r_pi, 0, .., 0) openings) start the fold at a sub-table: same values."""
+    g, c = pair(gpu, cpu, oracle, nv, 320 + nv)
+    rng = random.Random(1000 + nv)
+    points = [[0] + [1] * (nv - 1), [1] * nv, [0] * nv,
+              [rng.randrange(R) for _ in range(min(4, nv))] + [0] * max(0, nv - 4),
+              [rng.randrange(R) for _ in range(nv // 2)] + [rng.randrange(2) for _ in range(nv - nv // 2)],
+              [rng.randrange(2) for _ in range(nv - 1)] + [rng.randrange(R)]]
+    for pt in points:
+        assert gpu.evaluate_mle(g, pt) == cpu.evaluate_mle(c, pt), pt
+    many = gpu.evaluate_many([g] * len(points), points)
+    assert many == [cpu.evaluate_mle(c, pt) for pt in points]
+
+
 @pytest.mark.parametrize("nv", [1, 2, 5, 12, 13, 17])
 def test_build_eq_x_r(gpu, cpu, nv):
     rng = random.Random(40 + nv)
@@ -182,6 +198,22 @@ def test_evaluate_many_shared_points_use_eq_dot_products(gpu, oracle):
     points = [p1, p2, p1, p1, p2]
     many = gpu.evaluate_many(mles, points)
     assert many == [gpu.evaluate_mle(m, p) for m, p in zip(mles, points)]
+    cpu = oracle.CpuBackend()
+    assert many == [cpu.evaluate_mle(cpu.mle_from_evaluations(nv, t), p) for t, p in zip(tables, points)]
+
+
+def test_evaluate_many_large_shared_point_group(gpu, oracle):
+    """A point shared by more polynomials than one dot-product launch takes
+    (32): the group is split over launches, every value where it belongs."""
+    import random
+    rng = random.Random(23)
+    nv = 12
+    p1 = [rng.randrange(R) for _ in range(nv)]
+    p2 = [rng.randrange(R) for _ in range(nv)]
+    tables = [oracle.random_fr(700 + i, 1 << nv) for i in range(40)]
+    mles = [gpu.mle_from_evaluations(nv, t) for t in tables]
+    points = [p2 if i in (3, 17, 38) else p1 for i in range(40)]
+    many = gpu.evaluate_many(mles, points)
     cpu = oracle.CpuBackend()
     assert many == [cpu.evaluate_mle(cpu.mle_from_evaluations(nv, t), p) for t, p in zip(tables, points)]
 
