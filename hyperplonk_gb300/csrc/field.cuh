@@ -548,23 +548,129 @@ __device__ __forceinline__ bool is_canonical(const Field<P> &a) {
 }
 
 // a^(p-2) by square-and-multiply over the modulus bits (p is odd, > 2).
+// Modular inverse by the binary extended Euclidean algorithm (variable
+// time; the method of arkworks' Fp::inverse, Guajardo, Kumar, Paar and Pelzl
+// 2006, "Efficient software-implementation of finite fields with
+// applications to cryptography", Algorithm 16).  It runs on the Montgomery
+// representation A = aR: x1 = R^2, x2 = 0 keep x1 A = u R^2 and x2 A = v R^2
+// (mod p) through every halving and subtraction, so when u (or v) reaches 1,
+// x1 (or x2) = R^2 / (aR) = R / a, the Montgomery form of 1/a.  Each step is a
+// few limb-wide shifts, adds and subtracts: a chain of about 2 log2 p short
+// steps instead of the ~log2 p dependent multiplications of a^(p-2).  0 has no
+// inverse and returns 0 (as a^(p-2) does).  The loops are bounded: there are
+// at most log2 A + log2 p halvings and one subtraction more than halvings
+// (each difference of two odd values is even), under 4 * 32N steps in all;
+// the budget is 6 * 32N, and a budget that ran out would return 0 instead of
+// spinning.
+template <int N>
+__device__ __forceinline__ bool limbs_is_one(const uint32_t *x) {
+    uint32_t acc = x[0] ^ 1u;
+#pragma unroll
+    for (int i = 1; i < N; i++) acc |= x[i];
+    return acc == 0;
+}
+
+// x = x / 2 mod p for x < p: (x + p) / 2 when x is odd (the sum's carry is
+// the top bit of the shifted value)
+template <class P>
+__device__ __forceinline__ void limbs_half_mod(uint32_t *x) {
+    constexpr int N = P::N;
+    uint32_t top = 0;
+    if (x[0] & 1u) {
+        x[0] = add_cc(x[0], P::p(0));
+#pragma unroll
+        for (int i = 1; i < N; i++) x[i] = addc_cc(x[i], P::p(i));
+        top = addc(0u, 0u);
+    }
+#pragma unroll
+    for (int i = 0; i < N - 1; i++) x[i] = __funnelshift_r(x[i], x[i + 1], 1);
+    x[N - 1] = (x[N - 1] >> 1) | (top << 31);
+}
+
+template <int N>
+__device__ __forceinline__ void limbs_shr1(uint32_t *x) {
+#pragma unroll
+    for (int i = 0; i < N - 1; i++) x[i] = __funnelshift_r(x[i], x[i + 1], 1);
+    x[N - 1] >>= 1;
+}
+
+// x -= y; returns the borrow (1 when y > x)
+template <int N>
+__device__ __forceinline__ uint32_t limbs_sub(uint32_t *x, const uint32_t *y) {
+    x[0] = sub_cc(x[0], y[0]);
+#pragma unroll
+    for (int i = 1; i < N; i++) x[i] = subc_cc(x[i], y[i]);
+    return subc(0u, 0u) & 1u;
+}
+
+// x = x - y mod p for x, y < p
+template <class P>
+__device__ __forceinline__ void limbs_sub_mod(uint32_t *x, const uint32_t *y) {
+    constexpr int N = P::N;
+    if (limbs_sub<N>(x, y)) {
+        x[0] = add_cc(x[0], P::p(0));
+#pragma unroll
+        for (int i = 1; i < N - 1; i++) x[i] = addc_cc(x[i], P::p(i));
+        x[N - 1] = addc(x[N - 1], P::p(N - 1));
+    }
+}
+
 template <class P>
 __device__ __noinline__ Field<P> inverse(const Field<P> &a) {
     constexpr int N = P::N;
-    // exponent p - 2 with the borrow carried across limbs (Fr's low limb is 1)
-    uint32_t exp[N];
-    exp[0] = sub_cc(P::p(0), 2u);
+    uint32_t u[N], v[N], x1[N], x2[N];
 #pragma unroll
-    for (int i = 1; i < N; i++) exp[i] = subc_cc(P::p(i), 0u);
-    Field<P> acc = Field<P>::one();
-    for (int i = N - 1; i >= 0; i--) {
-        uint32_t e = exp[i];
-        for (int bit = 31; bit >= 0; bit--) {
-            acc = acc * acc;
-            if ((e >> bit) & 1) acc = acc * a;
+    for (int i = 0; i < N; i++) {
+        u[i] = a.v[i];
+        v[i] = P::p(i);
+        x1[i] = P::r2(i);
+        x2[i] = 0;
+    }
+    if (P::LAZY) {  // [0, 2p) -> [0, p)
+        uint32_t t[N];
+#pragma unroll
+        for (int i = 0; i < N; i++) t[i] = u[i];
+        if (!limbs_sub<N>(t, v)) {
+#pragma unroll
+            for (int i = 0; i < N; i++) u[i] = t[i];
         }
     }
-    return acc;
+    uint32_t nz = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++) nz |= u[i];
+    if (nz == 0) return Field<P>::zero();
+    constexpr int kBits = 32 * N;
+    int budget = 6 * kBits;
+    while (!limbs_is_one<N>(u) && !limbs_is_one<N>(v) && budget > 0) {
+        while ((u[0] & 1u) == 0 && budget > 0) {
+            limbs_shr1<N>(u);
+            limbs_half_mod<P>(x1);
+            budget--;
+        }
+        while ((v[0] & 1u) == 0 && budget > 0) {
+            limbs_shr1<N>(v);
+            limbs_half_mod<P>(x2);
+            budget--;
+        }
+        // u, v odd: the larger loses the smaller
+        uint32_t t[N];
+#pragma unroll
+        for (int i = 0; i < N; i++) t[i] = u[i];
+        if (!limbs_sub<N>(t, v)) {
+#pragma unroll
+            for (int i = 0; i < N; i++) u[i] = t[i];
+            limbs_sub_mod<P>(x1, x2);
+        } else {
+            limbs_sub<N>(v, u);
+            limbs_sub_mod<P>(x2, x1);
+        }
+        budget--;
+    }
+    Field<P> r;
+    const bool u1 = limbs_is_one<N>(u), v1 = limbs_is_one<N>(v);
+#pragma unroll
+    for (int i = 0; i < N; i++) r.v[i] = u1 ? x1[i] : v1 ? x2[i] : 0u;
+    return r;
 }
 
 // Small integer in Montgomery form.

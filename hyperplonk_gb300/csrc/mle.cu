@@ -176,24 +176,26 @@ __global__ void k_frac_products(Fr *num, Fr *den, FrPtrList fs, FrPtrList gs, in
 }
 
 // Block-level Montgomery-trick inversion: out[i] = num[i] / den[i].
-// Each thread owns kInvChunk consecutive entries; thread chunk products are
-// combined by shared-memory prefix/suffix scans so one field inversion serves
-// kInvBlock * kInvChunk entries.  Zero denominators were rejected before.
+// Thread t of block b owns the kInvChunk entries b * kInvBlock * kInvChunk +
+// k * kInvBlock + t (k = 0..kInvChunk-1: a warp's accesses are contiguous);
+// thread chunk products are combined by shared-memory prefix/suffix scans so
+// one field inversion serves kInvBlock * kInvChunk entries.  Zero
+// denominators were rejected before.
 constexpr int kInvBlock = 256;
 constexpr int kInvChunk = 8;
 
-__global__ void __launch_bounds__(kInvBlock) k_batch_div(const Fr *num, const Fr *den, Fr *out,
-                                                         size_t n) {
+__global__ void __launch_bounds__(kInvBlock) k_batch_div(const Fr *__restrict__ num, const Fr *__restrict__ den,
+                                                         Fr *__restrict__ out, size_t n) {
     __shared__ Fr pre[kInvBlock];
     __shared__ Fr suf[kInvBlock];
     __shared__ Fr total_inv;
     const int t = threadIdx.x;
-    const size_t base = (size_t(blockIdx.x) * kInvBlock + t) * kInvChunk;
+    const size_t base = size_t(blockIdx.x) * kInvBlock * kInvChunk + t;
     Fr one = Fr::one();
     // 1) local prefix products, stored in out[] as scratch
     Fr p = one;
     for (int k = 0; k < kInvChunk; k++) {
-        size_t i = base + k;
+        const size_t i = base + size_t(k) * kInvBlock;
         if (i < n) {
             store_fr(&out[i], p);
             p = p * load_fr(&den[i]);
@@ -219,11 +221,10 @@ __global__ void __launch_bounds__(kInvBlock) k_batch_div(const Fr *num, const Fr
     if (t + 1 < kInvBlock) inv = inv * suf[t + 1];
     // 4) backward pass over the chunk
     for (int k = kInvChunk - 1; k >= 0; k--) {
-        size_t i = base + k;
+        const size_t i = base + size_t(k) * kInvBlock;
         if (i < n) {
-            Fr d = load_fr(&den[i]);
-            Fr inv_i = inv * load_fr(&out[i]);
-            inv = inv * d;
+            const Fr inv_i = inv * load_fr(&out[i]);
+            inv = inv * load_fr(&den[i]);
             store_fr(&out[i], load_fr(&num[i]) * inv_i);
         }
     }
