@@ -901,6 +901,11 @@ def run_gb300(args, world, rank, local, pg):
         "gpu_launches": int(nl),
         "roofline": {"bound": "imad", "kernel": "k_msm_accumulate", "achieved": achieved, "peak": peak,
                      "unit": "TIMAD/s", "frac": achieved / peak if peak else None, "traffic": traffic,
+                     "traffic_source": ("dram__bytes_read.sum + dram__bytes_write.sum of one launch of this "
+                                        "kernel at this size from a separate ncu capture of the commit workload "
+                                        "(profiles/msm_accumulate_commit.md gives the command); not measured "
+                                        "in this run, which no profiler may attach to"
+                                        if traffic is not None else "no ncu capture at this size"),
                      "peak_source": "measured live: mad.lo.u32 issue rate on this GPU (libhp_probe)",
                      "launches": acc[1], "per_launch_ms": acc_ms_total / max(1, acc[1]),
                      "algorithmic_imad_per_launch": acc_work / max(1, acc[1])},
