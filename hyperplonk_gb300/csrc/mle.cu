@@ -819,6 +819,14 @@ extern "C" HpCudaStatus hp_cuda_v1_mle_build_eq_x_r(HpCudaContext *ctx, const ui
         hp::host_scalars_to_device(ctx, r, num_vars, rd.as<Fr>());
         OwnedBuffer buf(ctx, table_len(num_vars) * kFrBytes);
         hp::build_eq(ctx, rd.as<Fr>(), num_vars, buf.as<Fr>());
+        // the point rides with the table: a prover state over a product
+        // family sharing this factor takes the eq-factored zero-check round
+        std::vector<uint64_t> point(4 * num_vars);
+        for (size_t i = 0; i < num_vars; i++) {
+            const Fr v = hp::host_scalar(r + 32 * i);
+            std::memcpy(&point[4 * i], v.v, 32);
+        }
+        ctx->buffers.at(buf.ptr).eq_point = std::move(point);
         *out = buf.release();
     });
 }

@@ -101,6 +101,10 @@ struct HpCudaContext {
         int refs;
         bool public_handle;  // still owned by the caller (not yet retired)
         std::shared_ptr<HpCudaIngress> ingress;  // set while an asynchronous upload may still write it
+        // a table built by hp_cuda_v1_mle_build_eq_x_r: its point r (Montgomery
+        // Fr, 4 words per coordinate); tables are immutable, so the table is
+        // eq(x, r) for as long as the buffer lives
+        std::vector<uint64_t> eq_point;
     };
     std::unordered_map<void *, Buffer> buffers;
     // Asynchronous uploads: their own stream, and pinned host words that each

@@ -293,6 +293,115 @@ __global__ void HP_WIDE_BOUNDS k_sumcheck_round_wide(SumcheckDesc desc, FrPtrLis
                                use_claim ? &claim : nullptr);
 }
 
+// Zero-check rounds.  A state whose products all contain one factor exactly
+// once, that factor an eq table eq(x, r) built by hp_cuda_v1_mle_build_eq_x_r
+// (the context records its point; tables are immutable), has round
+// polynomials p(t) = eq1(t; r_i) Q(t): with the challenges c_0..c_{i-1}
+// folded in, the eq table's pair b is (a_b (1 - r_i), a_b r_i) with
+// a_b = prod_{j<i} eq1(c_j; r_j) eq(b; r_{i+1..}), so its pair sum
+// w_b = eq[2b] + eq[2b+1] is a_b and
+//     Q(t) = sum_b w_b g_b(t),
+// g the polynomial with that factor removed from every product (degree
+// d - 1).  Q needs d nodes instead of p's d + 1, and every product one
+// multiplication fewer per node (the round split of A. Gruen, "Some
+// improvements for the PIOP for ZeroCheck", IACR ePrint 2024/108, here
+// read off the folded eq table).  From round 2 on the claim
+// p(0) + p(1) = (1 - r_i) Q(0) + r_i Q(1) gives Q(0) = u + v Q(1) (u =
+// claim / (1 - r_i), v = -r_i / (1 - r_i), host-computed; not when r_i = 1).
+// The message is the same field elements as the generic kernels': p(x) =
+// (a + b x) Q(x) at x = 0..d, a = 1 - r_i, b = 2 r_i - 1, Q(x) from its
+// nodes by fixed Lagrange weights.  Items are (node, pair) as in the (slot,
+// pair) kernel; each evaluates every product at its node and accumulates
+// w_b g_b(t) unreduced; the last block finishes the round.
+struct EqRoundDesc {
+    int product_count;
+    int eq_factor;
+    uint16_t offsets[kMaxProducts + 1];  // the products without the eq factor, into indices
+    uint8_t indices[kMaxIndices];
+    uint8_t coef_kind[kMaxProducts];  // 0: c = 1, 1: c = -1, 2: c = coefs[p]
+};
+
+template <int MAXR>
+__global__ void HP_WIDE_BOUNDS k_sumcheck_round_eq(EqRoundDesc ed, FrPtrList tables, size_t pairs, int node0,
+                                                   int nodes, int blocks_per_node, const Fr *coefs, Fr *partials,
+                                                   unsigned *counter, const Fr *lag, int degree, Fr a, Fr b, Fr u,
+                                                   Fr v, Fr *out) {
+    __shared__ Fr wsum[kWideThreads / 32];
+    __shared__ Fr q[kMaxDegree + 1];
+    __shared__ bool last;
+    const int ni = int(blockIdx.x % unsigned(nodes)), blk = int(blockIdx.x / unsigned(nodes));
+    const int k = node0 + ni;
+    const Fr one = Fr::one();
+    const Fr *eqt = tables.p[ed.eq_factor];
+    FrAcc X;
+    acc_zero(X);
+    const size_t stride = size_t(blocks_per_node) * kWideThreads;
+    for (size_t pb = size_t(blk) * kWideThreads + threadIdx.x; pb < pairs; pb += stride) {
+        const Fr w = load_fr(eqt + 2 * pb) + load_fr(eqt + 2 * pb + 1);
+        Fr g = Fr::zero();
+        for (int p = 0; p < ed.product_count; p++) {
+            const int begin = ed.offsets[p], m = ed.offsets[p + 1] - begin;
+            Fr val = one;
+            auto factor = [&](int j) {
+                const Fr *t = tables.p[ed.indices[begin + j]] + 2 * pb;
+                const Fr lo = load_fr(t), hi = load_fr(t + 1);
+                Fr e = k == 0 ? lo : hi;
+                if (k >= 2) {
+                    const Fr step = hi - lo;
+                    for (int i = 1; i < k; i++) e = e + step;
+                }
+                val = j == 0 ? e : val * e;
+            };
+            if constexpr (MAXR > 0) {
+#pragma unroll
+                for (int j = 0; j < MAXR; j++)
+                    if (j < m) factor(j);
+            } else {
+                for (int j = 0; j < m; j++) factor(j);
+            }
+            const int kind = ed.coef_kind[p];
+            if (kind == 0) g = g + val;
+            else if (kind == 1) g = g - val;
+            else g = g + val * coefs[p];
+        }
+        acc_mul_add(X, w, g);
+    }
+    Fr s = acc_reduce(X);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    s = warp_sum(s);
+    if (lane == 0) wsum[warp] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        Fr t = wsum[0];
+#pragma unroll
+        for (int w2 = 1; w2 < kWideThreads / 32; w2++) t = t + wsum[w2];
+        partials[size_t(ni) * blocks_per_node + blk] = t;
+    }
+    // the last block to finish sums the partials of every node and writes p
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    for (int n = warp; n < nodes; n += kWideThreads / 32) {
+        Fr t = Fr::zero();
+        for (int j = lane; j < blocks_per_node; j += 32) t = t + load_fr_cg(&partials[size_t(n) * blocks_per_node + j]);
+        t = warp_sum(t);
+        if (lane == 0) q[node0 + n] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && node0 == 1) q[0] = u + v * q[1];
+    __syncthreads();
+    for (int x = threadIdx.x; x <= degree; x += blockDim.x) {
+        Fr qx = Fr::zero();
+        for (int j = 0; j < degree; j++) qx = qx + lag[size_t(x) * degree + j] * q[j];
+        Fr ex = a;
+        for (int i = 0; i < x; i++) ex = ex + b;
+        out[x] = from_mont(ex * qx);
+    }
+    if (threadIdx.x == 0) *counter = 0u;
+}
+
 // One thread per (product, pair) item, for the large rounds (more than
 // wide_max_pairs() pairs) of products of arity <= 3: the thread loads its
 // product's m factor rows at its pair once and evaluates all m + 1 slot
@@ -1119,6 +1228,17 @@ struct HpCudaSumCheckProverState {
     // the latest round message (Montgomery) and the round that produced it
     std::vector<hp::host::Fr64> last_msg;
     size_t last_round = SIZE_MAX;
+    // Zero-check states (k_sumcheck_round_eq): the factor that is an eq table
+    // eq(x, r) occurring once in every product (-1: none), r (Montgomery),
+    // the products without it, the largest of their arities, and a device
+    // buffer [product coefficients (Montgomery)][(max_degree + 1) x
+    // max_degree Lagrange weights of Q over the nodes 0..max_degree-1].
+    int eq_factor = -1;
+    std::vector<hp::host::Fr64> eq_r;
+    std::vector<hp::host::Fr64> eq_inv_a;  // 1 / (1 - r_i), 0 where r_i = 1
+    hp::EqRoundDesc eq_desc{};
+    int eq_max_rest = 0;
+    void *eq_buf = nullptr;
 };
 
 namespace hp {
@@ -1265,6 +1385,93 @@ static std::vector<host::Fr64> extrapolation_weights(const SumcheckDesc &d, cons
     return w;
 }
 
+// Zero-check detection at state creation: the first factor whose table
+// hp_cuda_v1_mle_build_eq_x_r built (its point rides with the buffer) and
+// whose address occurs exactly once in every product.  Fills the state's
+// eq fields and returns the host image of its device buffer (empty: no such
+// factor, or a degree below 2, where the generic rounds stay).
+static std::vector<host::Fr64> detect_eq_factor(HpCudaContext *ctx, HpCudaSumCheckProverState *s,
+                                                const HpCudaDeviceAddress *factors, const uint8_t *coefficients,
+                                                const size_t *product_offsets, const size_t *factor_indices) {
+    using host::Fr64;
+    const SumcheckDesc &d = s->desc;
+    const size_t P = size_t(d.product_count), D = s->max_degree, nv = s->num_vars;
+    if (D < 2 || P == 0) return {};
+    for (int f = 0; f < d.factor_count; f++) {
+        const auto &rec = ctx->buffers.at(factors[f]);
+        if (rec.eq_point.size() != 4 * nv) continue;
+        bool once = true;
+        for (size_t p = 0; p < P && once; p++) {
+            size_t c = 0;
+            for (size_t i = product_offsets[p]; i < product_offsets[p + 1]; i++)
+                c += factors[factor_indices[i]] == factors[f] ? 1 : 0;
+            once = c == 1;
+        }
+        if (!once) continue;
+        s->eq_factor = f;
+        s->eq_r.resize(nv);
+        for (size_t i = 0; i < nv; i++) std::memcpy(s->eq_r[i].v, &rec.eq_point[4 * i], 32);
+        // 1 / (1 - r_i) for the claim's Q(0), by one batched inversion
+        // (Montgomery's trick; a zero 1 - r_i is skipped and stays 0)
+        {
+            std::vector<Fr64> a(nv), pre(nv + 1);
+            pre[0] = host::one();
+            for (size_t i = 0; i < nv; i++) {
+                a[i] = host::add(host::one(), host::neg(s->eq_r[i]));
+                pre[i + 1] = host::is_zero(a[i]) ? pre[i] : host::mont_mul(pre[i], a[i]);
+            }
+            Fr64 inv = host::inverse(pre[nv]);
+            s->eq_inv_a.assign(nv, Fr64{{0, 0, 0, 0}});
+            for (size_t i = nv; i-- > 0;) {
+                if (host::is_zero(a[i])) continue;
+                s->eq_inv_a[i] = host::mont_mul(inv, pre[i]);
+                inv = host::mont_mul(inv, a[i]);
+            }
+        }
+        EqRoundDesc &ed = s->eq_desc;
+        ed.product_count = int(P);
+        ed.eq_factor = f;
+        std::vector<Fr64> img(P + (D + 1) * D, Fr64{{0, 0, 0, 0}});
+        const Fr64 one = host::one(), minus_one = host::neg(host::one());
+        size_t n = 0;
+        int max_rest = 0;
+        for (size_t p = 0; p < P; p++) {
+            ed.offsets[p] = uint16_t(n);
+            for (size_t i = product_offsets[p]; i < product_offsets[p + 1]; i++)
+                if (int(factor_indices[i]) != f) ed.indices[n++] = uint8_t(factor_indices[i]);
+            max_rest = std::max(max_rest, int(n - ed.offsets[p]));
+            Fr64 c;
+            if (!host::from_canonical(coefficients + 32 * p, c)) fail(HP_CUDA_STATUS_INVALID_PARAMETERS);
+            ed.coef_kind[p] = std::memcmp(&c, &one, sizeof c) == 0 ? 0 : std::memcmp(&c, &minus_one, sizeof c) == 0 ? 1 : 2;
+            img[p] = c;
+        }
+        ed.offsets[P] = uint16_t(n);
+        s->eq_max_rest = max_rest;
+        // L[x][j] = prod_{m != j} (x - m) / (j - m) over the nodes m = 0..D-1,
+        // 1 / prod_{m != j} (j - m) = (-1)^(D-1-j) / (j! (D-1-j)!): one inversion
+        auto small = [](long long k) {
+            return k >= 0 ? host::from_u64(uint64_t(k)) : host::neg(host::from_u64(uint64_t(-k)));
+        };
+        std::vector<Fr64> fact(D), inv_fact(D);
+        fact[0] = one;
+        for (size_t k = 1; k < D; k++) fact[k] = host::mont_mul(fact[k - 1], host::from_u64(uint64_t(k)));
+        inv_fact[D - 1] = host::inverse(fact[D - 1]);
+        for (size_t k = D - 1; k >= 1; k--) inv_fact[k - 1] = host::mont_mul(inv_fact[k], host::from_u64(uint64_t(k)));
+        for (size_t j = 0; j < D; j++) {
+            Fr64 inv_den = host::mont_mul(inv_fact[j], inv_fact[D - 1 - j]);
+            if ((D - 1 - j) & 1) inv_den = host::neg(inv_den);
+            for (size_t x = 0; x <= D; x++) {
+                Fr64 num = inv_den;
+                for (size_t m = 0; m < D; m++)
+                    if (m != j) num = host::mont_mul(num, small((long long)x - (long long)m));
+                img[P + x * D + j] = num;
+            }
+        }
+        return img;
+    }
+    return {};
+}
+
 static void release_state(HpCudaContext *ctx, HpCudaSumCheckProverState *s) {
     for (void *p : s->inputs) {
         try { ctx->unref(p); } catch (...) {}
@@ -1274,7 +1481,8 @@ static void release_state(HpCudaContext *ctx, HpCudaSumCheckProverState *s) {
     if (s->fold_b) ctx->scratch_free(s->fold_b);
     if (s->weights) ctx->scratch_free(s->weights);
     if (s->partials) ctx->scratch_free(s->partials);
-    s->fold_a = s->fold_b = s->weights = s->partials = nullptr;
+    if (s->eq_buf) ctx->scratch_free(s->eq_buf);
+    s->fold_a = s->fold_b = s->weights = s->partials = s->eq_buf = nullptr;
 }
 
 
@@ -1370,7 +1578,14 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_prover_state_create(
                                        wr.size() * sizeof(Fr), cudaMemcpyHostToDevice, ctx->stream));
             s->partials_bytes = hp::partials_capacity(d, ctx->sm_count);
             s->partials = ctx->scratch(s->partials_bytes);
-            ctx->sync();  // w is a pageable host vector
+            std::vector<hp::host::Fr64> eq_host = hp::detect_eq_factor(ctx, s, factors, coefficients, product_offsets,
+                                                                       factor_indices);
+            if (!eq_host.empty()) {
+                s->eq_buf = ctx->scratch(eq_host.size() * sizeof(Fr));
+                check_cuda(cudaMemcpyAsync(s->eq_buf, eq_host.data(), eq_host.size() * sizeof(Fr),
+                                           cudaMemcpyHostToDevice, ctx->stream));
+            }
+            ctx->sync();  // w and eq_host are pageable host vectors
             size_t a_len = hp::table_len(num_vars - 1);
             size_t b_len = num_vars >= 2 ? hp::table_len(num_vars - 2) : 1;
             size_t fcount = std::max(factor_count, size_t(1));
@@ -1403,6 +1618,7 @@ static size_t wide_max_pairs();
 static size_t wide_min_pairs();
 static size_t tiled_min_pairs();
 static size_t tiled_blocks_per_sm();
+static size_t eq_min_pairs();
 static bool product_pair_rounds();
 static bool fused_fold_pp();
 static size_t pp_min_pairs();
@@ -1421,6 +1637,7 @@ struct RoundShape {
     bool regs;         // arity <= 8 and <= kMaxSlotsV2 slots (per-thread kernels)
     bool all_written;  // every factor is read by some product (fused folds store it)
     bool products;     // at least one product
+    bool eq = false;   // a zero-check state (k_sumcheck_round_eq)
     int max_arity;
     int slots;
 };
@@ -1434,6 +1651,7 @@ static RoundShape round_shape(const HpCudaSumCheckProverState *s) {
     sh.all_written = true;
     for (int f = 0; f < d.factor_count; f++) sh.all_written = sh.all_written && d.writer[f] != kNoWriter;
     sh.products = d.product_count > 0;
+    sh.eq = s->eq_factor >= 0;
     sh.max_arity = d.max_arity;
     sh.slots = d.slot_count;
     return sh;
@@ -1448,6 +1666,7 @@ static bool route_valid(const RoundShape &sh, const RoundRoute &rt) {
         case kRouteSlotFused: return sh.products && sh.fold && sh.all_written;
         case kRoutePp: return sh.products && sh.max_arity <= 3 && sh.slots <= kMaxSlotsV2;
         case kRouteTiled: return sh.products && sh.regs;
+        case kRouteEq: return sh.products && sh.eq;
         case kRoutePpFused: return sh.products && sh.max_arity <= 3 && sh.slots <= kMaxSlotsV2 && sh.fold &&
                                    sh.all_written;
         default: return false;
@@ -1485,6 +1704,7 @@ static RoundRoute default_route(const RoundShape &sh) {
 // fits, else the built-in rules.
 static RoundRoute chosen_route(const RoundShape &sh) {
     RoundRoute rt;
+    if (sh.eq && sh.products && sh.pairs >= eq_min_pairs()) return RoundRoute{kRouteEq, 0};
     if (sumcheck_route_lookup(RoundKey{ceil_log2_size(sh.pairs), sh.max_arity, sh.slots, sh.fold ? 1 : 0}, rt) &&
         route_valid(sh, rt))
         return rt;
@@ -1620,6 +1840,51 @@ static void launch_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, const
             check_launch();
             break;
         }
+        case kRouteEq: {
+            FrPtrList tables = src;
+            if (fold) {
+                fold_all(ctx, d, src, dst, pairs, r, st);
+                tables = rd;
+            }
+            const int D = int(s->max_degree);
+            const host::Fr64 ri = s->eq_r[s->round];
+            const host::Fr64 a64 = host::add(host::one(), host::neg(ri));  // 1 - r_i
+            const host::Fr64 b64 = host::add(ri, host::neg(a64));          // 2 r_i - 1
+            host::Fr64 u64{{0, 0, 0, 0}}, v64{{0, 0, 0, 0}};
+            const bool use = red && !host::is_zero(a64);
+            if (use) {
+                const host::Fr64 &inv = s->eq_inv_a[s->round];
+                u64 = host::mont_mul(claim64, inv);
+                v64 = host::neg(host::mont_mul(ri, inv));
+            }
+            Fr a, b, u, v;
+            std::memcpy(a.v, a64.v, 32);
+            std::memcpy(b.v, b64.v, 32);
+            std::memcpy(u.v, u64.v, 32);
+            std::memcpy(v.v, v64.v, 32);
+            const int node0 = use ? 1 : 0, nodes = D - node0;
+            const size_t tiles = (pairs + kWideThreads - 1) / kWideThreads;
+            const size_t target = sms * big_blocks_per_sm();
+            const int bpn = int(std::max<size_t>(1, std::min(tiles, (target + size_t(nodes) - 1) / size_t(nodes))));
+            const unsigned grid = unsigned(nodes) * unsigned(bpn);
+            Scratch spill;
+            Fr *partials = round_partials(ctx, s, size_t(grid) * sizeof(Fr), spill, st);
+            const Fr *coefs = static_cast<const Fr *>(s->eq_buf);
+            const Fr *lag = coefs + s->desc.product_count;
+            const int etok = ctx->prof_begin("sumcheck_round_eq", st);
+            auto launch = [&](auto kernel) {
+                kernel<<<grid, kWideThreads, 0, st>>>(s->eq_desc, tables, pairs, node0, nodes, bpn, coefs, partials,
+                                                      round_counter(s), lag, D, a, b, u, v, out_dev);
+            };
+            if (s->eq_max_rest <= 2) launch(k_sumcheck_round_eq<2>);
+            else if (s->eq_max_rest <= 4) launch(k_sumcheck_round_eq<4>);
+            else if (s->eq_max_rest <= 6) launch(k_sumcheck_round_eq<6>);
+            else if (s->eq_max_rest <= 8) launch(k_sumcheck_round_eq<8>);
+            else launch(k_sumcheck_round_eq<0>);
+            check_launch();
+            ctx->prof_end(etok, st);
+            break;
+        }
         case kRouteOneBlock: {
             const size_t smem = size_t(d.slot_count) * (kSmallPairs + 1) * sizeof(Fr);
             auto launch = [&](auto kernel) {
@@ -1714,6 +1979,14 @@ static bool fused_fold_pp() {
 }
 // Rounds of at least HP_SUMCHECK_TILED pairs take the tiled kernel (0: none),
 // with HP_SUMCHECK_TILED_PER_SM blocks per SM.
+// Zero-check states take k_sumcheck_round_eq from rounds of this many pairs
+// up (HP_SUMCHECK_EQ_MIN_PAIRS; HP_SUMCHECK_EQ=0: never).
+static size_t eq_min_pairs() {
+    const char *off = std::getenv("HP_SUMCHECK_EQ");
+    if (off != nullptr && std::strcmp(off, "0") == 0) return SIZE_MAX;
+    return std::max<size_t>(1, env_size("HP_SUMCHECK_EQ_MIN_PAIRS", size_t(1) << 13));
+}
+
 static size_t tiled_min_pairs() {
     static const size_t v = env_size("HP_SUMCHECK_TILED", 0);
     return v;
@@ -2252,6 +2525,7 @@ extern "C" HpCudaStatus hp_cuda_v1_sumcheck_route_query(size_t pairs, int32_t ma
         sh.regs = max_arity <= 8 && slots <= kMaxSlotsV2;
         sh.all_written = true;
         sh.products = true;
+        sh.eq = false;  // the generic shape: zero-check states are recognised per state
         sh.max_arity = max_arity;
         sh.slots = slots;
         const RoundRoute rt = chosen_route(sh);

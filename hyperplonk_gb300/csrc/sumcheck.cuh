@@ -46,7 +46,8 @@ enum RouteKernel : uint8_t {
     kRoutePp = 5,         // (product, pair) items, separate fold pass
     kRoutePpFused = 6,    // (product, pair) items folding their own factors
     kRouteTiled = 7,      // shared-memory tiles staged by bulk copies, fold + (slot, pair) items
-    kRouteKinds = 8
+    kRouteEq = 8,         // zero-check states: (node, pair) items of the polynomial without its eq factor
+    kRouteKinds = 9
 };
 struct RoundRoute {
     uint8_t kernel;

@@ -66,7 +66,7 @@ def autotune(backend, prover_param, num_vars: Sequence[int], mode: int = ALONE) 
 
 
 ROUTE_KERNELS = {1: "one block", 2: "pair per thread", 3: "(slot, pair)", 4: "(slot, pair), fused fold",
-                 5: "(product, pair)", 6: "(product, pair), fused fold", 7: "bulk-copied tiles"}
+                 5: "(product, pair)", 6: "(product, pair), fused fold", 7: "bulk-copied tiles", 8: "(node, pair) without the eq factor"}
 
 
 @dataclasses.dataclass(frozen=True)

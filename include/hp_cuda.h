@@ -149,7 +149,13 @@ HpCudaStatus hp_cuda_v1_multilinear_kzg_open(
 
 /* ---- sumcheck prover (bridge.h:60-62; trait backend/src/sum_check.rs:17-38) */
 
-/* Replaces hp_ascend910b3_v1_sumcheck_prover_state_create (bridge.h:60). */
+/* Replaces hp_ascend910b3_v1_sumcheck_prover_state_create (bridge.h:60).
+ * Zero-check states: when some factor is a table that
+ * hp_cuda_v1_mle_build_eq_x_r returned (eq(x, r); tables are immutable, and
+ * the context keeps r with the buffer) and its address occurs exactly once in
+ * every product, the state's large rounds evaluate the polynomial without
+ * that factor at max_degree nodes and multiply by eq's linear factor in the
+ * current variable (the same messages; HP_SUMCHECK_EQ=0 turns it off). */
 HpCudaStatus hp_cuda_v1_sumcheck_prover_state_create(
     HpCudaContext *ctx, size_t num_vars, size_t max_degree, const HpCudaDeviceAddress *factors,
     size_t factor_count, const uint8_t *coefficients, const size_t *product_offsets,
@@ -430,7 +436,8 @@ HpCudaStatus hp_cuda_v1_msm_tuning_clear(void);
  * (fold != 0: a round after the first) would take now (kernel codes: 1 one block, 2 one pair per thread, 3
  * (slot, pair), 4 (slot, pair) with fused fold, 5 (product, pair), 6
  * (product, pair) with fused fold, 7 shared-memory tiles staged by bulk
- * copies). */
+ * copies, 8 (node, pair) items of the polynomial without its eq factor:
+ * zero-check states only, recognised per state, so never the answer here). */
 typedef struct HpCudaRoundTuning {
     uint64_t pairs;
     uint32_t kernel, blocks_per_sm;

@@ -331,7 +331,7 @@ def test_round_route_file_round_trip_and_validity(tuning, tmp_path):
     assert tuning.route(1 << 19, 2, 12) == (SLOT, 8)
 
 
-@pytest.mark.parametrize("bad", ["round 19 2 12 1 8 8 1.0", "round 19 2 12 1 0 8 1.0", "round 19 2 12 1 3 99 1.0",
+@pytest.mark.parametrize("bad", ["round 19 2 12 1 9 8 1.0", "round 19 2 12 1 0 8 1.0", "round 19 2 12 1 3 99 1.0",
                                  "round 19 0 12 1 3 8 1.0", "round 19 2 12 2 3 8 1.0", "round 19 2 12 1 3 8",
                                  "round 19 2 12 1 3 8 1.0 x"])
 def test_malformed_round_lines_are_rejected(tuning, tmp_path, bad):
