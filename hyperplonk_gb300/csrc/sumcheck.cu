@@ -321,8 +321,16 @@ struct EqRoundDesc {
     uint8_t coef_kind[kMaxProducts];  // 0: c = 1, 1: c = -1, 2: c = coefs[p]
 };
 
+// (HP_EQ_MINBLOCKS: a minimum-blocks-per-SM bound, a tuning hook; none by
+// default, ~89 registers, 5 blocks per SM)
+#ifdef HP_EQ_MINBLOCKS
+#define HP_EQ_BOUNDS __launch_bounds__(kWideThreads, HP_EQ_MINBLOCKS)
+#else
+#define HP_EQ_BOUNDS __launch_bounds__(kWideThreads)
+#endif
+
 template <int MAXR>
-__global__ void HP_WIDE_BOUNDS k_sumcheck_round_eq(EqRoundDesc ed, FrPtrList tables, size_t pairs, int node0,
+__global__ void HP_EQ_BOUNDS k_sumcheck_round_eq(EqRoundDesc ed, FrPtrList tables, size_t pairs, int node0,
                                                    int nodes, int blocks_per_node, const Fr *coefs, Fr *partials,
                                                    unsigned *counter, const Fr *lag, int degree, Fr a, Fr b, Fr u,
                                                    Fr v, Fr *out) {
@@ -1619,6 +1627,7 @@ static size_t wide_min_pairs();
 static size_t tiled_min_pairs();
 static size_t tiled_blocks_per_sm();
 static size_t eq_min_pairs();
+static size_t env_size(const char *name, size_t dflt);
 static bool product_pair_rounds();
 static bool fused_fold_pp();
 static size_t pp_min_pairs();
@@ -1864,7 +1873,7 @@ static void launch_round(HpCudaContext *ctx, HpCudaSumCheckProverState *s, const
             std::memcpy(v.v, v64.v, 32);
             const int node0 = use ? 1 : 0, nodes = D - node0;
             const size_t tiles = (pairs + kWideThreads - 1) / kWideThreads;
-            const size_t target = sms * big_blocks_per_sm();
+            const size_t target = sms * std::max<size_t>(1, env_size("HP_SUMCHECK_EQ_PER_SM", big_blocks_per_sm()));
             const int bpn = int(std::max<size_t>(1, std::min(tiles, (target + size_t(nodes) - 1) / size_t(nodes))));
             const unsigned grid = unsigned(nodes) * unsigned(bpn);
             Scratch spill;
