@@ -63,13 +63,18 @@ def build(verbose: bool = False, extra_flags: list[str] | None = None) -> pathli
     nvcc = _nvcc()
     headers = _headers()
     if extra_flags is None and os.environ.get("HP_EXTRA_NVCC_FLAGS"):
-        # tuning hook: e.g. HP_EXTRA_NVCC_FLAGS="-DHP_FQ_INLINE" (forces a full rebuild)
+        # tuning hook: e.g. HP_EXTRA_NVCC_FLAGS="-DHP_FQ_INLINE" (a changed flag set rebuilds everything)
         extra_flags = os.environ["HP_EXTRA_NVCC_FLAGS"].split()
     flags = NVCC_FLAGS + (extra_flags or [])
+    # objects built with other flags (a tuning build) are rebuilt: the flag
+    # set of the last build is kept beside the objects
+    stamp = BUILD / "flags.txt"
+    flag_text = " ".join(ARCH + flags)
+    flags_changed = not stamp.exists() or stamp.read_text() != flag_text
     jobs = []
     for src in sources():
         obj = BUILD / (src.stem + ".o")
-        if _stale(obj, src, headers) or extra_flags:
+        if _stale(obj, src, headers) or flags_changed:
             jobs.append([nvcc, *ARCH, *flags, "-c", str(src), "-o", str(obj)])
 
     def run(cmd):
@@ -87,6 +92,7 @@ def build(verbose: bool = False, extra_flags: list[str] | None = None) -> pathli
         tmp = BUILD / "libhp_cuda.so.tmp"
         run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *objs, *WRAP_FLAGS])
         os.replace(tmp, LIB)
+    stamp.write_text(flag_text)
     probe_src = PROBE_DIR / "int_probe.cu"
     if probe_src.exists() and (not PROBE_LIB.exists() or _stale(PROBE_LIB, probe_src, headers)):
         PROBE_LIB.parent.mkdir(exist_ok=True)
