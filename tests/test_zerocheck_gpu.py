@@ -64,7 +64,8 @@ def run_rounds(gpu, cpu, vg, vc, seed):
 
 
 @pytest.fixture
-def profiled(gpu):
+def profiled(gpu, monkeypatch):
+    monkeypatch.delenv("HP_SUMCHECK_EQ", raising=False)  # these tests count eq launches
     gpu.lib.hp_cuda_v1_context_profile(gpu.ctx.raw, 1)
     yield gpu
     gpu.lib.hp_cuda_v1_context_profile(gpu.ctx.raw, 0)
