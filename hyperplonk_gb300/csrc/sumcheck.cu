@@ -304,8 +304,8 @@ __global__ void HP_WIDE_BOUNDS k_sumcheck_round_wide(SumcheckDesc desc, FrPtrLis
 // g the polynomial with that factor removed from every product (degree
 // d - 1).  Q needs d nodes instead of p's d + 1, and every product one
 // multiplication fewer per node (the round split of A. Gruen, "Some
-// improvements for the PIOP for ZeroCheck", IACR ePrint 2024/108, here
-// read off the folded eq table).  From round 2 on the claim
+// improvements for the PIOP for ZeroCheck", IACR ePrint 2024, here read
+// off the folded eq table).  From round 2 on the claim
 // p(0) + p(1) = (1 - r_i) Q(0) + r_i Q(1) gives Q(0) = u + v Q(1) (u =
 // claim / (1 - r_i), v = -r_i / (1 - r_i), host-computed; not when r_i = 1).
 // The message is the same field elements as the generic kernels': p(x) =
