@@ -729,6 +729,32 @@ __global__ void __launch_bounds__(256) k_dot_partials(FrPtrList tables, const Fr
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
 
+// The same with eq(x, point) = lo[x & mask] hi[x >> low_bits] never built:
+// the grid's stride is a multiple of 2^low_bits, so a thread's entries all
+// share x & mask = l and it sums f[x] hi[x >> low_bits] (unreduced) and
+// multiplies by lo[l] once at the end.
+__global__ void __launch_bounds__(256) k_dot_split_partials(FrPtrList tables, const Fr *lo, const Fr *hi,
+                                                            int low_bits, size_t n, Fr *partials) {
+    const Fr *a = tables.p[blockIdx.y];
+    partials += size_t(blockIdx.y) * gridDim.x;
+    FrAcc X;
+    acc_zero(X);
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    const size_t first = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+    size_t i = first;
+    for (; i + stride < n; i += 2 * stride) {
+        const Fr a0 = load_fr(&a[i]), h0 = load_fr(&hi[i >> low_bits]);
+        const Fr a1 = load_fr(&a[i + stride]), h1 = load_fr(&hi[(i + stride) >> low_bits]);
+        acc_mul_add(X, a0, h0);
+        acc_mul_add(X, a1, h1);
+    }
+    if (i < n) acc_mul_add(X, load_fr(&a[i]), load_fr(&hi[i >> low_bits]));
+    Fr v = acc_reduce(X);
+    if (first < n) v = v * load_fr(&lo[first & ((size_t(1) << low_bits) - 1)]);
+    Fr acc = block_sum(v);
+    if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+}
+
 // Block y sums row y of a [rows][count] partial matrix into out[index[y]].
 __global__ void __launch_bounds__(256) k_sum_partials(const Fr *partials, int count, Fr *out, DotRows rows) {
     partials += size_t(blockIdx.x) * count;
@@ -780,14 +806,27 @@ extern "C" HpCudaStatus hp_cuda_v1_mle_evaluate_many(HpCudaContext *ctx, size_t 
                     group.push_back(j);
             if (group.size() < 2) continue;
             const size_t nv = num_vars[k], n = hp::table_len(nv);
-            Scratch rd(ctx, nv * sizeof(Fr)), eq(ctx, n * sizeof(Fr));
+            Scratch rd(ctx, nv * sizeof(Fr));
             check_cuda(cudaMemcpyAsync(rd.ptr, pts[k].data(), nv * sizeof(Fr), cudaMemcpyHostToDevice, ctx->stream));
-            hp::build_eq(ctx, rd.as<Fr>(), nv, eq.as<Fr>());
-            // a few blocks per SM: long per-thread runs amortise the reduction
+            // a few blocks per SM: long per-thread runs amortise the reduction;
             // the group's dot products in one launch (up to 32 tables per launch)
             const unsigned grid = hp::grid_for(ctx, n, 256, 2);
             const size_t rows = std::min(group.size(), size_t(hp::kMaxList));
             Scratch part(ctx, rows * grid * sizeof(Fr));
+            // eq(x, point) as its two half tables (the split of build_eq) when
+            // the grid's stride fixes every thread's low half, else in full
+            const size_t low = nv / 2, high = nv - low;
+            const bool split = nv > 12 && (size_t(grid) * 256) % hp::table_len(low) == 0;
+            Scratch eq(ctx, split ? (hp::table_len(low) + hp::table_len(high)) * sizeof(Fr) : n * sizeof(Fr));
+            if (split) {
+                const unsigned lo_blocks = hp::grid_for(ctx, hp::table_len(low), 256);
+                const unsigned hi_blocks = hp::grid_for(ctx, hp::table_len(high), 256);
+                hp::k_eq_direct2<<<lo_blocks + hi_blocks, 256, 0, ctx->stream>>>(
+                    eq.as<Fr>(), eq.as<Fr>() + hp::table_len(low), rd.as<Fr>(), int(low), int(high), lo_blocks);
+                check_launch();
+            } else {
+                hp::build_eq(ctx, rd.as<Fr>(), nv, eq.as<Fr>());
+            }
             for (size_t g0 = 0; g0 < group.size(); g0 += hp::kMaxList) {
                 const unsigned m = unsigned(std::min(group.size() - g0, size_t(hp::kMaxList)));
                 hp::FrPtrList tl{};
@@ -797,7 +836,11 @@ extern "C" HpCudaStatus hp_cuda_v1_mle_evaluate_many(HpCudaContext *ctx, size_t 
                     dr.index[y] = uint32_t(group[g0 + y]);
                     done[group[g0 + y]] = true;
                 }
-                hp::k_dot_partials<<<dim3(grid, m), 256, 0, ctx->stream>>>(tl, eq.as<Fr>(), n, part.as<Fr>());
+                if (split)
+                    hp::k_dot_split_partials<<<dim3(grid, m), 256, 0, ctx->stream>>>(
+                        tl, eq.as<Fr>(), eq.as<Fr>() + hp::table_len(low), int(low), n, part.as<Fr>());
+                else
+                    hp::k_dot_partials<<<dim3(grid, m), 256, 0, ctx->stream>>>(tl, eq.as<Fr>(), n, part.as<Fr>());
                 check_launch();
                 hp::k_sum_partials<<<m, 256, 0, ctx->stream>>>(part.as<Fr>(), int(grid), res.as<Fr>(), dr);
                 check_launch();

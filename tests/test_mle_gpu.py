@@ -202,12 +202,14 @@ def test_evaluate_many_shared_points_use_eq_dot_products(gpu, oracle):
     assert many == [cpu.evaluate_mle(cpu.mle_from_evaluations(nv, t), p) for t, p in zip(tables, points)]
 
 
-def test_evaluate_many_large_shared_point_group(gpu, oracle):
+@pytest.mark.parametrize("nv", [12, 13, 17])
+def test_evaluate_many_large_shared_point_group(gpu, oracle, nv):
     """A point shared by more polynomials than one dot-product launch takes
-    (32): the group is split over launches, every value where it belongs."""
+    (32): the group is split over launches, every value where it belongs.
+    From nv = 13 on the dot products take eq's two half tables instead of
+    the full table (nv = 17: the grid's stride spans many rows)."""
     import random
-    rng = random.Random(23)
-    nv = 12
+    rng = random.Random(23 + nv)
     p1 = [rng.randrange(R) for _ in range(nv)]
     p2 = [rng.randrange(R) for _ in range(nv)]
     tables = [oracle.random_fr(700 + i, 1 << nv) for i in range(40)]
