@@ -85,6 +85,27 @@ def test_eq_rounds_match_the_oracle(profiled, cpu, oracle, monkeypatch, shape, n
     assert eq_rounds(gpu) == (nv if min_pairs else 2)
 
 
+def test_eq_round_with_r_equal_one(profiled, cpu, oracle, monkeypatch):
+    """r_2 = 1: round 2's Q(0) cannot come from the claim (1 - r_2 = 0) and
+    the kernel evaluates it; the other rounds take the claim."""
+    gpu = profiled
+    monkeypatch.setenv("HP_SUMCHECK_EQ_MIN_PAIRS", "1")
+    nv = 8
+    rng = random.Random(77)
+    r = [rng.randrange(R) for _ in range(nv)]
+    r[1] = 1
+    tables = [oracle.random_fr(300 + j, 1 << nv) for j in range(N_MLES["gate"])]
+    gm = [gpu.mle_from_evaluations(nv, t) for t in tables]
+    cm = [cpu.mle_from_evaluations(nv, t) for t in tables]
+    ge, ce = gpu.build_eq_x_r(r), cpu.build_eq_x_r(r)
+    vg, vc = VirtualPolynomial(nv), VirtualPolynomial(nv)
+    for coef, ix in SHAPES["gate"]:
+        vg.add_mle_list([ge if i == "e" else gm[i] for i in ix], coef)
+        vc.add_mle_list([ce if i == "e" else cm[i] for i in ix], coef)
+    run_rounds(gpu, cpu, vg, vc, 8)
+    assert eq_rounds(gpu) == nv
+
+
 @pytest.mark.parametrize("variant", ["eq_twice", "eq_plain"])
 def test_other_eq_uses_stay_generic(profiled, cpu, oracle, monkeypatch, variant):
     """eq twice in one product, or an eq table uploaded as a plain table (no
