@@ -377,3 +377,13 @@ def test_sumcheck_autotune_then_rounds_equal_oracle(gpu, cpu, oracle, tuning, ar
         assert gpu.prove_round_and_update_state(sg, ch) == cpu.prove_round_and_update_state(sc, ch), k
         ch = rng.randrange(R)
     assert gpu.final_evaluations(sg, ch) == cpu.final_evaluations(sc, ch)
+
+
+def test_route_kernel_names_cover_every_route_code():
+    """tuning.ROUTE_KERNELS names every route code csrc/sumcheck.cuh defines
+    (1 .. kRouteKinds - 1), so tuner records always print a kernel name."""
+    import re
+    from hyperplonk_gb300 import tuning as tn
+    text = (pathlib.Path(__file__).resolve().parent.parent / "hyperplonk_gb300" / "csrc" / "sumcheck.cuh").read_text()
+    kinds = int(re.search(r"kRouteKinds\s*=\s*(\d+)", text).group(1))
+    assert sorted(tn.ROUTE_KERNELS) == list(range(1, kinds))
